@@ -1,0 +1,179 @@
+/*
+ * xrdt.h -- C ABI of the GB300 XRD-tomography projector library (libxrdt.so).
+ *
+ * The library replaces the `Forward_XRD` MEX call of the reference
+ * (Forward_XRD.cu:76-301, a mexcuda build of Forward_projector_kernels/*.cu).
+ * Every entry point takes plain pointers and sizes; no C++ or torch types
+ * cross this boundary.  All array arguments keep the reference's
+ * column-major layouts (first index fastest), so a MATLAB / Python / C
+ * caller can hand over the very buffers it would have passed to
+ * Forward_XRD.
+ *
+ * Pointers may be host or device memory: every array pointer is classified
+ * with cudaPointerGetAttributes and host arrays are staged through device
+ * buffers owned by the context.  Calls return an xrdt_status code and never
+ * throw; a human-readable reason for the last failure is available from
+ * xrdt_last_error().
+ *
+ * Compile-time constants of the reference (Forward_XRD.cu:16-53) and the
+ * hard-coded scanner (integrate_diffraction.cu:81-143) are runtime fields
+ * of xrdt_problem.  xrdt_problem_reference() fills in exactly the values
+ * the reference compiles with.
+ */
+#ifndef XRDT_H
+#define XRDT_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define XRDT_ABI_VERSION 1
+
+/* Status codes.  The reference checks no CUDA errors at all
+ * (Forward_XRD.cu:210-259); every failure here is reported instead. */
+typedef enum xrdt_status {
+    XRDT_OK = 0,
+    XRDT_ERR_NULL = 1,        /* a required pointer is NULL                    */
+    XRDT_ERR_DIMS = 2,        /* a dimension is out of the supported range     */
+    XRDT_ERR_GEOMETRY = 3,    /* a source or detector lies inside the phantom  */
+    XRDT_ERR_INPUT = 4,       /* bad input values (material id > n_mat, ...)  */
+    XRDT_ERR_CUDA = 5,        /* a CUDA runtime call failed                    */
+    XRDT_ERR_ALLOC = 6,       /* device or pinned allocation failed            */
+    XRDT_ERR_UNSUPPORTED = 7, /* a flag combination that is not implemented    */
+    XRDT_ERR_TIMEOUT = 8      /* a bounded device wait gave up                 */
+} xrdt_status;
+
+/* Bits of xrdt_problem.quirks: behaviours of the reference kernel that are
+ * reproduced on request. */
+/* integrate_diffraction.cu:181 samples the (a1,a2) map at the coordinates of
+ * the PREVIOUS non-empty voxel (Rvox_x/Rvox_y are assigned only at :192-193,
+ * after the fetch); the first non-empty voxel reads them uninitialised.  With
+ * this bit set the Compton term uses that stale sample, with (0,0) as the
+ * first coordinates; with it clear it uses the current voxel's own value. */
+#define XRDT_QUIRK_STALE_VOXEL_A 0x1u
+
+/* Problem description: dimensions, grids, physics constants and scanner
+ * geometry.  Lengths are in voxel units (the voxel side is geom vox_side).
+ * Field names follow the reference's identifiers. */
+typedef struct xrdt_problem {
+    int32_t nx, ny;           /* phantom voxels (Forward_XRD.cu:117-119)          */
+    int32_t n_src;            /* SRC: source positions (Forward_XRD.cu:17)        */
+    int32_t n_col, n_row;     /* COL, ROW: detector pixels (Forward_XRD.cu:18-20) */
+    int32_t nrg_src;          /* source energy bins (rows of the spectrum matrix) */
+    int32_t nrg_det;          /* NRG: detector energy bins (Forward_XRD.cu:21)    */
+    int32_t dnrg;             /* DNRG: window half-width (Forward_XRD.cu:22)      */
+    int32_t nwt;              /* NWT: coarse q bins of the model matrix (:23)     */
+    int32_t nqf;              /* NQF: fine q bins of Ifine (:24)                  */
+    int32_t n_mat;            /* MAT: materials (:25)                             */
+    int32_t nq, na;           /* NQ, NA: Compton table size (:47-48)              */
+    uint32_t quirks;          /* XRDT_QUIRK_* bits                                */
+    int32_t reserved0;        /* must be 0                                        */
+
+    /* Energy grids in keV (integrate_diffraction.cu:138-142): bin i of a grid
+     * spans [e_min + i*dE, e_min + (i+1)*dE], dE = (e_max - e_min)/bins. */
+    double e_src_min, e_src_max;
+    double e_det_min, e_det_max;
+
+    /* q grids in 1/Angstrom (Forward_XRD.cu:39-42; wvt_value.cu:8-22). */
+    double q_lo;              /* qmin */
+    double q_hi;              /* qmax */
+    double dq0;               /* first coarse bin width */
+
+    /* Physics constants (Forward_XRD.cu:34-36,44,51-53; integrate_diffraction.cu:278). */
+    double hbarc;             /* keV*Angstrom */
+    double mec2;              /* electron rest energy, keV */
+    double kn0, kn1, kn2;     /* Klein-Nishina^-1 quadratic fit */
+    double rsqrt2pi;          /* 1/sqrt(2 pi) as the reference rounds it */
+    double dq_step;           /* DQ: line-integral step in voxels */
+
+    /* Scanner geometry (integrate_diffraction.cu:81-128), voxel units. */
+    double cx, cy;            /* rotation centre (Lx/2, Ly/2)                     */
+    double r_src, r_det;      /* source / detector trajectory radii              */
+    double src_arc;           /* angle spanned by n_src sources (2 pi)           */
+    double src_phi0;          /* angle of source 0                               */
+    double col_pitch, row_pitch, z0;
+    double focal_spot;        /* focal spot size                                 */
+    double target_angle;      /* anode target angle, rad                         */
+    double wedge_angle;       /* geomphi: fan wedge opening, rad                 */
+    double vox_side;          /* geomdvox                                        */
+} xrdt_problem;
+
+/* Opaque per-stream context: device buffers, staging, cached tables. */
+typedef struct xrdt_ctx xrdt_ctx;
+
+/* Flags of xrdt_forward. */
+#define XRDT_FWD_PLAIN_FP64 0x1u  /* run the FP64 kernel at the reference's launch
+                                     shape (one block per ray, NWT threads) */
+#define XRDT_FWD_NO_SYNC    0x2u  /* return without synchronising the stream; only
+                                     valid when every array is device memory */
+
+/* ---- library ---------------------------------------------------------- */
+int32_t xrdt_abi_version(void);
+const char *xrdt_status_string(int32_t status);
+
+/* ---- problem ---------------------------------------------------------- */
+/* Fills *p with the values Forward_XRD.cu compiles with (SRC=32, COL=1024,
+ * ROW=1, NRG=64, DNRG=5, NWT=256, NQF=768, MAT=3, NQ=NA=64; Forward_XRD.cu:16-53)
+ * and the scanner of integrate_diffraction.cu:81-143 scaled by NX/100, for an
+ * nx x ny phantom.  quirks = XRDT_QUIRK_STALE_VOXEL_A. */
+int32_t xrdt_problem_reference(xrdt_problem *p, int32_t nx, int32_t ny);
+/* Checks dimensions and geometry; XRDT_OK or the first violated rule. */
+int32_t xrdt_problem_validate(const xrdt_problem *p);
+/* Element counts of the outputs: rays = n_src*n_col*n_row*nrg_det and
+ * amatrix = nwt*n_mat*rays (Forward_XRD.cu:143,160). */
+int64_t xrdt_problem_rays(const xrdt_problem *p);
+int64_t xrdt_problem_amatrix_elems(const xrdt_problem *p);
+
+/* ---- context ---------------------------------------------------------- */
+/* stream: a cudaStream_t, or NULL for a stream the context creates. */
+int32_t xrdt_ctx_create(xrdt_ctx **ctx, int32_t device, void *stream);
+int32_t xrdt_ctx_destroy(xrdt_ctx *ctx);
+int32_t xrdt_ctx_synchronize(xrdt_ctx *ctx);
+const char *xrdt_last_error(const xrdt_ctx *ctx);
+/* Number of kernels this context has launched since creation. */
+int64_t xrdt_ctx_launch_count(const xrdt_ctx *ctx);
+
+/* ---- forward projector (replaces mexFunction, Forward_XRD.cu:76-301) -- */
+/* Inputs in the order of Forward_XRD's prhs[0..9] (Forward_XRD.cu:82-110):
+ *   spectrum  f32 [nrg_src, nrg_det]   detector-smeared source spectrum
+ *   Ifine     f32 [nqf * n_mat]        fine-grid XRD pattern per material
+ *   seg       i32 [nx, ny]             material id, 1-based, 0 = empty
+ *   a1, a2    f32 [nx, ny]             photoelectric / Compton coefficients, 1/voxel
+ *   S2        f32 [nq, na]             Compton table scaled to 0..255
+ *   q_min, q_max, a_min, a_max         log2 edges of the S2 table axes
+ * Outputs (plhs[0..2], Forward_XRD.cu:142-166), caller-owned, fully written:
+ *   Nphotons  f32 [n_src, n_col, n_row, nrg_det]   coherent (XRD) counts
+ *   Cphotons  f32 [n_src, n_col, n_row, nrg_det]   Compton counts (unscaled)
+ *   Amatrix   f32 [nwt, n_mat, n_src, n_col, n_row, nrg_det]  model matrix,
+ *             or NULL to skip it.
+ * Returns XRDT_ERR_INPUT if a segmentation value exceeds n_mat. */
+int32_t xrdt_forward(xrdt_ctx *ctx, const xrdt_problem *p,
+                     const float *spectrum, const float *Ifine,
+                     const int32_t *seg, const float *a1, const float *a2,
+                     const float *S2,
+                     float q_min, float q_max, float a_min, float a_max,
+                     float *Nphotons, float *Cphotons, float *Amatrix,
+                     uint32_t flags);
+
+/* Forward projection of selected rays only.  rays[i] is the linear output
+ * index src + det*n_src + nrg*n_src*n_det of Forward_XRD's outputs
+ * (integrate_diffraction.cu:404).  Nphotons[i], Cphotons[i] and the model-matrix
+ * row A_rows[i][n_mat][nwt] (or NULL) receive what xrdt_forward writes at that
+ * index.  No counterpart in the reference, which always computes every ray;
+ * used to time and check rays of workloads too large for the FP64 paths. */
+int32_t xrdt_forward_rays(xrdt_ctx *ctx, const xrdt_problem *p,
+                          const float *spectrum, const float *Ifine,
+                          const int32_t *seg, const float *a1, const float *a2,
+                          const float *S2,
+                          float q_min, float q_max, float a_min, float a_max,
+                          const int64_t *rays, int64_t n_rays,
+                          float *Nphotons, float *Cphotons, float *A_rows,
+                          uint32_t flags);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* XRDT_H */

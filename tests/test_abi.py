@@ -1,0 +1,89 @@
+"""The C ABI library: load, exports, presets and validation (CPU only; no
+compute call runs without a GPU)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import xrd_tomography_gb300 as xt
+from xrd_tomography_gb300 import synth
+from xrd_tomography_gb300.api import SIGNATURES
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "xrdt.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(xrdt_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = xt.lib()
+    names = header_functions()
+    assert len(names) >= 10
+    for n in names:
+        assert hasattr(L, n), n
+    assert set(names) == set(SIGNATURES), "ctypes signatures and header diverge"
+
+
+def test_abi_version():
+    assert xt.lib().xrdt_abi_version() == 1
+
+
+def test_problem_struct_layout_matches_c():
+    # the C preset and the Python preset agree byte for byte
+    for nx, ny in ((100, 100), (16, 16), (20, 12)):
+        assert bytes(xt.c_reference_problem(nx, ny)) == bytes(xt.reference_problem(nx, ny))
+
+
+def test_problem_counts():
+    p = xt.reference_problem(100)
+    L = xt.lib()
+    assert L.xrdt_problem_rays(ctypes.byref(p)) == 32 * 1024 * 64 == p.rays
+    assert L.xrdt_problem_amatrix_elems(ctypes.byref(p)) == 256 * 3 * 32 * 1024 * 64
+
+
+@pytest.mark.parametrize("index", [0, 1, 2, 4])
+def test_configs_validate(index):
+    assert xt.validate(synth.config_problem(index)) == 0
+
+
+def test_validation_rejects_bad_problems():
+    p = xt.reference_problem(16)
+    assert xt.validate(p) == 0
+    assert xt.validate(p.copy(nx=0)) == 2
+    assert xt.validate(p.copy(nrg_src=10)) == 2          # narrower than the 11-bin window
+    assert xt.validate(p.copy(reserved0=1)) == 2
+    assert xt.validate(p.copy(quirks=0x80)) == 2
+    assert xt.validate(p.copy(dq_step=0.0)) == 2
+    assert xt.validate(p.copy(q_hi=float("nan"))) == 2
+    # a source on the phantom's edge, a detector panel through the phantom
+    assert xt.validate(p.copy(r_src=5.0)) == 3
+    assert xt.validate(p.copy(r_det=3.0)) == 3
+    assert xt.lib().xrdt_problem_validate(None) == 1
+
+
+def test_status_strings():
+    L = xt.lib()
+    for s in range(0, 9):
+        assert L.xrdt_status_string(s)
+
+
+def test_null_arguments_are_reported():
+    L = xt.lib()
+    assert L.xrdt_ctx_create(None, 0, None) == 1
+    assert L.xrdt_ctx_destroy(None) == 1
+    assert L.xrdt_forward(None, None, *([None] * 6), 0.0, 0.0, 0.0, 0.0, None, None, None, 0) == 1
+
+
+def test_no_silent_cpu_path_without_gpu():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    # without a GPU the context cannot be created: the library reports it and
+    # the Python front end raises rather than computing anything on the CPU
+    with pytest.raises(xt.XrdtError):
+        xt.Context(0)

@@ -1,0 +1,221 @@
+"""Python front end of libxrdt.so, mirroring the reference's MEX interface.
+
+`Forward_XRD(spectrum, Ifine, seg, a1, a2, S2, q_min, q_max, a_min, a_max)`
+takes the ten arguments of the MATLAB call (main.m:56-64, Forward_XRD.cu:82-110)
+and returns (Nphotons, Cphotons, Amatrix) shaped [SRC, COL, ROW, NRG] and
+[NWT, MAT, SRC, COL, ROW, NRG] in column-major order, as
+mxGPUCreateGPUArray lays them out (Forward_XRD.cu:143-166).
+
+Arrays may be numpy arrays (host memory) or torch tensors on the GPU; the
+library decides per pointer.  There is no CPU fallback: if libxrdt.so is
+missing or fails to load, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .problem import Problem, reference_problem
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libxrdt.so")
+
+FWD_PLAIN_FP64 = 0x1
+FWD_NO_SYNC = 0x2
+
+_P = ctypes.POINTER(Problem)
+_vp = ctypes.c_void_p
+
+# name -> (restype, argtypes); must match include/xrdt.h
+SIGNATURES = {
+    "xrdt_abi_version": (ctypes.c_int32, []),
+    "xrdt_status_string": (ctypes.c_char_p, [ctypes.c_int32]),
+    "xrdt_problem_reference": (ctypes.c_int32, [_P, ctypes.c_int32, ctypes.c_int32]),
+    "xrdt_problem_validate": (ctypes.c_int32, [_P]),
+    "xrdt_problem_rays": (ctypes.c_int64, [_P]),
+    "xrdt_problem_amatrix_elems": (ctypes.c_int64, [_P]),
+    "xrdt_ctx_create": (ctypes.c_int32, [ctypes.POINTER(_vp), ctypes.c_int32, _vp]),
+    "xrdt_ctx_destroy": (ctypes.c_int32, [_vp]),
+    "xrdt_ctx_synchronize": (ctypes.c_int32, [_vp]),
+    "xrdt_last_error": (ctypes.c_char_p, [_vp]),
+    "xrdt_ctx_launch_count": (ctypes.c_int64, [_vp]),
+    "xrdt_forward": (ctypes.c_int32, [_vp, _P, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_float, ctypes.c_float,
+                                      ctypes.c_float, ctypes.c_float, _vp, _vp, _vp, ctypes.c_uint32]),
+    "xrdt_forward_rays": (ctypes.c_int32, [_vp, _P, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_float,
+                                           ctypes.c_float, ctypes.c_float, ctypes.c_float, _vp, ctypes.c_int64,
+                                           _vp, _vp, _vp, ctypes.c_uint32]),
+}
+
+
+class XrdtError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"xrdt status {status}: {msg}")
+        self.status = status
+
+
+_lib = None
+
+
+def lib():
+    """Loads libxrdt.so (building it first if the CUDA toolkit is present)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            from . import build
+            build.build()
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(rc: int, ctx=None):
+    if rc != 0:
+        msg = ""
+        if ctx is not None:
+            msg = (lib().xrdt_last_error(ctx) or b"").decode()
+        if not msg:
+            msg = lib().xrdt_status_string(rc).decode()
+        raise XrdtError(rc, msg)
+
+
+def c_reference_problem(nx: int, ny: int | None = None) -> Problem:
+    p = Problem()
+    _check(lib().xrdt_problem_reference(ctypes.byref(p), nx, nx if ny is None else ny))
+    return p
+
+
+def validate(p: Problem) -> int:
+    return lib().xrdt_problem_validate(ctypes.byref(p))
+
+
+class Context:
+    """An xrdt_ctx bound to one device and stream (stream=None: its own)."""
+
+    def __init__(self, device: int = 0, stream: int | None = None):
+        h = _vp()
+        _check(lib().xrdt_ctx_create(ctypes.byref(h), device, _vp(stream) if stream else None))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().xrdt_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):  # pragma: no cover - interpreter shutdown order
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def synchronize(self):
+        _check(lib().xrdt_ctx_synchronize(self.h), self.h)
+
+    @property
+    def launches(self) -> int:
+        return int(lib().xrdt_ctx_launch_count(self.h))
+
+    def last_error(self) -> str:
+        return (lib().xrdt_last_error(self.h) or b"").decode()
+
+
+_default_ctx = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+def _ptr(a, dtype):
+    """Device or host address of a torch tensor / numpy array (kept alive by caller)."""
+    if a is None:
+        return None, None
+    if hasattr(a, "data_ptr"):  # torch tensor
+        if not a.is_contiguous():
+            raise ValueError("tensors must be contiguous")
+        return a.data_ptr(), a
+    arr = np.ascontiguousarray(a, dtype=dtype)
+    return arr.ctypes.data, arr
+
+
+def forward(p: Problem, spectrum, Ifine, seg, a1, a2, S2, q_min, q_max, a_min, a_max,
+            Nphotons=None, Cphotons=None, Amatrix=None, want_amatrix: bool = True,
+            plain: bool = False, ctx: Context | None = None, flags: int = 0):
+    """xrdt_forward.  Outputs default to new numpy arrays (host staging by
+    the library); pass torch CUDA tensors to keep everything on the device.
+    Returns (Nphotons, Cphotons, Amatrix-or-None) as flat arrays."""
+    ctx = ctx or default_context()
+    rays = p.rays
+    if Nphotons is None:
+        Nphotons = np.empty(rays, np.float32)
+    if Cphotons is None:
+        Cphotons = np.empty(rays, np.float32)
+    if Amatrix is None and want_amatrix:
+        Amatrix = np.empty(p.amatrix_elems, np.float32)
+    keep = []
+    ptrs = []
+    for a, dt in ((spectrum, np.float32), (Ifine, np.float32), (seg, np.int32), (a1, np.float32),
+                  (a2, np.float32), (S2, np.float32), (Nphotons, np.float32), (Cphotons, np.float32),
+                  (Amatrix, np.float32)):
+        pt, k = _ptr(a, dt)
+        ptrs.append(pt)
+        keep.append(k)
+    fl = flags | (FWD_PLAIN_FP64 if plain else 0)
+    rc = lib().xrdt_forward(ctx.h, ctypes.byref(p), ptrs[0], ptrs[1], ptrs[2], ptrs[3], ptrs[4], ptrs[5],
+                            float(q_min), float(q_max), float(a_min), float(a_max),
+                            ptrs[6], ptrs[7], ptrs[8], fl)
+    _check(rc, ctx.h)
+    return keep[6], keep[7], keep[8]
+
+
+def forward_rays(p: Problem, rays, spectrum, Ifine, seg, a1, a2, S2, q_min, q_max, a_min, a_max,
+                 want_amatrix: bool = False, plain: bool = False, ctx: Context | None = None):
+    """xrdt_forward_rays: (N[n], C[n], A_rows[n, n_mat, nwt] or None) for the
+    listed linear ray indices."""
+    ctx = ctx or default_context()
+    rays = np.ascontiguousarray(rays, np.int64)
+    n = rays.size
+    N = np.empty(n, np.float32)
+    C = np.empty(n, np.float32)
+    A = np.empty((n, p.n_mat, p.nwt), np.float32) if want_amatrix else None
+    keep = []
+    ptrs = []
+    for a, dt in ((spectrum, np.float32), (Ifine, np.float32), (seg, np.int32), (a1, np.float32),
+                  (a2, np.float32), (S2, np.float32)):
+        pt, k = _ptr(a, dt)
+        ptrs.append(pt)
+        keep.append(k)
+    rc = lib().xrdt_forward_rays(ctx.h, ctypes.byref(p), *ptrs, float(q_min), float(q_max), float(a_min),
+                                 float(a_max), rays.ctypes.data, n, N.ctypes.data, C.ctypes.data,
+                                 A.ctypes.data if A is not None else None, FWD_PLAIN_FP64 if plain else 0)
+    _check(rc, ctx.h)
+    return N, C, A
+
+
+def Forward_XRD(spectrum, Ifine, segmentation, a1, a2, S2, q_min, q_max, a_min, a_max,
+                problem: Problem | None = None, ctx: Context | None = None):
+    """Drop-in for the MEX call of main.m:56-64.
+
+    Without `problem`, uses the reference's compiled configuration for the
+    phantom size of `segmentation` (a 2-D [NX, NY] array).  Returns numpy
+    arrays shaped like the MATLAB outputs (column-major)."""
+    seg = np.asarray(segmentation)
+    if problem is None:
+        if seg.ndim != 2:
+            raise ValueError("segmentation must be a 2-D [NX, NY] array")
+        problem = reference_problem(seg.shape[0], seg.shape[1])
+    flat = lambda x: np.asarray(x).reshape(-1, order="F")  # noqa: E731
+    N, C, A = forward(problem, flat(spectrum), flat(Ifine), flat(seg).astype(np.int32), flat(a1), flat(a2),
+                      flat(S2), q_min, q_max, a_min, a_max, ctx=ctx)
+    p = problem
+    shp = (p.n_src, p.n_col, p.n_row, p.nrg_det)
+    return (N.reshape(shp, order="F"), C.reshape(shp, order="F"),
+            A.reshape((p.nwt, p.n_mat) + shp, order="F"))

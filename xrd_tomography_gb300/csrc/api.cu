@@ -1,0 +1,688 @@
+// api.cu -- the C ABI of libxrdt.so (include/xrdt.h).
+//
+// Host side of the drop-in for mexFunction (Forward_XRD.cu:76-301): input
+// validation, staging of host arrays, the per-call tables that the reference
+// derives inside every block, and the kernel sequence.  The reference checks
+// no CUDA error (Forward_XRD.cu:210-259); here every call is checked and
+// reported through xrdt_status and xrdt_last_error.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "xrdt_device.cuh"
+
+using namespace xrdt;
+
+struct xrdt_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string err;
+    int64_t launches = 0;
+    // grow-only device buffers, one per slot
+    std::vector<void *> buf;
+    std::vector<size_t> cap;
+    int *h_counters = nullptr;  // pinned
+};
+
+namespace xrdt {
+
+std::string fmt(const char *f, ...)
+{
+    char b[512];
+    va_list ap;
+    va_start(ap, f);
+    vsnprintf(b, sizeof b, f, ap);
+    va_end(ap);
+    return std::string(b);
+}
+
+} // namespace xrdt
+
+namespace {
+
+enum Slot {
+    S_SPEC, S_IFINE, S_SEG, S_A1, S_A2, S_S2, S_N, S_C, S_A,
+    S_CELLS, S_VXY, S_VMAT, S_VNA, S_VA2, S_CNT, S_ASRC, S_S2U8,
+    S_SRCG, S_ENERGY, S_RFWIN, S_OFFS, S_WINLO, S_WINN, S_FINEQ, S_COARSEQ, S_COARSEQD,
+    S_RAYS, S_PAIRS, S_NC, S_CC, S_AC,
+    S_COUNT
+};
+
+int fail(xrdt_ctx *c, int status, const std::string &msg)
+{
+    if (c) c->err = msg;
+    return status;
+}
+
+#define CK(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess)                                                            \
+            return fail(ctx, XRDT_ERR_CUDA, fmt("%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                                               __FILE__, __LINE__));                      \
+    } while (0)
+
+int get_buf(xrdt_ctx *ctx, int slot, size_t bytes, void **out)
+{
+    if ((int)ctx->buf.size() < S_COUNT) {
+        ctx->buf.assign(S_COUNT, nullptr);
+        ctx->cap.assign(S_COUNT, 0);
+    }
+    if (bytes == 0) bytes = 16;
+    if (ctx->cap[slot] < bytes) {
+        if (ctx->buf[slot]) {
+            cudaStreamSynchronize(ctx->stream);
+            cudaFree(ctx->buf[slot]);
+            ctx->buf[slot] = nullptr;
+            ctx->cap[slot] = 0;
+        }
+        void *p = nullptr;
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(ctx, XRDT_ERR_ALLOC, fmt("cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e)));
+        }
+        ctx->buf[slot] = p;
+        ctx->cap[slot] = bytes;
+    }
+    *out = ctx->buf[slot];
+    return XRDT_OK;
+}
+
+bool is_device_ptr(const void *p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// Device view of an input: the pointer itself, or a staged copy.
+int stage_in(xrdt_ctx *ctx, int slot, const void *p, size_t bytes, const void **dev)
+{
+    if (is_device_ptr(p)) {
+        *dev = p;
+        return XRDT_OK;
+    }
+    void *d;
+    int rc = get_buf(ctx, slot, bytes, &d);
+    if (rc) return rc;
+    if (bytes) CK(cudaMemcpyAsync(d, p, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    *dev = d;
+    return XRDT_OK;
+}
+
+bool finite_all(const xrdt_problem *p)
+{
+    const double v[] = {p->e_src_min, p->e_src_max, p->e_det_min, p->e_det_max, p->q_lo, p->q_hi,
+                        p->dq0, p->hbarc, p->mec2, p->kn0, p->kn1, p->kn2, p->rsqrt2pi, p->dq_step,
+                        p->cx, p->cy, p->r_src, p->r_det, p->src_arc, p->src_phi0, p->col_pitch,
+                        p->row_pitch, p->z0, p->focal_spot, p->target_angle, p->wedge_angle, p->vox_side};
+    for (double x : v)
+        if (!std::isfinite(x)) return false;
+    return true;
+}
+
+// Positions of the sources and detector pixels, as integrate_diffraction.cu:93-109.
+void src_geom(const xrdt_problem *p, int src, SrcGeom *g)
+{
+    const double phi = ((double)src / (double)p->n_src) * p->src_arc + p->src_phi0;
+    g->sphi = sin(phi);
+    g->cphi = cos(phi);
+    g->Rsrc_x = p->cx + p->r_src * g->sphi;
+    g->Rsrc_y = p->cy - p->r_src * g->cphi;
+}
+
+bool inside_roi(const xrdt_problem *p, double x, double y)
+{
+    const double m = 1e-3;  // a margin of a thousandth of a voxel
+    return x > -m && x < p->nx * p->vox_side + m && y > -m && y < p->ny * p->vox_side + m;
+}
+
+} // namespace
+
+namespace xrdt {
+
+int build_dev_problem(const xrdt_problem *p, float q_min, float q_max, float a_min, float a_max,
+                      DevProblem *d, std::string *err)
+{
+    memset(d, 0, sizeof *d);
+    d->nx = p->nx;
+    d->ny = p->ny;
+    d->n_src = p->n_src;
+    d->n_col = p->n_col;
+    d->n_row = p->n_row;
+    d->n_det = p->n_col * p->n_row;
+    d->nrg_src = p->nrg_src;
+    d->nrg_det = p->nrg_det;
+    d->dnrg = p->dnrg;
+    d->nwt = p->nwt;
+    d->nqf = p->nqf;
+    d->n_mat = p->n_mat;
+    d->nq = p->nq;
+    d->na = p->na;
+    d->quirk_stale = (p->quirks & XRDT_QUIRK_STALE_VOXEL_A) ? 1 : 0;
+    d->dEs = (p->e_src_max - p->e_src_min) / (double)p->nrg_src;
+    d->dEd = (p->e_det_max - p->e_det_min) / (double)p->nrg_det;
+    d->e_src_min = p->e_src_min;
+    d->e_det_min = p->e_det_min;
+    d->q_lo = p->q_lo;
+    d->q_hi = p->q_hi;
+    d->dq0 = p->dq0;
+    d->dq_fine = (p->q_hi - p->q_lo) / (double)p->nqf;
+    d->hbarc = p->hbarc;
+    d->mec2 = p->mec2;
+    d->kn0 = p->kn0;
+    d->kn1 = p->kn1;
+    d->kn2 = p->kn2;
+    d->rsqrt2pi = p->rsqrt2pi;
+    d->DQ = p->dq_step;
+    d->cx = p->cx;
+    d->cy = p->cy;
+    d->r_src = p->r_src;
+    d->r_det = p->r_det;
+    d->col_pitch = p->col_pitch;
+    d->row_pitch = p->row_pitch;
+    d->z0 = p->z0;
+    d->focal = p->focal_spot;
+    d->geomAdet = p->col_pitch * p->row_pitch;
+    d->vox = p->vox_side;
+    d->tan_half = tan(p->wedge_angle / 2.0);
+    d->tan_full = tan(p->wedge_angle);
+    d->sta = sin(p->target_angle);
+    d->cta = cos(p->target_angle);
+    d->q_min = q_min;
+    d->q_max = q_max;
+    d->a_min = a_min;
+    d->a_max = a_max;
+    d->dq_tab = ((double)q_max - (double)q_min) / (double)p->nq;
+    d->da_tab = ((double)a_max - (double)a_min) / (double)p->na;
+    // maxBatch of integrate_diffraction.cu:160-161, times the block size
+    const double diag = sqrt((double)((int64_t)p->nx * p->nx + (int64_t)p->ny * p->ny));
+    d->kmax = (long long)ceil(diag / (p->dq_step * (double)p->nwt)) * (long long)p->nwt;
+    const int same = (p->nrg_src == p->nrg_det && p->e_src_min == p->e_det_min && p->e_src_max == p->e_det_max);
+    int lo_all = p->nrg_src, hi_all = -1;
+    for (int n = 0; n < p->nrg_det; n++) {
+        int lo, hi;
+        src_nrg_range(*d, same, n, &lo, &hi);
+        if (lo < lo_all) lo_all = lo;
+        if (hi > hi_all) hi_all = hi;
+    }
+    d->e_lo = lo_all;
+    d->e_hi = hi_all;
+    (void)err;
+    return XRDT_OK;
+}
+
+} // namespace xrdt
+
+extern "C" {
+
+int32_t xrdt_abi_version(void) { return XRDT_ABI_VERSION; }
+
+const char *xrdt_status_string(int32_t s)
+{
+    switch (s) {
+    case XRDT_OK: return "ok";
+    case XRDT_ERR_NULL: return "null pointer";
+    case XRDT_ERR_DIMS: return "dimension out of range";
+    case XRDT_ERR_GEOMETRY: return "source or detector inside the phantom";
+    case XRDT_ERR_INPUT: return "invalid input values";
+    case XRDT_ERR_CUDA: return "CUDA error";
+    case XRDT_ERR_ALLOC: return "allocation failed";
+    case XRDT_ERR_UNSUPPORTED: return "unsupported option";
+    case XRDT_ERR_TIMEOUT: return "device wait timed out";
+    default: return "unknown status";
+    }
+}
+
+int32_t xrdt_problem_reference(xrdt_problem *p, int32_t nx, int32_t ny)
+{
+    if (!p) return XRDT_ERR_NULL;
+    if (nx <= 0 || ny <= 0) return XRDT_ERR_DIMS;
+    memset(p, 0, sizeof *p);
+    p->nx = nx;
+    p->ny = ny;
+    p->n_src = 32;      // Forward_XRD.cu:17-25,47-48
+    p->n_col = 1024;
+    p->n_row = 1;
+    p->nrg_src = 64;
+    p->nrg_det = 64;
+    p->dnrg = 5;
+    p->nwt = 256;
+    p->nqf = 768;
+    p->n_mat = 3;
+    p->nq = 64;
+    p->na = 64;
+    p->quirks = XRDT_QUIRK_STALE_VOXEL_A;
+    p->e_src_min = p->e_det_min = 8.0;   // integrate_diffraction.cu:138-140
+    p->e_src_max = p->e_det_max = 80.0;
+    p->q_lo = (double)0.5f;              // Forward_XRD.cu:39-41
+    p->q_hi = (double)6.0f;
+    p->dq0 = (double)0.01f;
+    p->hbarc = (double)1.973269804f;     // Forward_XRD.cu:36
+    p->mec2 = (double)510.99895f;        // integrate_diffraction.cu:278
+    p->kn0 = (double)0.751691286166726f; // Forward_XRD.cu:51-53
+    p->kn1 = (double)1.4599683207703f;
+    p->kn2 = (double)-0.64597532690936f;
+    p->rsqrt2pi = (double)0.398942280401433f;  // Forward_XRD.cu:34
+    p->dq_step = (double)0.25f;          // Forward_XRD.cu:44
+    const double mmv = (double)nx / 100.0;     // integrate_diffraction.cu:81
+    const double Lx = 200.0 * mmv, Ly = 200.0 * mmv;
+    p->cx = Lx / 2.0;
+    p->cy = Ly / 2.0;
+    p->r_src = 150.0 * mmv;              // :84-85
+    p->r_det = 170.0 * mmv;
+    p->src_arc = (double)6.28318530717959f;  // twopi, Forward_XRD.cu:35
+    p->src_phi0 = 0.0;
+    p->col_pitch = 0.5 * mmv;            // :99-101
+    p->row_pitch = 1.0 * mmv;
+    p->z0 = 10.0 * mmv;
+    p->focal_spot = 0.5 * mmv;           // :118
+    p->target_angle = (double)0.523598775598299f;   // :117
+    p->wedge_angle = (double)0.00872664625997165f;  // :126
+    p->vox_side = 1.0;                   // :128
+    return XRDT_OK;
+}
+
+int32_t xrdt_problem_validate(const xrdt_problem *p)
+{
+    if (!p) return XRDT_ERR_NULL;
+    if (p->nx < 1 || p->ny < 1 || p->nx > 32767 || p->ny > 32767) return XRDT_ERR_DIMS;
+    if (p->n_src < 1 || p->n_src > 65535 || p->n_col < 1 || p->n_row < 1) return XRDT_ERR_DIMS;
+    if ((int64_t)p->n_col * p->n_row > 2147483647LL) return XRDT_ERR_DIMS;
+    if (p->dnrg < 0 || p->nrg_det < 1 || p->nrg_src < 2 * p->dnrg + 1) return XRDT_ERR_DIMS;
+    if (p->nwt < 1 || p->nqf < 1 || p->n_mat < 1 || p->nq < 1 || p->na < 1) return XRDT_ERR_DIMS;
+    if (p->reserved0 != 0 || (p->quirks & ~XRDT_QUIRK_STALE_VOXEL_A)) return XRDT_ERR_DIMS;
+    if (!finite_all(p)) return XRDT_ERR_DIMS;
+    if (!(p->e_src_max > p->e_src_min) || !(p->e_det_max > p->e_det_min) || !(p->q_hi > p->q_lo))
+        return XRDT_ERR_DIMS;
+    if (!(p->dq0 > 0) || !(p->dq_step > 0) || !(p->hbarc > 0) || !(p->mec2 > 0) || !(p->vox_side > 0))
+        return XRDT_ERR_DIMS;
+    for (int s = 0; s < p->n_src; s++) {
+        SrcGeom g;
+        src_geom(p, s, &g);
+        if (inside_roi(p, g.Rsrc_x, g.Rsrc_y)) return XRDT_ERR_GEOMETRY;
+        // the detector panel is a segment; its end pixels bound it
+        for (int c = 0; c < p->n_col; c += (p->n_col > 1 ? p->n_col - 1 : 1)) {
+            const double rdet = ((double)c - (double)p->n_col / 2.0 + 0.5) * p->col_pitch;
+            const double x = p->cx - p->r_det * g.sphi + rdet * g.cphi;
+            const double y = p->cy + p->r_det * g.cphi + rdet * g.sphi;
+            if (inside_roi(p, x, y)) return XRDT_ERR_GEOMETRY;
+        }
+        // the segment between the end pixels must not cross the ROI either
+        const double r0 = (0.0 - (double)p->n_col / 2.0 + 0.5) * p->col_pitch;
+        const double r1 = ((double)(p->n_col - 1) - (double)p->n_col / 2.0 + 0.5) * p->col_pitch;
+        for (int k = 1; k < 64; k++) {
+            const double r = r0 + (r1 - r0) * k / 64.0;
+            if (inside_roi(p, p->cx - p->r_det * g.sphi + r * g.cphi, p->cy + p->r_det * g.cphi + r * g.sphi))
+                return XRDT_ERR_GEOMETRY;
+        }
+    }
+    return XRDT_OK;
+}
+
+int64_t xrdt_problem_rays(const xrdt_problem *p)
+{
+    if (!p) return -1;
+    return (int64_t)p->n_src * p->n_col * p->n_row * p->nrg_det;
+}
+
+int64_t xrdt_problem_amatrix_elems(const xrdt_problem *p)
+{
+    if (!p) return -1;
+    return xrdt_problem_rays(p) * p->nwt * p->n_mat;
+}
+
+int32_t xrdt_ctx_create(xrdt_ctx **out, int32_t device, void *stream)
+{
+    if (!out) return XRDT_ERR_NULL;
+    *out = nullptr;
+    xrdt_ctx *ctx = new xrdt_ctx();
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) {
+        if (stream) {
+            ctx->stream = (cudaStream_t)stream;
+        } else {
+            e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+            ctx->own_stream = (e == cudaSuccess);
+        }
+    }
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&ctx->h_counters, 16 * sizeof(int));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+        delete ctx;
+        return XRDT_ERR_CUDA;
+    }
+    ctx->buf.assign(S_COUNT, nullptr);
+    ctx->cap.assign(S_COUNT, 0);
+    *out = ctx;
+    return XRDT_OK;
+}
+
+int32_t xrdt_ctx_destroy(xrdt_ctx *ctx)
+{
+    if (!ctx) return XRDT_ERR_NULL;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (void *p : ctx->buf)
+        if (p) cudaFree(p);
+    if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return XRDT_OK;
+}
+
+int32_t xrdt_ctx_synchronize(xrdt_ctx *ctx)
+{
+    if (!ctx) return XRDT_ERR_NULL;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return XRDT_OK;
+}
+
+const char *xrdt_last_error(const xrdt_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int64_t xrdt_ctx_launch_count(const xrdt_ctx *ctx) { return ctx ? ctx->launches : -1; }
+
+} // extern "C"
+
+namespace {
+
+// Shared body of xrdt_forward (rays == NULL: every ray, the Forward_XRD
+// layout) and xrdt_forward_rays (outputs per listed ray).
+int forward_impl(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, const float *Ifine,
+                 const int32_t *seg, const float *a1, const float *a2, const float *S2, float q_min,
+                 float q_max, float a_min, float a_max, const int64_t *ray_list, int64_t n_list,
+                 float *Nphotons, float *Cphotons, float *Amatrix, uint32_t flags)
+{
+    if (!ctx) return XRDT_ERR_NULL;
+    ctx->err.clear();
+    if (!p || !spectrum || !Ifine || !seg || !a1 || !a2 || !S2 || !Nphotons || !Cphotons)
+        return fail(ctx, XRDT_ERR_NULL, "a required array pointer is NULL");
+    int rc = xrdt_problem_validate(p);
+    if (rc) return fail(ctx, rc, fmt("problem rejected: %s", xrdt_status_string(rc)));
+    if (flags & ~(XRDT_FWD_PLAIN_FP64 | XRDT_FWD_NO_SYNC))
+        return fail(ctx, XRDT_ERR_UNSUPPORTED, "unknown flag bits");
+    if (!std::isfinite(q_min) || !std::isfinite(q_max) || !std::isfinite(a_min) || !std::isfinite(a_max))
+        return fail(ctx, XRDT_ERR_INPUT, "table edges must be finite");
+    const bool plain = flags & XRDT_FWD_PLAIN_FP64;
+    if (plain && (p->nwt % 32 != 0 || p->nwt > 1024))
+        return fail(ctx, XRDT_ERR_UNSUPPORTED, "the reference launch shape needs NWT a multiple of 32, <= 1024");
+    DevProblem P;
+    std::string err;
+    build_dev_problem(p, q_min, q_max, a_min, a_max, &P, &err);
+    if (!plain && P.e_hi - P.e_lo + 1 > 128)
+        return fail(ctx, XRDT_ERR_UNSUPPORTED, "more than 128 source energy bins in the windows");
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+
+    const int64_t nvox = (int64_t)p->nx * p->ny;
+    const int64_t all_rays = xrdt_problem_rays(p);
+    const int64_t MW = (int64_t)p->nwt * p->n_mat;
+    const int W = 2 * p->dnrg + 1;
+    if (ray_list) {
+        if (n_list < 0 || n_list > 2147483647LL) return fail(ctx, XRDT_ERR_DIMS, "bad ray count");
+        if (is_device_ptr(ray_list)) return fail(ctx, XRDT_ERR_UNSUPPORTED, "the ray list must be host memory");
+        for (int64_t i = 0; i < n_list; i++)
+            if (ray_list[i] < 0 || ray_list[i] >= all_rays)
+                return fail(ctx, XRDT_ERR_INPUT, fmt("ray %lld out of range", (long long)ray_list[i]));
+    }
+    // output element counts
+    const int64_t rays = ray_list ? n_list : all_rays;
+    const int64_t aelems = rays * MW;
+
+    // ---- inputs ----
+    const void *d_spec, *d_ifine, *d_seg, *d_a1, *d_a2, *d_S2;
+    if ((rc = stage_in(ctx, S_SPEC, spectrum, sizeof(float) * p->nrg_src * p->nrg_det, &d_spec))) return rc;
+    if ((rc = stage_in(ctx, S_IFINE, Ifine, sizeof(float) * (size_t)p->nqf * p->n_mat, &d_ifine))) return rc;
+    if ((rc = stage_in(ctx, S_SEG, seg, sizeof(int32_t) * nvox, &d_seg))) return rc;
+    if ((rc = stage_in(ctx, S_A1, a1, sizeof(float) * nvox, &d_a1))) return rc;
+    if ((rc = stage_in(ctx, S_A2, a2, sizeof(float) * nvox, &d_a2))) return rc;
+    if ((rc = stage_in(ctx, S_S2, S2, sizeof(float) * (size_t)p->nq * p->na, &d_S2))) return rc;
+    const bool hostN = !is_device_ptr(Nphotons), hostC = !is_device_ptr(Cphotons);
+    const bool hostA = Amatrix && !is_device_ptr(Amatrix);
+    if ((flags & XRDT_FWD_NO_SYNC) && (hostN || hostC || hostA))
+        return fail(ctx, XRDT_ERR_UNSUPPORTED, "XRDT_FWD_NO_SYNC needs device outputs");
+    float *dN = Nphotons, *dC = Cphotons, *dA = Amatrix;
+    void *tmp;
+    if (hostN) { if ((rc = get_buf(ctx, S_N, sizeof(float) * rays, &tmp))) return rc; dN = (float *)tmp; }
+    if (hostC) { if ((rc = get_buf(ctx, S_C, sizeof(float) * rays, &tmp))) return rc; dC = (float *)tmp; }
+    if (hostA) { if ((rc = get_buf(ctx, S_A, sizeof(float) * aelems, &tmp))) return rc; dA = (float *)tmp; }
+
+    // ---- per-call tables (host, double) ----
+    std::vector<SrcGeom> hsg(p->n_src);
+    for (int s = 0; s < p->n_src; s++) src_geom(p, s, &hsg[s]);
+    PrepBuffers B;
+    void *d_srcg;
+    if ((rc = get_buf(ctx, S_SRCG, sizeof(SrcGeom) * p->n_src, &d_srcg))) return rc;
+    CK(cudaMemcpyAsync(d_srcg, hsg.data(), sizeof(SrcGeom) * p->n_src, cudaMemcpyHostToDevice, st));
+    if ((rc = get_buf(ctx, S_CELLS, sizeof(float4) * 2 * (size_t)(p->nx + 1) * (p->ny + 1), &tmp))) return rc;
+    B.cells = (float4 *)tmp;
+    if ((rc = get_buf(ctx, S_VXY, sizeof(int) * nvox, &tmp))) return rc;
+    B.vox_xy = (int *)tmp;
+    if ((rc = get_buf(ctx, S_VMAT, sizeof(int) * nvox, &tmp))) return rc;
+    B.vox_mat = (int *)tmp;
+    if ((rc = get_buf(ctx, S_VNA, sizeof(int) * nvox, &tmp))) return rc;
+    B.vox_na = (int *)tmp;
+    if ((rc = get_buf(ctx, S_VA2, sizeof(float) * nvox, &tmp))) return rc;
+    B.vox_a2 = (float *)tmp;
+    if ((rc = get_buf(ctx, S_CNT, sizeof(int) * 4, &tmp))) return rc;
+    B.counters = (int *)tmp;
+    if ((rc = get_buf(ctx, S_S2U8, (size_t)p->nq * p->na, &tmp))) return rc;
+    B.s2u8 = (unsigned char *)tmp;
+    B.atten_src = nullptr;
+
+    CK(launch_prep_voxels(P, (const int32_t *)d_seg, (const float *)d_a1, (const float *)d_a2, B, st,
+                          &ctx->launches));
+    CK(cudaMemcpyAsync(ctx->h_counters, B.counters, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    const int nv = ctx->h_counters[0];
+    if (ctx->h_counters[1])
+        return fail(ctx, XRDT_ERR_INPUT, fmt("segmentation holds a material id above n_mat = %d", p->n_mat));
+
+    if (plain) {
+        std::vector<double> cq(2 * (size_t)p->nwt);
+        for (int k = 0; k < p->nwt; k++) {
+            const double NWT = (double)p->nwt;
+            const double e1 = p->q_lo + (double)k * p->dq0 +
+                              (p->q_hi - p->q_lo - p->dq0 * NWT) * (double)((int64_t)k * k) / (NWT * NWT);
+            const double e2 = p->q_lo + (double)(k + 1) * p->dq0 +
+                              (p->q_hi - p->q_lo - p->dq0 * NWT) * (double)((int64_t)(k + 1) * (k + 1)) / (NWT * NWT);
+            cq[2 * k] = 0.5 * (e1 + e2);
+            cq[2 * k + 1] = e2 - e1;
+        }
+        if ((rc = get_buf(ctx, S_COARSEQD, sizeof(double) * cq.size(), &tmp))) return rc;
+        CK(cudaMemcpyAsync(tmp, cq.data(), sizeof(double) * cq.size(), cudaMemcpyHostToDevice, st));
+        const int64_t *d_rays = nullptr;
+        if (ray_list) {
+            void *dr;
+            if ((rc = get_buf(ctx, S_RAYS, sizeof(int64_t) * (n_list ? n_list : 1), &dr))) return rc;
+            if (n_list) CK(cudaMemcpyAsync(dr, ray_list, sizeof(int64_t) * n_list, cudaMemcpyHostToDevice, st));
+            d_rays = (const int64_t *)dr;
+        }
+        CK(launch_plain_forward(P, (const SrcGeom *)d_srcg, (const float *)d_spec, (const float *)d_ifine,
+                                (const int32_t *)d_seg, (const float *)d_a1, (const float *)d_a2,
+                                (const float *)d_S2, (const double *)tmp, d_rays, n_list, dN, dC, dA, st,
+                                &ctx->launches));
+    } else if (nv == 0) {
+        // empty phantom: every output is zero (integrate_diffraction.cu:148-150,364-409)
+        CK(cudaMemsetAsync(dN, 0, sizeof(float) * rays, st));
+        CK(cudaMemsetAsync(dC, 0, sizeof(float) * rays, st));
+        if (dA) CK(cudaMemsetAsync(dA, 0, sizeof(float) * aelems, st));
+    } else {
+        // energy rows
+        std::vector<EnergyRow> er(p->nrg_src);
+        for (int e = 0; e < p->nrg_src; e++) {
+            EnergyRow &r = er[e];
+            r.Esrc1 = P.e_src_min + (double)e * P.dEs;
+            r.Esrc2 = P.e_src_min + (double)(e + 1) * P.dEs;
+            r.Esrc = 0.5 * (r.Esrc1 + r.Esrc2);
+            r.ein = r.Esrc / P.mec2;
+            const double f1 = r.ein * r.ein * r.ein, f2 = P.kn0 + P.kn1 * r.ein + P.kn2 * r.ein * r.ein;
+            r.inv_f1 = (float)(1.0 / f1);
+            r.inv_f2 = (float)(1.0 / f2);
+            const double wf = 2.0 * r.Esrc / P.hbarc;
+            r.wfac_hi = (float)wf;
+            r.wfac_lo = (float)(wf - (double)r.wfac_hi);
+            r.sig_c1 = (float)((2.0 / P.hbarc) * (2.0 / P.hbarc) * P.dEs * P.dEs / 12.0);
+            r.sig_c2 = (float)((r.Esrc / P.hbarc) * (r.Esrc / P.hbarc) / 4.0);
+            r.einf = (float)r.ein;
+            r.Esrc1f = (float)r.Esrc1;
+            r.Esrc2f = (float)r.Esrc2;
+            r.pad = 0.f;
+        }
+        const int same = (p->nrg_src == p->nrg_det && p->e_src_min == p->e_det_min && p->e_src_max == p->e_det_max);
+        std::vector<float> rfw((size_t)p->nrg_det * W), offs((size_t)p->nrg_det * W);
+        std::vector<int> wlo(p->nrg_det), wn(2 * (size_t)p->nrg_src);
+        for (int e = 0; e < p->nrg_src; e++) {
+            wn[2 * e] = p->nrg_det;
+            wn[2 * e + 1] = -1;
+        }
+        std::vector<float> hspec;
+        const float *spec_h = spectrum;
+        if (is_device_ptr(spectrum)) {
+            hspec.resize((size_t)p->nrg_src * p->nrg_det);
+            CK(cudaMemcpy(hspec.data(), spectrum, sizeof(float) * hspec.size(), cudaMemcpyDeviceToHost));
+            spec_h = hspec.data();
+        }
+        for (int n = 0; n < p->nrg_det; n++) {
+            int lo, hi;
+            src_nrg_range(P, same, n, &lo, &hi);
+            wlo[n] = lo;
+            const double Ed1 = P.e_det_min + (double)n * P.dEd;
+            for (int j = 0; j < W; j++) {
+                rfw[(size_t)n * W + j] = spec_h[(lo + j) + (size_t)n * p->nrg_src];
+                offs[(size_t)n * W + j] = (float)((P.e_src_min + (double)(lo + j) * P.dEs) - Ed1);
+                const int e = lo + j;
+                if (n < wn[2 * e]) wn[2 * e] = n;
+                if (n > wn[2 * e + 1]) wn[2 * e + 1] = n;
+            }
+        }
+        std::vector<float2> fq(p->nqf);
+        for (int j = 0; j < p->nqf; j++) {
+            const double q = P.q_lo + P.dq_fine * (0.5 + (double)j);
+            fq[j].x = (float)q;
+            fq[j].y = (float)(q - (double)fq[j].x);
+        }
+        std::vector<float4> cqf(p->nwt);
+        for (int k = 0; k < p->nwt; k++) {
+            const double NWT = (double)p->nwt;
+            const double e1 = p->q_lo + (double)k * p->dq0 +
+                              (p->q_hi - p->q_lo - p->dq0 * NWT) * (double)((int64_t)k * k) / (NWT * NWT);
+            const double e2 = p->q_lo + (double)(k + 1) * p->dq0 +
+                              (p->q_hi - p->q_lo - p->dq0 * NWT) * (double)((int64_t)(k + 1) * (k + 1)) / (NWT * NWT);
+            const double q = 0.5 * (e1 + e2);
+            cqf[k].x = (float)q;
+            cqf[k].y = (float)(q - (double)cqf[k].x);
+            cqf[k].z = (float)(e2 - e1);
+            cqf[k].w = 0.f;
+        }
+        FwdTables T;
+        void *d;
+        if ((rc = get_buf(ctx, S_ENERGY, sizeof(EnergyRow) * er.size(), &d))) return rc;
+        CK(cudaMemcpyAsync(d, er.data(), sizeof(EnergyRow) * er.size(), cudaMemcpyHostToDevice, st));
+        T.energy = (const EnergyRow *)d;
+        if ((rc = get_buf(ctx, S_RFWIN, sizeof(float) * rfw.size(), &d))) return rc;
+        CK(cudaMemcpyAsync(d, rfw.data(), sizeof(float) * rfw.size(), cudaMemcpyHostToDevice, st));
+        T.rf_win = (const float *)d;
+        if ((rc = get_buf(ctx, S_OFFS, sizeof(float) * offs.size(), &d))) return rc;
+        CK(cudaMemcpyAsync(d, offs.data(), sizeof(float) * offs.size(), cudaMemcpyHostToDevice, st));
+        T.offs = (const float *)d;
+        if ((rc = get_buf(ctx, S_WINLO, sizeof(int) * wlo.size(), &d))) return rc;
+        CK(cudaMemcpyAsync(d, wlo.data(), sizeof(int) * wlo.size(), cudaMemcpyHostToDevice, st));
+        T.win_lo = (const int *)d;
+        if ((rc = get_buf(ctx, S_WINN, sizeof(int) * wn.size(), &d))) return rc;
+        CK(cudaMemcpyAsync(d, wn.data(), sizeof(int) * wn.size(), cudaMemcpyHostToDevice, st));
+        T.win_n = (const int *)d;
+        if ((rc = get_buf(ctx, S_FINEQ, sizeof(float2) * fq.size(), &d))) return rc;
+        CK(cudaMemcpyAsync(d, fq.data(), sizeof(float2) * fq.size(), cudaMemcpyHostToDevice, st));
+        T.fine_q = (const float2 *)d;
+        if ((rc = get_buf(ctx, S_COARSEQ, sizeof(float4) * cqf.size(), &d))) return rc;
+        CK(cudaMemcpyAsync(d, cqf.data(), sizeof(float4) * cqf.size(), cudaMemcpyHostToDevice, st));
+        T.coarse_q = (const float4 *)d;
+
+        if ((rc = get_buf(ctx, S_ASRC, sizeof(float2) * (size_t)p->n_src * nv, &tmp))) return rc;
+        B.atten_src = (float2 *)tmp;
+        CK(launch_prep_map(P, (const float *)d_a1, (const float *)d_a2, (const float *)d_S2, B, st, &ctx->launches));
+        CK(launch_src_atten(P, (const SrcGeom *)d_srcg, nv, B, st, &ctx->launches));
+        if (!ray_list) {
+            CK(launch_fast_forward(P, (const SrcGeom *)d_srcg, T, B, nv, (const float *)d_ifine, nullptr, 0, dN,
+                                   dC, dA, st, &ctx->launches));
+        } else if (n_list > 0) {
+            // the (src, det) pairs the listed rays need, then a gather
+            std::vector<int64_t> cols(n_list);
+            for (int64_t i = 0; i < n_list; i++) cols[i] = ray_list[i] % ((int64_t)p->n_src * P.n_det);
+            std::vector<int64_t> uniq(cols);
+            std::sort(uniq.begin(), uniq.end());
+            uniq.erase(std::unique(uniq.begin(), uniq.end()), uniq.end());
+            const int np = (int)uniq.size();
+            std::vector<int2> pairs(np);
+            for (int i = 0; i < np; i++) pairs[i] = make_int2((int)(uniq[i] % p->n_src), (int)(uniq[i] / p->n_src));
+            std::vector<int64_t> idx(n_list);
+            for (int64_t i = 0; i < n_list; i++) {
+                const int64_t pi = std::lower_bound(uniq.begin(), uniq.end(), cols[i]) - uniq.begin();
+                const int64_t nrg = ray_list[i] / ((int64_t)p->n_src * P.n_det);
+                idx[i] = pi + nrg * np;
+            }
+            void *dpairs, *didx, *dNc, *dCc, *dAc = nullptr;
+            const int64_t ncomp = (int64_t)np * p->nrg_det;
+            if ((rc = get_buf(ctx, S_PAIRS, sizeof(int2) * np, &dpairs))) return rc;
+            if ((rc = get_buf(ctx, S_RAYS, sizeof(int64_t) * n_list, &didx))) return rc;
+            if ((rc = get_buf(ctx, S_NC, sizeof(float) * ncomp, &dNc))) return rc;
+            if ((rc = get_buf(ctx, S_CC, sizeof(float) * ncomp, &dCc))) return rc;
+            if (dA && (rc = get_buf(ctx, S_AC, sizeof(float) * ncomp * MW, &dAc))) return rc;
+            CK(cudaMemcpyAsync(dpairs, pairs.data(), sizeof(int2) * np, cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(didx, idx.data(), sizeof(int64_t) * n_list, cudaMemcpyHostToDevice, st));
+            CK(launch_fast_forward(P, (const SrcGeom *)d_srcg, T, B, nv, (const float *)d_ifine,
+                                   (const int2 *)dpairs, np, (float *)dNc, (float *)dCc, (float *)dAc, st,
+                                   &ctx->launches));
+            CK(launch_gather_rays((const int64_t *)didx, n_list, (const float *)dNc, (const float *)dCc,
+                                  (const float *)dAc, (int)MW, dN, dC, dA, st, &ctx->launches));
+            // the pair list and index buffers are read asynchronously
+            CK(cudaStreamSynchronize(st));
+        }
+    }
+
+    // ---- outputs ----
+    if (hostN) CK(cudaMemcpyAsync(Nphotons, dN, sizeof(float) * rays, cudaMemcpyDeviceToHost, st));
+    if (hostC) CK(cudaMemcpyAsync(Cphotons, dC, sizeof(float) * rays, cudaMemcpyDeviceToHost, st));
+    if (hostA) CK(cudaMemcpyAsync(Amatrix, dA, sizeof(float) * aelems, cudaMemcpyDeviceToHost, st));
+    if (!(flags & XRDT_FWD_NO_SYNC)) CK(cudaStreamSynchronize(st));
+    return XRDT_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int32_t xrdt_forward(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, const float *Ifine,
+                     const int32_t *seg, const float *a1, const float *a2, const float *S2, float q_min,
+                     float q_max, float a_min, float a_max, float *Nphotons, float *Cphotons,
+                     float *Amatrix, uint32_t flags)
+{
+    return forward_impl(ctx, p, spectrum, Ifine, seg, a1, a2, S2, q_min, q_max, a_min, a_max, nullptr, 0,
+                        Nphotons, Cphotons, Amatrix, flags);
+}
+
+int32_t xrdt_forward_rays(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, const float *Ifine,
+                          const int32_t *seg, const float *a1, const float *a2, const float *S2, float q_min,
+                          float q_max, float a_min, float a_max, const int64_t *rays, int64_t n_rays,
+                          float *Nphotons, float *Cphotons, float *A_rows, uint32_t flags)
+{
+    if (!rays && n_rays) return fail(ctx, XRDT_ERR_NULL, "ray list is NULL");
+    static const int64_t none = 0;
+    return forward_impl(ctx, p, spectrum, Ifine, seg, a1, a2, S2, q_min, q_max, a_min, a_max,
+                        rays ? rays : &none, n_rays, Nphotons, Cphotons, A_rows, flags);
+}
+
+} // extern "C"

@@ -1,0 +1,532 @@
+// k_fwd.cu -- factored forward projector (Nphotons, Cphotons, Amatrix).
+//
+// Same model as integrate_diffraction.cu:9-409, reorganised for the GPU:
+//
+//  * One block per (source, detector pixel) instead of one per
+//    (source, pixel, detector energy bin).  Everything except the spectrum
+//    weight RF = spectrum[e, nrg] and the Compton channel overlap depends on
+//    the source energy e only (:266-356), so the block accumulates
+//    T[e] = sum_v W(v,e) ... once per source bin and applies the banded
+//    response afterwards: Nphotons[nrg] = sum_{e in window(nrg)} RF[e,nrg] T[e].
+//    The reference evaluates each (voxel, e) pair once per detector bin whose
+//    window holds e (11 times).
+//  * Gaussian q-resolution sums (:299-315) run over the bins within 7 sigma of
+//    the wavevector transfer only (the dropped tail is below 3e-11 of the
+//    peak); the reference sums every fine bin.
+//  * The detector-side line integral is a warp-cooperative walk over the
+//    bilinear cell map; the source-side one comes from a per-(source, voxel)
+//    table (k_prep.cu), since it does not depend on the detector pixel.
+//  * Scattering geometry, ROI entry points and sample counts are FP64; the
+//    wavevector transfer is carried as a float pair (about 48 significant
+//    bits) because the Gaussian at 3 sigma amplifies its relative error by
+//    several hundred; the rest is FP32 with Kahan-compensated sums over
+//    voxels.
+//
+// Work split inside a block (8 warps): warp w takes voxel chunks w, w+8, ...
+// of 32 voxels.  For a chunk, lane = voxel computes the FP64 geometry; then
+// for each voxel of the chunk the warp walks its detector-side ray together
+// and lane = source energy evaluates the (voxel, energy) term, so each lane
+// keeps the running sum of its own energies in registers.
+#include "xrdt_device.cuh"
+#include "walk.cuh"
+
+namespace xrdt {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kMaxRounds = 4;           // source bins per block <= 128
+constexpr float kSig = 7.0f;            // Gaussian window, in sigma
+constexpr float kLog2e = 1.4426950408889634f;
+
+__device__ __forceinline__ void kahan_add(float &s, float &c, float x)
+{
+    const float y = x - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+struct Layout {
+    size_t en, rf, offs, winlo, wn, ifine, fq, cq, s2, tn, cw, ck, ta, total;
+};
+
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+// Shared-memory layout; identical on host and device.
+__host__ __device__ inline Layout fwd_layout(const DevProblem &P, int E, int e_pass, bool with_n,
+                                             bool with_a)
+{
+    Layout L;
+    const int W = 2 * P.dnrg + 1;
+    size_t o = 0;
+    L.tn = o; o = align16(o + sizeof(double) * E);
+    L.ck = o; o = align16(o + sizeof(float2) * kWarps * P.nrg_det);
+    L.en = o; o = align16(o + sizeof(float) * 9 * E);
+    L.rf = o; o = align16(o + sizeof(float) * P.nrg_det * W);
+    L.offs = o; o = align16(o + sizeof(float) * P.nrg_det * W);
+    L.winlo = o; o = align16(o + sizeof(int) * P.nrg_det);
+    L.wn = o; o = align16(o + sizeof(int) * 2 * E);
+    L.cw = o; o = align16(o + sizeof(float) * kWarps * P.nrg_det);
+    L.ifine = o; if (with_n) o = align16(o + sizeof(float) * P.n_mat * P.nqf);
+    L.fq = o; if (with_n) o = align16(o + sizeof(float2) * P.nqf);
+    L.cq = o; if (with_a) o = align16(o + sizeof(float4) * P.nwt);
+    L.s2 = o; o = align16(o + (size_t)P.nq * P.na);
+    L.ta = o; if (with_a) o = align16(o + sizeof(float) * (size_t)e_pass * P.n_mat * P.nwt);
+    L.total = o;
+    return L;
+}
+
+struct FwdArgs {
+    DevProblem P;
+    const SrcGeom *sg;
+    FwdTables T;
+    const int *vox_xy, *vox_mat, *vox_na;
+    const float *vox_a2;
+    const float4 *cells;
+    const float2 *atten_src;
+    const unsigned char *s2u8;
+    const float *Ifine;
+    float *N, *C, *A;
+    const int2 *pairs;
+    int n_pairs;
+    int nv, E, e_pass;
+    float qpar_a, qpar_b;   // coarse grid inversion: edge(n) = q_lo + b n + a n^2
+};
+
+template <bool WITH_N, bool WITH_A>
+__global__ void __launch_bounds__(kThreads)
+k_fwd(const FwdArgs args)
+{
+    extern __shared__ __align__(16) unsigned char sm[];
+    const DevProblem &P = args.P;
+    const int E = args.E;
+    const int W = 2 * P.dnrg + 1;
+    const Layout L = fwd_layout(P, E, args.e_pass, WITH_N, WITH_A);
+    double *TN = (double *)(sm + L.tn);
+    float2 *Ck = (float2 *)(sm + L.ck);
+    float *en = (float *)(sm + L.en);   // SoA: 9 rows of E
+    float *en_if1 = en, *en_if2 = en + E, *en_wh = en + 2 * E, *en_wl = en + 3 * E;
+    float *en_c1 = en + 4 * E, *en_c2 = en + 5 * E, *en_ein = en + 6 * E;
+    float *rf = (float *)(sm + L.rf);
+    float *offs = (float *)(sm + L.offs);
+    int *winlo = (int *)(sm + L.winlo);
+    int *wn = (int *)(sm + L.wn);
+    float *Cw = (float *)(sm + L.cw);
+    float *Is = (float *)(sm + L.ifine);
+    float2 *fq = (float2 *)(sm + L.fq);
+    float4 *cq = (float4 *)(sm + L.cq);
+    unsigned char *S2 = sm + L.s2;
+    float *TA = (float *)(sm + L.ta);
+
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    int det, src;
+    int64_t colidx, ncols;   // output column of this block and the number of columns
+    if (args.pairs) {
+        const int2 pr = args.pairs[blockIdx.x];
+        src = pr.x;
+        det = pr.y;
+        colidx = blockIdx.x;
+        ncols = args.n_pairs;
+    } else {
+        det = blockIdx.x;
+        src = blockIdx.y;
+        colidx = (int64_t)src + (int64_t)det * P.n_src;
+        ncols = (int64_t)P.n_src * P.n_det;
+    }
+
+    // ---- stage the tables ----
+    for (int i = tid; i < E; i += kThreads) {
+        const EnergyRow r = args.T.energy[P.e_lo + i];
+        en_if1[i] = r.inv_f1;
+        en_if2[i] = r.inv_f2;
+        en_wh[i] = r.wfac_hi;
+        en_wl[i] = r.wfac_lo;
+        en_c1[i] = r.sig_c1;
+        en_c2[i] = r.sig_c2;
+        en_ein[i] = r.einf;
+        TN[i] = 0.0;
+        wn[2 * i] = args.T.win_n[2 * (P.e_lo + i)];
+        wn[2 * i + 1] = args.T.win_n[2 * (P.e_lo + i) + 1];
+    }
+    for (int i = tid; i < P.nrg_det * W; i += kThreads) {
+        rf[i] = args.T.rf_win[i];
+        offs[i] = args.T.offs[i];
+    }
+    for (int i = tid; i < P.nrg_det; i += kThreads) winlo[i] = args.T.win_lo[i];
+    for (int i = tid; i < kWarps * P.nrg_det; i += kThreads) {
+        Cw[i] = 0.f;
+        Ck[i] = make_float2(0.f, 0.f);
+    }
+    if (WITH_N) {
+        for (int i = tid; i < P.n_mat * P.nqf; i += kThreads) Is[i] = __ldg(args.Ifine + i);
+        for (int i = tid; i < P.nqf; i += kThreads) fq[i] = args.T.fine_q[i];
+    }
+    if (WITH_A)
+        for (int i = tid; i < P.nwt; i += kThreads) cq[i] = args.T.coarse_q[i];
+    for (int i = tid; i < P.nq * P.na; i += kThreads) S2[i] = args.s2u8[i];
+
+    // ---- per-(source, pixel) geometry, integrate_diffraction.cu:81-128 ----
+    const SrcGeom g = args.sg[src];
+    double Rdet_x, Rdet_y, Rdet_z;
+    det_position(P, g.sphi, g.cphi, det, &Rdet_x, &Rdet_y, &Rdet_z);
+    const double ndet_x = g.sphi, ndet_y = -g.cphi;
+    const double nsrc_x = -g.sphi * P.sta, nsrc_y = g.cphi * P.sta, nsrc_z = -P.cta;
+    const double nsrc_xy = sqrt(nsrc_x * nsrc_x + nsrc_y * nsrc_y);
+    const float rsqrt2pi = (float)P.rsqrt2pi;
+    const float DQf = (float)P.DQ;
+    const float dqf_hi = (float)P.dq_fine, dqf_lo = (float)(P.dq_fine - (double)dqf_hi);
+    const float inv_dqf = (float)(1.0 / P.dq_fine), qlo_f = (float)P.q_lo;
+    const float kn0 = (float)P.kn0, kn1 = (float)P.kn1, kn2 = (float)P.kn2;
+    const float edmin = (float)P.e_det_min, inv_dEd = (float)(1.0 / P.dEd), dEdf = (float)P.dEd;
+    const float dEsf = (float)P.dEs;
+    const float qmin_t = (float)P.q_min, inv_dqt = (float)(1.0 / P.dq_tab);
+    const int lo_e = P.e_lo;
+    __syncthreads();
+
+    float tn[kMaxRounds], tc[kMaxRounds];
+#pragma unroll
+    for (int r = 0; r < kMaxRounds; r++) tn[r] = tc[r] = 0.f;
+
+    const int nv = args.nv;
+    const int nchunks = (nv + 31) >> 5;
+    for (int pe0 = 0; pe0 < E; pe0 += args.e_pass) {
+        const int pe1 = min(E, pe0 + args.e_pass);
+        if (WITH_A) {
+            for (int i = tid; i < (pe1 - pe0) * P.n_mat * P.nwt; i += kThreads) TA[i] = 0.f;
+            __syncthreads();
+        }
+        for (int chunk = wid; chunk < nchunks; chunk += kWarps) {
+            // ---- lane = voxel: FP64 geometry (integrate_diffraction.cu:192-255) ----
+            const int v = chunk * 32 + lane;
+            const bool valid = v < nv;
+            const int vv = valid ? v : nv - 1;
+            const int xy = args.vox_xy[vv];
+            const double vx = ((double)(xy & 0xffff) + 0.5) * P.vox;
+            const double vy = ((double)(xy >> 16) + 0.5) * P.vox;
+            const double ax = vx - g.Rsrc_x, ay = vy - g.Rsrc_y;
+            const double proj = ax * nsrc_x + ay * nsrc_y;
+            const double Rvox_z = -proj / nsrc_xy * P.tan_half;
+            const double Hvox = proj / nsrc_xy * P.tan_full;
+            const double az = Rvox_z;
+            const double bx = Rdet_x - vx, by = Rdet_y - vy, bz = Rdet_z - Rvox_z;
+            const double ab = ax * bx + ay * by + az * bz;
+            const double anorm2 = ax * ax + ay * ay + az * az;
+            const double bnorm2 = bx * bx + by * by + bz * bz;
+            const double costheta = ab * (1.0 / sqrt(anorm2)) * (1.0 / sqrt(bnorm2));
+            const double omc = 1.0 - costheta;
+            const double sth = sqrt(fabs(omc) / 2.0);
+            const double Sx = bx - ab * ax / anorm2, Sy = by - ab * ay / anorm2, Sz = bz - ab * az / anorm2;
+            const double Dx = -ax + ab * bx / bnorm2, Dy = -ay + ab * by / bnorm2, Dz = -az + ab * bz / bnorm2;
+            const double Vx = -(Sx + Dx), Vy = -(Sy + Dy), Vz = -(Sz + Dz);
+            const double Dndet = Dx * ndet_x + Dy * ndet_y;
+            const double Snsrc = Sx * nsrc_x + Sy * nsrc_y + Sz * nsrc_z;
+            const double dD2 = (Dx * Dx + Dy * Dy + Dz * Dz - Dndet * Dndet) * P.geomAdet / 12.0;
+            const double vV2 = (P.vox * P.vox * (Vx * Vx + Vy * Vy) + Hvox * Hvox * Vz * Vz) / 12.0;
+            const double sS2 = (Sx * Sx + Sy * Sy + Sz * Sz - Snsrc * Snsrc) * P.focal * P.focal / 12.0;
+            const double Rdotn = -g.sphi * ax + g.cphi * ay;
+            const double cospsi = Rdotn * (1.0 / sqrt(ax * ax + ay * ay));
+            const double gsv = cospsi * (1.0 / sqrt(anorm2)) * P.tan_full;
+            const double gvd = -(ndet_x * bx + ndet_y * by) * (1.0 / sqrt(bnorm2 * bnorm2 * bnorm2));
+            const double gpd = gsv * gvd;
+            const float s_hi = (float)sth, s_lo = (float)(sth - (double)s_hi);
+            const float omc_hi = (float)omc, omc_lo = (float)(omc - (double)omc_hi);
+            const float sgv = (float)((sS2 + vV2 + dD2) / anorm2 / bnorm2);
+            const float gpv = (float)gpd;
+            const float Wgv = (float)(gpd * ((1.0 + costheta * costheta) / 2.0));
+            const float cos2v = (float)(costheta * costheta);
+            const int mv = args.vox_mat[vv];
+            const int nav = args.vox_na[vv];
+            const float a2v = args.vox_a2[vv];
+            const float2 Asv = args.atten_src[(int64_t)src * nv + vv];
+            WalkSetup ws;
+            walk_setup(P, Rdet_x, Rdet_y, vx, vy, &ws);
+
+            const int nin = min(32, nv - chunk * 32);
+            for (int i = 0; i < nin; i++) {
+                WalkSetup wi;
+                wi.rx = __shfl_sync(0xffffffffu, ws.rx, i);
+                wi.ry = __shfl_sync(0xffffffffu, ws.ry, i);
+                wi.Lx = __shfl_sync(0xffffffffu, ws.Lx, i);
+                wi.Ly = __shfl_sync(0xffffffffu, ws.Ly, i);
+                wi.n = __shfl_sync(0xffffffffu, ws.n, i);
+                // labels as at integrate_diffraction.cu:259-260: the detector-side
+                // integral feeds Pin, the source-side one Pout.
+                const float2 Ad = walk_coop(args.cells, P.nx, P.ny, wi, DQf, lane);
+                const float sh = __shfl_sync(0xffffffffu, s_hi, i);
+                const float sl = __shfl_sync(0xffffffffu, s_lo, i);
+                const float oh = __shfl_sync(0xffffffffu, omc_hi, i);
+                const float ol = __shfl_sync(0xffffffffu, omc_lo, i);
+                const float sg = __shfl_sync(0xffffffffu, sgv, i);
+                const float gp = __shfl_sync(0xffffffffu, gpv, i);
+                const float Wg = __shfl_sync(0xffffffffu, Wgv, i);
+                const float cos2 = __shfl_sync(0xffffffffu, cos2v, i);
+                const int m = __shfl_sync(0xffffffffu, mv, i);
+                const int na = __shfl_sync(0xffffffffu, nav, i);
+                const float a2now = __shfl_sync(0xffffffffu, a2v, i);
+                const float Asx = __shfl_sync(0xffffffffu, Asv.x, i);
+                const float Asy = __shfl_sync(0xffffffffu, Asv.y, i);
+                const float s2f = sh * sh;
+#pragma unroll
+                for (int r = 0; r < kMaxRounds; r++) {
+                    const int el = lane + 32 * r;
+                    if (el < pe0 || el >= pe1) continue;
+                    // ---- (voxel, source energy) term, :266-356 ----
+                    const float if1 = en_if1[el], if2 = en_if2[el];
+                    const float Xin = fmaf(Ad.x, if1, Ad.y * if2);
+                    const float Xout = fmaf(Asx, if1, Asy * if2);
+                    const float wh0 = en_wh[el], wl0 = en_wl[el];
+                    float w_hi = wh0 * sh;
+                    float w_lo = fmaf(wh0, sh, -w_hi) + fmaf(wh0, sl, wl0 * sh);
+                    {
+                        const float t = w_hi + w_lo;
+                        w_lo = w_lo - (t - w_hi);
+                        w_hi = t;
+                    }
+                    const float sig2 = fmaf(en_c1[el], s2f, en_c2[el] * sg / s2f);
+                    const float rs = rsqrtf(sig2);
+                    const float cexp = -0.5f * kLog2e / sig2;
+                    const float PP = exp2f(-(Xin + Xout) * kLog2e);
+                    const float pref = PP * Wg * rsqrt2pi * rs;
+                    const float half = kSig * sig2 * rs;
+                    if (WITH_N) {
+                        const float jc = (w_hi - qlo_f) * inv_dqf - 0.5f;
+                        int jlo = (int)ceilf(jc - half * inv_dqf);
+                        int jhi = (int)floorf(jc + half * inv_dqf);
+                        jlo = max(jlo, 0);
+                        jhi = min(jhi, P.nqf - 1);
+                        float acc = 0.f;
+                        if (jlo <= jhi) {
+                            const float2 q0 = fq[jlo];
+                            const float d0 = (w_hi - q0.x) + (w_lo - q0.y);
+                            const float *Ir = Is + m * P.nqf;
+                            float t = 0.f;
+                            for (int j = jlo; j <= jhi; j++, t += 1.f) {
+                                const float d = fmaf(-t, dqf_lo, fmaf(-t, dqf_hi, d0));
+                                acc = fmaf(exp2f(cexp * d * d), Ir[j], acc);
+                            }
+                        }
+                        kahan_add(tn[r], tc[r], pref * dqf_hi * acc);
+                    }
+                    if (WITH_A) {
+                        // coarse bins near w: invert edge(n) = q_lo + b n + a n^2
+                        int klo = 0, khi = P.nwt - 1;
+                        {
+                            const float qa = w_hi - half - qlo_f, qb = w_hi + half - qlo_f;
+                            const float a = args.qpar_a, b = args.qpar_b;
+                            const float da = fmaf(4.f * a, qa, b * b), db = fmaf(4.f * a, qb, b * b);
+                            if (da >= 0.f && db >= 0.f) {
+                                const float na_ = 2.f * qa / (b + sqrtf(da));
+                                const float nb_ = 2.f * qb / (b + sqrtf(db));
+                                klo = max(klo, (int)floorf(na_) - 1);
+                                khi = min(khi, (int)floorf(nb_) + 1);
+                            }
+                        }
+                        float *tar = TA + ((size_t)(el - pe0) * P.n_mat + m) * P.nwt;
+                        for (int k = klo; k <= khi; k++) {
+                            const float4 c = cq[k];
+                            const float d = (w_hi - c.x) + (w_lo - c.y);
+                            atomicAdd(tar + k, pref * c.z * exp2f(cexp * d * d));
+                        }
+                    }
+                    // ---- Compton, :318-356 ----
+                    {
+                        const float ein = en_ein[el];
+                        const float x = ein * oh;                 // eratio - 1
+                        const float eratio = 1.f + x;
+                        const float inv_er = 1.f / eratio;
+                        const int eg = lo_e + el;
+                        // detector bins whose window holds e and whose channel the
+                        // outgoing range [E1, E2]/eratio can overlap
+                        const float Eo_lo = (float)(P.e_src_min) + (float)eg * dEsf;
+                        int n0 = max(wn[2 * el], (int)floorf((Eo_lo * inv_er - edmin) * inv_dEd) - 1);
+                        int n1 = min(wn[2 * el + 1], (int)floorf(((Eo_lo + dEsf) * inv_er - edmin) * inv_dEd) + 1);
+                        if (n0 <= n1) {
+                            const float wC = ein * sh;
+                            const float l2 = log2f(wC * sqrtf(eratio + wC * wC) * inv_er);
+                            const float tq = (l2 - qmin_t) * inv_dqt;
+                            const float fr = tq - floorf(tq);
+                            int nq;
+                            if (fr > 2e-4f && fr < 1.f - 2e-4f) {
+                                nq = (int)floorf(tq);
+                            } else {  // near a bin edge: decide in FP64 as the oracle does
+                                const double eind = args.T.energy[eg].ein;
+                                const double omcd = (double)oh + (double)ol;
+                                const double sd = sqrt(fabs(omcd) / 2.0);
+                                const double erd = 1.0 + eind * omcd;
+                                const double wd = eind * sd;
+                                const double l2d = log2(wd * sqrt(erd + wd * wd) / erd);
+                                nq = floor_to_int((l2d - P.q_min) / P.dq_tab);
+                            }
+                            nq = nq < 0 ? 0 : (nq >= P.nq ? P.nq - 1 : nq);
+                            const float eout = ein * inv_er;
+                            const float f1 = eout * eout * eout;
+                            const float f2 = fmaf(kn2 * eout, eout, fmaf(kn1, eout, kn0));
+                            const float Xc = Asx / f1 + Asy / f2;
+                            const float Pc = exp2f(-(Xin + Xc) * kLog2e);
+                            const float Cf = eratio * eratio * (eratio + inv_er - 1.f + cos2) * 0.5f;
+                            const float base = Pc * gp * Cf * a2now * (float)S2[nq + na * P.nq];
+                            const float span = dEsf * inv_er;   // Eout2 - Eout1
+                            for (int n = n0; n <= n1; n++) {
+                                const int j = eg - winlo[n];
+                                const float Ed1 = edmin + (float)n * dEdf;
+                                // outgoing range relative to the channel's left edge:
+                                // u1 = Eout1 - Edet1 = ((Esrc1 - Edet1) - Edet1*x)/eratio
+                                const float u1 = fmaf(-Ed1, x, offs[n * W + j]) * inv_er;
+                                const float u2 = u1 + span;
+                                const float ov = fminf(u2, dEdf) - fmaxf(u1, 0.f);
+                                if (ov > 0.f)
+                                    atomicAdd(&Cw[wid * P.nrg_det + n], ov / span * rf[n * W + j] * base);
+                            }
+                        }
+                    }
+                }
+            }
+            __syncwarp();
+            for (int n = lane; n < P.nrg_det; n += 32) {
+                float2 k = Ck[wid * P.nrg_det + n];
+                kahan_add(k.x, k.y, Cw[wid * P.nrg_det + n]);
+                Ck[wid * P.nrg_det + n] = k;
+                Cw[wid * P.nrg_det + n] = 0.f;
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+        if (WITH_A) {
+            // Amatrix[k, m, src, det, nrg] = sum_{e in window(nrg)} RF[e,nrg] T_A[e,m,k]
+            const int MW = P.n_mat * P.nwt;
+            const int64_t colbase = colidx * MW;
+            const int64_t nstride = (int64_t)MW * ncols;
+            for (int idx = tid; idx < P.nrg_det * MW; idx += kThreads) {
+                const int n = idx / MW, mk = idx - n * MW;
+                float acc = 0.f;
+                for (int j = 0; j < W; j++) {
+                    const int el = winlo[n] + j - lo_e;
+                    if (el >= pe0 && el < pe1) acc = fmaf(rf[n * W + j], TA[(size_t)(el - pe0) * MW + mk], acc);
+                }
+                float *dst = args.A + colbase + (int64_t)n * nstride + mk;
+                if (pe0 == 0) *dst = acc;
+                else *dst += acc;
+            }
+            __syncthreads();
+        }
+    }
+
+    // ---- outputs: ray index src + det*SRC + nrg*SRC*DET (:404) ----
+#pragma unroll
+    for (int r = 0; r < kMaxRounds; r++) {
+        const int el = lane + 32 * r;
+        if (el < E) atomicAdd(&TN[el], (double)tn[r] - (double)tc[r]);
+    }
+    __syncthreads();
+    for (int n = tid; n < P.nrg_det; n += kThreads) {
+        const int64_t ray = colidx + (int64_t)n * ncols;
+        if (WITH_N) {
+            double acc = 0.0;
+            for (int j = 0; j < W; j++) acc += (double)rf[n * W + j] * TN[winlo[n] + j - lo_e];
+            args.N[ray] = (float)acc;
+        }
+        double c = 0.0;
+        for (int w = 0; w < kWarps; w++) {
+            const float2 k = Ck[w * P.nrg_det + n];
+            c += (double)k.x - (double)k.y;
+        }
+        args.C[ray] = (float)c;
+    }
+}
+
+template <bool WN, bool WA>
+cudaError_t launch_variant(const FwdArgs &a, size_t smem, cudaStream_t s)
+{
+    cudaError_t e = cudaFuncSetAttribute(k_fwd<WN, WA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid(a.P.n_det, a.P.n_src);
+    if (a.pairs) grid = dim3((unsigned)a.n_pairs, 1);
+    k_fwd<WN, WA><<<grid, kThreads, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+__global__ void k_gather_rays(const int64_t *__restrict__ idx, int64_t n, const float *__restrict__ Nc,
+                              const float *__restrict__ Cc, const float *__restrict__ Ac, int mw,
+                              float *__restrict__ N, float *__restrict__ C, float *__restrict__ A)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+        N[i] = Nc[idx[i]];
+        C[i] = Cc[idx[i]];
+    }
+    if (A)
+        for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * mw; t += stride)
+            A[t] = Ac[idx[t / mw] * mw + t % mw];
+}
+
+} // namespace
+
+cudaError_t launch_gather_rays(const int64_t *idx, int64_t n, const float *Nc, const float *Cc,
+                               const float *Ac, int mw, float *N, float *C, float *A, cudaStream_t s,
+                               int64_t *launches)
+{
+    if (n == 0) return cudaSuccess;
+    k_gather_rays<<<1024, 256, 0, s>>>(idx, n, Nc, Cc, Ac, mw, N, C, A);
+    if (launches) (*launches)++;
+    return cudaGetLastError();
+}
+
+size_t fast_forward_smem(const DevProblem &P, int e_pass, bool with_n, bool with_a)
+{
+    const int E = P.e_hi - P.e_lo + 1;
+    return fwd_layout(P, E, e_pass, with_n, with_a).total;
+}
+
+cudaError_t launch_fast_forward(const DevProblem &P, const SrcGeom *d_src, const FwdTables &T,
+                                const PrepBuffers &B, int nv, const float *Ifine, const int2 *pairs,
+                                int n_pairs, float *N, float *C, float *A, cudaStream_t s,
+                                int64_t *launches)
+{
+    FwdArgs a;
+    a.pairs = pairs;
+    a.n_pairs = n_pairs;
+    a.P = P;
+    a.sg = d_src;
+    a.T = T;
+    a.vox_xy = B.vox_xy;
+    a.vox_mat = B.vox_mat;
+    a.vox_na = B.vox_na;
+    a.vox_a2 = B.vox_a2;
+    a.cells = B.cells;
+    a.atten_src = B.atten_src;
+    a.s2u8 = B.s2u8;
+    a.Ifine = Ifine;
+    a.N = N;
+    a.C = C;
+    a.A = A;
+    a.nv = nv;
+    a.E = P.e_hi - P.e_lo + 1;
+    const double NWT = (double)P.nwt;
+    a.qpar_b = (float)P.dq0;
+    a.qpar_a = (float)((P.q_hi - P.q_lo - P.dq0 * NWT) / (NWT * NWT));
+    const bool with_n = (N != nullptr);
+    const bool with_a = (A != nullptr);
+    // energies per pass: all of them unless the model-matrix accumulator
+    // would push the block past ~110 KB of shared memory
+    int e_pass = a.E;
+    if (with_a) {
+        while (e_pass > 1 && fwd_layout(P, a.E, e_pass, with_n, true).total > 110 * 1024) e_pass = (e_pass + 1) / 2;
+    }
+    a.e_pass = e_pass;
+    const size_t smem = fwd_layout(P, a.E, e_pass, with_n, with_a).total;
+    if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
+    if (launches) (*launches)++;
+    if (nv == 0) {
+        // empty phantom: the reference writes zeros (integrate_diffraction.cu:364-409)
+        cudaError_t e = cudaSuccess;
+        return e;
+    }
+    if (with_n && with_a) return launch_variant<true, true>(a, smem, s);
+    if (with_n) return launch_variant<true, false>(a, smem, s);
+    if (with_a) return launch_variant<false, true>(a, smem, s);
+    return launch_variant<false, false>(a, smem, s);
+}
+
+} // namespace xrdt

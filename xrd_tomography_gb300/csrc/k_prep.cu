@@ -1,0 +1,175 @@
+// k_prep.cu -- per-call staging for the factored forward projector.
+//
+//  * k_build_cells: the (a1,a2) map as bilinear cells.  Replaces Copy2Vector
+//    (Copy2Vector.cu:9-23) and the cudaArray/texture set-up of
+//    Forward_XRD.cu:209-237: cell (ci,cj) holds the four texels
+//    (ci-1..ci, cj-1..cj) of a zero-bordered map as two float4, so one
+//    bilinear sample is two 16-byte loads with no border tests.  Also
+//    quantises the Compton table to u8 (integrate_diffraction.cu:66-74).
+//  * k_compact_voxels: non-empty voxels in the reference's loop order
+//    (nx outer, ny inner; integrate_diffraction.cu:173-178) and the material
+//    id check (ids above n_mat would index past Ifine in the reference).
+//  * k_voxel_compton: the (a1,a2) sample of the Compton table lookup per voxel
+//    (integrate_diffraction.cu:181-189), honouring the stale-coordinate quirk.
+//  * k_src_atten: the source-side line integral per (source, voxel), which
+//    the reference recomputes in every block (integrate_diffraction.cu:260).
+#include "xrdt_device.cuh"
+#include "walk.cuh"
+
+namespace xrdt {
+
+namespace {
+
+__global__ void k_build_cells(int nx, int ny, const float *__restrict__ a1, const float *__restrict__ a2,
+                              float4 *__restrict__ cells, const float *__restrict__ S2,
+                              unsigned char *__restrict__ s2u8, int ns2)
+{
+    const int64_t ncell = (int64_t)(nx + 1) * (ny + 1);
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncell; c += stride) {
+        const int ci = (int)(c % (nx + 1)), cj = (int)(c / (nx + 1));
+        float v[2][2][2];
+#pragma unroll
+        for (int dj = 0; dj < 2; dj++)
+#pragma unroll
+            for (int di = 0; di < 2; di++) {
+                const int i = ci - 1 + di, j = cj - 1 + dj;
+                const bool in = (i >= 0 && i < nx && j >= 0 && j < ny);
+                const int64_t idx = in ? (int64_t)i + (int64_t)j * nx : 0;
+                v[dj][di][0] = in ? a1[idx] : 0.f;
+                v[dj][di][1] = in ? a2[idx] : 0.f;
+            }
+        cells[2 * c] = make_float4(v[0][0][0], v[0][0][1], v[0][1][0], v[0][1][1]);
+        cells[2 * c + 1] = make_float4(v[1][0][0], v[1][0][1], v[1][1][0], v[1][1][1]);
+    }
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ns2; i += stride) {
+        const int q = floor_to_int((double)S2[i]);
+        s2u8[i] = (unsigned char)(q < 0 ? 0 : (q > 255 ? 255 : q));
+    }
+}
+
+// One block of 1024 threads: stream compaction in loop order.
+__global__ void __launch_bounds__(1024)
+k_compact_voxels(int nx, int ny, int n_mat, const int32_t *__restrict__ seg, int *__restrict__ vox_xy,
+                 int *__restrict__ vox_mat, int *__restrict__ counters)
+{
+    __shared__ int warp_cnt[32];
+    __shared__ int base_s;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (threadIdx.x == 0) base_s = 0;
+    __syncthreads();
+    int bad = 0;
+    const int64_t total = (int64_t)nx * ny;
+    for (int64_t L0 = 0; L0 < total; L0 += blockDim.x) {
+        const int64_t L = L0 + threadIdx.x;
+        int x = 0, y = 0, s = 0;
+        if (L < total) {
+            x = (int)(L / ny);
+            y = (int)(L % ny);
+            s = seg[(int64_t)x + (int64_t)y * nx];
+            bad |= (s > n_mat);
+        }
+        const bool keep = (L < total) && (s > 0) && (s <= n_mat);
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (lane == 0) warp_cnt[wid] = __popc(m);
+        __syncthreads();
+        int off = 0, tot = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+            if (w < wid) off += warp_cnt[w];
+            tot += warp_cnt[w];
+        }
+        const int base = base_s;
+        if (keep) {
+            const int pos = base + off + __popc(m & ((1u << lane) - 1u));
+            vox_xy[pos] = x | (y << 16);
+            vox_mat[pos] = s - 1;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) base_s = base + tot;
+        __syncthreads();
+    }
+    bad = __syncthreads_or(bad);
+    if (threadIdx.x == 0) {
+        counters[0] = base_s;
+        counters[1] = bad;
+    }
+}
+
+__global__ void k_voxel_compton(DevProblem P, const float *__restrict__ a1, const float *__restrict__ a2,
+                                const int *__restrict__ vox_xy, const int *__restrict__ counters,
+                                int *__restrict__ vox_na, float *__restrict__ vox_a2)
+{
+    const int nv = counters[0];
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
+        double sx = 0.0, sy = 0.0;  // stale coordinates start at (0,0)
+        int use = P.quirk_stale ? v - 1 : v;
+        if (use >= 0) {
+            const int xy = vox_xy[use];
+            sx = ((double)(xy & 0xffff) + 0.5) * P.vox;
+            sy = ((double)(xy >> 16) + 0.5) * P.vox;
+        }
+        double a1now, a2now;
+        bilinear_f64(a1, a2, P.nx, P.ny, sx, sy, &a1now, &a2now);
+        int na = floor_to_int((log2(fabs(a1now / a2now)) - P.a_min) / P.da_tab);
+        vox_na[v] = na < 0 ? 0 : (na >= P.na ? P.na - 1 : na);
+        vox_a2[v] = (float)a2now;
+    }
+}
+
+// One warp per (source, voxel): attenuator(Rsrc, Rvox) of integrate_diffraction.cu:260.
+__global__ void k_src_atten(DevProblem P, const SrcGeom *__restrict__ sg, const int *__restrict__ vox_xy,
+                            int nv, const float4 *__restrict__ cells, float2 *__restrict__ out)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t nwork = (int64_t)P.n_src * nv;
+    const int64_t wstride = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t w = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); w < nwork; w += wstride) {
+        const int src = (int)(w / nv), v = (int)(w % nv);
+        const int xy = vox_xy[v];
+        const double vx = ((double)(xy & 0xffff) + 0.5) * P.vox;
+        const double vy = ((double)(xy >> 16) + 0.5) * P.vox;
+        WalkSetup ws;
+        walk_setup(P, sg[src].Rsrc_x, sg[src].Rsrc_y, vx, vy, &ws);
+        const float2 A = walk_coop(cells, P.nx, P.ny, ws, (float)P.DQ, lane);
+        if (lane == 0) out[(int64_t)src * nv + v] = A;
+    }
+}
+
+} // namespace
+
+cudaError_t launch_prep_map(const DevProblem &P, const float *a1, const float *a2, const float *S2,
+                            PrepBuffers &B, cudaStream_t s, int64_t *launches)
+{
+    const int64_t ncell = (int64_t)(P.nx + 1) * (P.ny + 1);
+    int blocks = (int)((ncell + 255) / 256);
+    if (blocks > 4096) blocks = 4096;
+    k_build_cells<<<blocks, 256, 0, s>>>(P.nx, P.ny, a1, a2, B.cells, S2, B.s2u8, P.nq * P.na);
+    if (launches) (*launches)++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_prep_voxels(const DevProblem &P, const int32_t *seg, const float *a1,
+                               const float *a2, PrepBuffers &B, cudaStream_t s, int64_t *launches)
+{
+    k_compact_voxels<<<1, 1024, 0, s>>>(P.nx, P.ny, P.n_mat, seg, B.vox_xy, B.vox_mat, B.counters);
+    const int64_t nvox = (int64_t)P.nx * P.ny;
+    int blocks = (int)((nvox + 255) / 256);
+    if (blocks > 2048) blocks = 2048;
+    k_voxel_compton<<<blocks, 256, 0, s>>>(P, a1, a2, B.vox_xy, B.counters, B.vox_na, B.vox_a2);
+    if (launches) (*launches) += 2;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_src_atten(const DevProblem &P, const SrcGeom *d_src, int nv, PrepBuffers &B,
+                             cudaStream_t s, int64_t *launches)
+{
+    if (nv == 0) return cudaSuccess;
+    const int64_t warps = (int64_t)P.n_src * nv;
+    int64_t blocks = (warps + 7) / 8;
+    if (blocks > 152 * 64) blocks = 152 * 64;
+    k_src_atten<<<(int)blocks, 256, 0, s>>>(P, d_src, B.vox_xy, nv, B.cells, B.atten_src);
+    if (launches) (*launches)++;
+    return cudaGetLastError();
+}
+
+} // namespace xrdt

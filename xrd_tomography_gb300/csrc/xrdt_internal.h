@@ -1,0 +1,101 @@
+// xrdt_internal.h -- definitions shared by the host library and its kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+
+#include "../../include/xrdt.h"
+
+namespace xrdt {
+
+constexpr int kMaxSrc = 1 << 16;
+constexpr int kWarp = 32;
+
+// Problem constants in the form the kernels consume: everything the
+// reference derives inside integrate_diffraction (:81-168) that does not
+// depend on the voxel is derived once on the host, in double.
+struct DevProblem {
+    int nx, ny, n_src, n_col, n_row, n_det, nrg_src, nrg_det, dnrg;
+    int nwt, nqf, n_mat, nq, na;
+    int quirk_stale;
+    int e_lo, e_hi;        // source bins used by any detector window
+    long long kmax;        // maxBatch * NWT: cap on line-integral samples
+    double dEs, dEd, e_src_min, e_det_min;
+    double q_lo, q_hi, dq0, dq_fine;
+    double hbarc, mec2, kn0, kn1, kn2, rsqrt2pi, DQ;
+    double cx, cy, r_src, r_det, col_pitch, row_pitch, z0, focal, geomAdet, vox;
+    double tan_half, tan_full, sta, cta;
+    double q_min, q_max, a_min, a_max, dq_tab, da_tab;
+};
+
+// Per-source geometry (integrate_diffraction.cu:93-121), host-computed in double.
+struct SrcGeom {
+    double sphi, cphi;
+    double Rsrc_x, Rsrc_y;
+};
+
+// Energy-bin table of the source grid (integrate_diffraction.cu:269-292).
+struct EnergyRow {
+    double Esrc1, Esrc2, Esrc, ein;
+    float inv_f1, inv_f2;       // 1/ein^3, 1/KN(ein)
+    float wfac_hi, wfac_lo;     // 2*Esrc/hbarc as a float pair
+    float sig_c1, sig_c2;       // sigma^2 = c1*s^2 + c2*sg/s^2
+    float einf, Esrc1f, Esrc2f, pad;
+};
+
+std::string fmt(const char *f, ...);
+
+// ---- host-side builders (api.cu) ----
+int build_dev_problem(const xrdt_problem *p, float q_min, float q_max, float a_min,
+                      float a_max, DevProblem *d, std::string *err);
+
+// ---- kernels (launchers return cudaError_t of the launch) ----
+// k_plain.cu: FP64 at the reference launch shape.
+cudaError_t launch_plain_forward(const DevProblem &P, const SrcGeom *d_src,
+                                 const float *spectrum, const float *Ifine, const int32_t *seg,
+                                 const float *a1, const float *a2, const float *S2,
+                                 const double *d_coarse_q, const int64_t *d_rays, int64_t n_rays,
+                                 float *N, float *C, float *A, cudaStream_t s, int64_t *launches);
+
+// k_prep.cu
+struct PrepBuffers {
+    float4 *cells;          // [(ny+1)*(nx+1)*2] bilinear cells
+    int *vox_xy;            // [nx*ny] packed x | y << 16 of non-empty voxels
+    int *vox_mat;           // [nx*ny]
+    int *vox_na;            // [nx*ny] Compton table column per voxel
+    float *vox_a2;          // [nx*ny] a2 used by the Compton term
+    int *counters;          // [0] = number of non-empty voxels, [1] = bad material flag
+    float2 *atten_src;      // [n_src * nv] source-side line integrals
+    unsigned char *s2u8;    // [nq*na]
+};
+cudaError_t launch_prep_map(const DevProblem &P, const float *a1, const float *a2,
+                            const float *S2, PrepBuffers &B, cudaStream_t s, int64_t *launches);
+cudaError_t launch_prep_voxels(const DevProblem &P, const int32_t *seg, const float *a1,
+                               const float *a2, PrepBuffers &B, cudaStream_t s, int64_t *launches);
+cudaError_t launch_src_atten(const DevProblem &P, const SrcGeom *d_src, int nv, PrepBuffers &B,
+                             cudaStream_t s, int64_t *launches);
+
+// k_fwd.cu: factored FP32 forward over (src, det) pairs.
+struct FwdTables {
+    const EnergyRow *energy;   // [nrg_src]
+    const float *rf_win;       // [nrg_det][2*dnrg+1] spectrum window per detector bin
+    const float *offs;         // [nrg_det][2*dnrg+1] Esrc1(window bin) - Edet1(nrg)
+    const int *win_lo;         // [nrg_det] first source bin of each window
+    const int *win_n;          // [nrg_src][2] detector bins whose window holds e
+    const float2 *fine_q;      // [nqf] fine q axis as (hi, lo)
+    const float4 *coarse_q;    // [nwt] (q_hi, q_lo, dq, 0)
+};
+size_t fast_forward_smem(const DevProblem &P, int e_pass, bool with_n, bool with_a);
+// pairs (nullable): (src, det) of each block; outputs then go to the compact
+// layout [nrg_det][n_pairs] (and [nrg_det][n_pairs][n_mat*nwt] for A).
+cudaError_t launch_fast_forward(const DevProblem &P, const SrcGeom *d_src, const FwdTables &T,
+                                const PrepBuffers &B, int nv, const float *Ifine,
+                                const int2 *pairs, int n_pairs,
+                                float *N, float *C, float *A, cudaStream_t s, int64_t *launches);
+// out[i] = compact[idx[i]] for N, C and the rows of A (row length mw).
+cudaError_t launch_gather_rays(const int64_t *idx, int64_t n, const float *Nc, const float *Cc,
+                               const float *Ac, int mw, float *N, float *C, float *A, cudaStream_t s,
+                               int64_t *launches);
+
+} // namespace xrdt
