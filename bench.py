@@ -1,0 +1,371 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the XRD forward projector (one JSON line).
+
+Workload (N=1): the single-phantom forward model of the 256x256 synthetic
+phantom -- 8 materials, 180 views, 512 detector pixels x 64 energy bins,
+64-bin source spectrum, 128 fine q bins -- computing the coherent and Compton
+counts of all 5.9 M rays (the model matrix is not stored: matrix-free).
+A step is one forward projection.
+
+Metric: G ray-voxel-q/s, counted in reference-equivalent units: one
+(ray, non-empty voxel, source energy of the ray's window, fine q bin) term
+of the Nphotons sum, i.e. rays * voxels * (2*DNRG+1) * NQF per projection,
+the dense term count the reference evaluates (integrate_diffraction.cu:266-308).
+
+  value  -- device-resident inputs and outputs, CUDA events on the stream
+            the library launches on, L2 flushed (a 256 MB write) between steps
+  e2e    -- the same projection through the C ABI with host buffers: the
+            inputs are copied from pinned host memory and both outputs back
+            to pinned host memory inside the timed region
+  cpu_baseline -- the FP64 oracle (the reference's algorithm restated in C,
+            OpenMP over rays) on a bounded sample of rays on the host cores
+  plain_fp64_gpu -- the FP64 kernel at the reference's launch shape
+            (one block per ray) timed on a ray subset
+
+--impl reference times the CPU restatement of the reference's algorithm (the
+reference itself needs MATLAB and a removed CUDA texture API) with every host
+thread, each step a bounded sample of rays, in the same unit.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = 1            # index of the synthetic configuration
+FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU baseline sample")
+    ap.add_argument("--no-baselines", action="store_true", help="skip the CPU and plain-FP64 baselines")
+    return ap.parse_args()
+
+
+def ref_equiv_terms(inp, rays=None) -> float:
+    p = inp.problem
+    nv = int((inp.seg > 0).sum())
+    r = p.rays if rays is None else rays
+    return float(r) * nv * (2 * p.dnrg + 1) * p.nqf
+
+
+def workload_config(inp, **extra):
+    p = inp.problem
+    cfg = {
+        "workload": f"single-phantom forward projection, {p.nx}x{p.ny} voxels, {p.n_mat} materials, "
+                    f"{p.n_src} views, {p.n_col} px x {p.nrg_det} energy bins, {p.nrg_src}-bin source spectrum, "
+                    f"{p.nqf} fine q bins; Nphotons + Cphotons, matrix-free",
+        "rays": p.rays,
+        "nonempty_voxels": int((inp.seg > 0).sum()),
+        "energy_window": 2 * p.dnrg + 1,
+        "nqf": p.nqf,
+        "seed": inp.meta.get("seed"),
+    }
+    cfg.update(extra)
+    return cfg
+
+
+# ---- distributed plumbing (one process per GPU; weak scaling) --------------
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        dist.init_process_group(backend)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def all_max(ws, x, device=None):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---- clocks sampled during the timed region ---------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        finally:
+            os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["clock sampling unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        loaded = [s for s in sm if mx and s > 0.5 * max(mx)] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+
+
+# ---- CPU leg: the oracle on a bounded ray sample ------------------------------
+
+def cpu_sample_rate(inp, budget_s: float, rng_seed: int = 0):
+    """G ray-voxel-q/s of the FP64 oracle with all host threads, on a ray
+    sample sized to about budget_s seconds."""
+    from oracle import pyoracle
+    pyoracle.build(ref=False)
+    p = inp.problem
+    threads = os.cpu_count() or 1
+    rng = np.random.default_rng(rng_seed)
+    calib = rng.choice(p.rays, threads, replace=False)
+    t0 = time.perf_counter()
+    pyoracle.forward_rays(inp, calib, threads=threads)
+    t_calib = time.perf_counter() - t0
+    n = int(max(threads, min(p.rays, threads * max(1.0, budget_s / max(t_calib, 1e-3)))))
+    rays = rng.choice(p.rays, n, replace=False)
+    t0 = time.perf_counter()
+    pyoracle.forward_rays(inp, rays, threads=threads)
+    dt = time.perf_counter() - t0
+    return ref_equiv_terms(inp, n) / dt / 1e9, threads, n, dt
+
+
+def run_reference(args):
+    """--impl reference: the CPU restatement of the reference's algorithm."""
+    from xrd_tomography_gb300 import synth
+    ws, rank, _ = dist_setup(args)
+    if rank != 0:
+        barrier(ws)
+        return
+    inp = synth.config_inputs(WORKLOAD)
+    from oracle import pyoracle
+    pyoracle.build(ref=False)
+    p = inp.problem
+    threads = os.cpu_count() or 1
+    rng = np.random.default_rng(1)
+    step_rays = max(threads, 2 * threads)
+    for _ in range(args.warmup):
+        pyoracle.forward_rays(inp, rng.choice(p.rays, step_rays, replace=False), threads=threads)
+    t_total = 0.0
+    for _ in range(args.steps):
+        rays = rng.choice(p.rays, step_rays, replace=False)
+        t0 = time.perf_counter()
+        pyoracle.forward_rays(inp, rays, threads=threads)
+        t_total += time.perf_counter() - t0
+    v = ref_equiv_terms(inp, step_rays) * args.steps / t_total / 1e9
+    sample = (f"{step_rays} randomly drawn rays of the {p.rays}-ray projection per step "
+              f"(all {int((inp.seg > 0).sum())} voxels, every fine q bin, FP64)")
+    line = {
+        "impl": "reference", "metric": "forward projector throughput (reference-equivalent ray-voxel-q terms)",
+        "value": v, "unit": "G ray-voxel-q/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": workload_config(inp, sample_rays_per_step=step_rays),
+        "cpu_baseline": {"value": v, "unit": "G ray-voxel-q/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": v, "unit": "G ray-voxel-q/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    barrier(ws)
+
+
+# ---- GPU leg -------------------------------------------------------------------
+
+def run_ours(args):
+    import torch
+    import xrd_tomography_gb300 as xt
+    from xrd_tomography_gb300 import synth
+    from xrd_tomography_gb300 import build as lib_build
+
+    ws, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    lib_build.build()
+    lib_build.build_probe()
+    inp = synth.config_inputs(WORKLOAD)
+    p = inp.problem
+    stream = torch.cuda.Stream(dev)          # the library launches on this stream
+    torch.cuda.set_stream(stream)
+    ctx = xt.Context(local, stream=stream.cuda_stream)
+
+    host = [np.ascontiguousarray(x) for x in (inp.spectrum, inp.Ifine, inp.seg, inp.a1, inp.a2, inp.S2)]
+    d_in = [torch.from_numpy(x).to(dev) for x in host]
+    Nd = torch.empty(p.rays, dtype=torch.float32, device=dev)
+    Cd = torch.empty_like(Nd)
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    tables = (inp.q_min, inp.q_max, inp.a_min, inp.a_max)
+
+    def step_dev():
+        xt.forward(p, *d_in, *tables, Nphotons=Nd, Cphotons=Cd, want_amatrix=False, ctx=ctx,
+                   flags=xt.FWD_NO_SYNC)
+
+    for _ in range(args.warmup):
+        step_dev()
+    torch.cuda.synchronize(dev)
+
+    # device-resident timed region (profiling on: per-kernel events)
+    ctx.set_profiling(True)
+    launches0 = ctx.launches
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier(ws)
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            ev[i][0].record(stream)
+            step_dev()
+            ev[i][1].record(stream)
+        torch.cuda.synchronize(dev)
+    barrier(ws)
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    gpu_launches = ctx.launches - launches0
+    total_s = all_max(ws, sum(step_ms) / 1e3, dev)
+    units = ref_equiv_terms(inp) * args.steps * ws
+    value = units / total_s / 1e9
+    fwd_n, fwd_ms, fwd_work = ctx.kernel_stats(xt.api.KERNEL_FORWARD)
+    kstats = {name: ctx.kernel_stats(k)[:2] for name, k in
+              (("prep_map", xt.api.KERNEL_PREP_MAP), ("prep_voxels", xt.api.KERNEL_PREP_VOXELS),
+               ("src_atten", xt.api.KERNEL_SRC_ATTEN), ("forward", xt.api.KERNEL_FORWARD))}
+    ctx.set_profiling(False)
+    clocks = clk.summary()
+
+    # end-to-end through the C ABI with host buffers
+    pin = [torch.from_numpy(x).pin_memory() for x in host]
+    Nh = torch.empty(p.rays, dtype=torch.float32).pin_memory()
+    Ch = torch.empty_like(Nh).pin_memory()
+    h2d = sum(int(x.numel() * x.element_size()) for x in pin)
+    d2h = int(Nh.numel() * 4 + Ch.numel() * 4)
+
+    def step_e2e():
+        xt.forward(p, *pin, *tables, Nphotons=Nh, Cphotons=Ch, want_amatrix=False, ctx=ctx)
+
+    step_e2e()
+    ev2 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier(ws)
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        ev2[i][0].record(stream)
+        step_e2e()
+        ev2[i][1].record(stream)
+    torch.cuda.synchronize(dev)
+    e2e_s = all_max(ws, sum(a.elapsed_time(b) for a, b in ev2) / 1e3, dev)
+    e2e_value = units / e2e_s / 1e9
+
+    line = {
+        "metric": "forward projector throughput (reference-equivalent ray-voxel-q terms)",
+        "value": value, "unit": "G ray-voxel-q/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (FP64 geometry and integer decisions)",
+        "data": "synthetic (seeded phantom, patterns, spectrum)",
+        "config": workload_config(inp, parallelism=f"replicas x{ws}" if ws > 1 else "single GPU",
+                                  l2="flushed between steps (256 MB write)"),
+        "e2e": {"value": e2e_value, "unit": "G ray-voxel-q/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": gpu_launches,
+        "clocks": clocks,
+        "kernel_ms_per_step": {k: v[1] / max(1, args.steps) for k, v in kstats.items()},
+    }
+
+    if rank == 0:
+        # roofline of the dominant kernel: the forward kernel's exponentials
+        # (Gaussian q terms, attenuation and Compton factors) on the SFU
+        probe = __import__("ctypes").CDLL(lib_build.PROBE_LIB)
+        probe.xrdt_probe_peak.restype = __import__("ctypes").c_double
+        ex2_peak = probe.xrdt_probe_peak(1)
+        fma_peak = probe.xrdt_probe_peak(0)
+        fp64_peak = probe.xrdt_probe_peak(2)
+        per_launch_ms = fwd_ms / max(1, fwd_n)
+        work = fwd_work / max(1, fwd_n)
+        achieved = work / (per_launch_ms * 1e-3) / 1e9
+        line["roofline"] = {
+            "bound": "sfu", "achieved": achieved, "peak": ex2_peak / 1e9, "unit": "G exp2/s",
+            "frac": achieved / (ex2_peak / 1e9) if ex2_peak > 0 else None, "traffic": None,
+            "kernel": "k_fwd (factored forward projector)",
+            "work_per_launch": work, "launch_ms": per_launch_ms,
+            "peak_source": "measured on this GPU by xrdt_probe_peak (ex2.approx, all SMs)",
+        }
+        line["measured_peaks"] = {"fp32_tflops": fma_peak / 1e12, "sfu_ex2_gops": ex2_peak / 1e9,
+                                  "fp64_tflops": fp64_peak / 1e12}
+        if not args.no_baselines:
+            # plain FP64 kernel at the reference launch shape, on a ray subset
+            rng = np.random.default_rng(2)
+            sub = rng.choice(p.rays, 32, replace=False)
+            xt.forward_rays(p, sub[:4], *host, *tables, plain=True, ctx=ctx)
+            t0 = time.perf_counter()
+            xt.forward_rays(p, sub, *host, *tables, plain=True, ctx=ctx)
+            dt = time.perf_counter() - t0
+            plain_v = ref_equiv_terms(inp, sub.size) / dt / 1e9
+            line["plain_fp64_gpu"] = {"value": plain_v, "unit": "G ray-voxel-q/s", "sample_rays": int(sub.size),
+                                      "speedup_of_value": value / plain_v}
+            cv, cores, n, dt = cpu_sample_rate(inp, args.cpu_seconds)
+            line["cpu_baseline"] = {"value": cv, "unit": "G ray-voxel-q/s", "cores": cores, "kind": "port",
+                                    "sample": f"{n} randomly drawn rays of the {p.rays}-ray projection "
+                                              f"({dt:.1f} s, FP64 oracle, OpenMP over rays)"}
+        print(json.dumps(line), flush=True)
+    barrier(ws)
+    ctx.close()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

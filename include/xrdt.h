@@ -136,6 +136,26 @@ const char *xrdt_last_error(const xrdt_ctx *ctx);
 /* Number of kernels this context has launched since creation. */
 int64_t xrdt_ctx_launch_count(const xrdt_ctx *ctx);
 
+/* ---- profiling (no counterpart in the reference, which only times the
+ * whole MEX call with tic/toc, main.m:55,70) ----------------------------- */
+/* Kernel groups reported by xrdt_ctx_kernel_stats. */
+#define XRDT_KERNEL_PREP_MAP    0  /* bilinear cell map + Compton table quantisation */
+#define XRDT_KERNEL_PREP_VOXELS 1  /* voxel compaction + per-voxel Compton sample    */
+#define XRDT_KERNEL_SRC_ATTEN   2  /* source-side line integrals                     */
+#define XRDT_KERNEL_FORWARD     3  /* factored forward projector                     */
+#define XRDT_KERNEL_PLAIN       4  /* FP64 kernel at the reference launch shape      */
+#define XRDT_KERNEL_GATHER      5  /* ray-subset gather                              */
+#define XRDT_KERNEL_COUNT       6
+/* With profiling on, every launch is bracketed by CUDA events on the
+ * context's stream and the forward kernel counts the exponentials it
+ * evaluates.  Off by default; turning it on or off clears the statistics. */
+int32_t xrdt_ctx_set_profiling(xrdt_ctx *ctx, int32_t enable);
+/* Launch count, summed device milliseconds, and work units (exp2
+ * evaluations, forward kernel only) of one kernel group since profiling was
+ * switched on.  Synchronises the context's stream. */
+int32_t xrdt_ctx_kernel_stats(xrdt_ctx *ctx, int32_t kernel, int64_t *launches,
+                              double *total_ms, int64_t *work);
+
 /* ---- forward projector (replaces mexFunction, Forward_XRD.cu:76-301) -- */
 /* Inputs in the order of Forward_XRD's prhs[0..9] (Forward_XRD.cu:82-110):
  *   spectrum  f32 [nrg_src, nrg_det]   detector-smeared source spectrum

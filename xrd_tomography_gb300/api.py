@@ -24,6 +24,7 @@ LIB_PATH = os.path.join(HERE, "libxrdt.so")
 
 FWD_PLAIN_FP64 = 0x1
 FWD_NO_SYNC = 0x2
+KERNEL_PREP_MAP, KERNEL_PREP_VOXELS, KERNEL_SRC_ATTEN, KERNEL_FORWARD, KERNEL_PLAIN, KERNEL_GATHER = range(6)
 
 _P = ctypes.POINTER(Problem)
 _vp = ctypes.c_void_p
@@ -41,6 +42,9 @@ SIGNATURES = {
     "xrdt_ctx_synchronize": (ctypes.c_int32, [_vp]),
     "xrdt_last_error": (ctypes.c_char_p, [_vp]),
     "xrdt_ctx_launch_count": (ctypes.c_int64, [_vp]),
+    "xrdt_ctx_set_profiling": (ctypes.c_int32, [_vp, ctypes.c_int32]),
+    "xrdt_ctx_kernel_stats": (ctypes.c_int32, [_vp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int64),
+                                               ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)]),
     "xrdt_forward": (ctypes.c_int32, [_vp, _P, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_float, ctypes.c_float,
                                       ctypes.c_float, ctypes.c_float, _vp, _vp, _vp, ctypes.c_uint32]),
     "xrdt_forward_rays": (ctypes.c_int32, [_vp, _P, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_float,
@@ -122,6 +126,16 @@ class Context:
 
     def last_error(self) -> str:
         return (lib().xrdt_last_error(self.h) or b"").decode()
+
+    def set_profiling(self, on: bool):
+        _check(lib().xrdt_ctx_set_profiling(self.h, 1 if on else 0), self.h)
+
+    def kernel_stats(self, kernel: int):
+        """(launches, total device ms, work units) of one kernel group."""
+        n, ms, w = ctypes.c_int64(), ctypes.c_double(), ctypes.c_int64()
+        _check(lib().xrdt_ctx_kernel_stats(self.h, kernel, ctypes.byref(n), ctypes.byref(ms), ctypes.byref(w)),
+               self.h)
+        return n.value, ms.value, w.value
 
 
 _default_ctx = None

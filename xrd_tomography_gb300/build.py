@@ -79,6 +79,23 @@ def build(verbose: bool = False, force: bool = False, ptxas_v: bool = False) -> 
     return LIB
 
 
+PROBE_SRC = os.path.join(HERE, "probe", "peaks.cu")
+PROBE_LIB = os.path.join(HERE, "libxrdt_probe.so")
+
+
+def build_probe(force: bool = False) -> str:
+    """libxrdt_probe.so: the throughput probes the benchmark uses for its
+    roofline denominators."""
+    if not force and os.path.exists(PROBE_LIB) and os.path.getmtime(PROBE_LIB) >= os.path.getmtime(PROBE_SRC):
+        return PROBE_LIB
+    cmd = [nvcc(), *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", PROBE_SRC, "-o", PROBE_LIB]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed on {PROBE_SRC}:\n{r.stderr}")
+    return PROBE_LIB
+
+
 if __name__ == "__main__":
     v = "-v" in sys.argv
     print(build(verbose=v, force="-f" in sys.argv, ptxas_v=v))
+    print(build_probe(force="-f" in sys.argv))

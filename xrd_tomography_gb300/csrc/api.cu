@@ -28,6 +28,16 @@ struct xrdt_ctx {
     std::vector<void *> buf;
     std::vector<size_t> cap;
     int *h_counters = nullptr;  // pinned
+    // profiling: events bracketing launches, folded into totals on query
+    bool profiling = false;
+    struct Pending {
+        int kernel;
+        cudaEvent_t a, b;
+    };
+    std::vector<Pending> pending;
+    int64_t prof_launches[XRDT_KERNEL_COUNT] = {};
+    double prof_ms[XRDT_KERNEL_COUNT] = {};
+    unsigned long long *d_work = nullptr;  // exp2 evaluations of the forward kernel
 };
 
 namespace xrdt {
@@ -58,6 +68,41 @@ int fail(xrdt_ctx *c, int status, const std::string &msg)
 {
     if (c) c->err = msg;
     return status;
+}
+
+// Brackets one kernel group with events when profiling is on.
+struct ProfScope {
+    xrdt_ctx *ctx;
+    int kernel;
+    cudaEvent_t a = nullptr, b = nullptr;
+    ProfScope(xrdt_ctx *c, int k) : ctx(c), kernel(k)
+    {
+        if (!ctx->profiling) return;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cudaEventRecord(a, ctx->stream);
+    }
+    ~ProfScope()
+    {
+        if (!a) return;
+        cudaEventRecord(b, ctx->stream);
+        ctx->pending.push_back({kernel, a, b});
+    }
+};
+
+void fold_pending(xrdt_ctx *ctx)
+{
+    for (auto &p : ctx->pending) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(p.b) == cudaSuccess && cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+            ctx->prof_ms[p.kernel] += ms;
+            ctx->prof_launches[p.kernel] += 1;
+        }
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+    }
+    ctx->pending.clear();
+    cudaGetLastError();
 }
 
 #define CK(call)                                                                          \
@@ -370,11 +415,53 @@ int32_t xrdt_ctx_create(xrdt_ctx **out, int32_t device, void *stream)
     return XRDT_OK;
 }
 
+int32_t xrdt_ctx_set_profiling(xrdt_ctx *ctx, int32_t enable)
+{
+    if (!ctx) return XRDT_ERR_NULL;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    fold_pending(ctx);
+    for (int k = 0; k < XRDT_KERNEL_COUNT; k++) {
+        ctx->prof_launches[k] = 0;
+        ctx->prof_ms[k] = 0.0;
+    }
+    if (enable && !ctx->d_work) {
+        cudaError_t e = cudaMalloc((void **)&ctx->d_work, sizeof(unsigned long long));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(ctx, XRDT_ERR_ALLOC, "profiling counter allocation failed");
+        }
+    }
+    if (ctx->d_work) CK(cudaMemset(ctx->d_work, 0, sizeof(unsigned long long)));
+    ctx->profiling = enable != 0;
+    return XRDT_OK;
+}
+
+int32_t xrdt_ctx_kernel_stats(xrdt_ctx *ctx, int32_t kernel, int64_t *launches, double *total_ms, int64_t *work)
+{
+    if (!ctx) return XRDT_ERR_NULL;
+    if (kernel < 0 || kernel >= XRDT_KERNEL_COUNT) return fail(ctx, XRDT_ERR_DIMS, "unknown kernel group");
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    fold_pending(ctx);
+    if (launches) *launches = ctx->prof_launches[kernel];
+    if (total_ms) *total_ms = ctx->prof_ms[kernel];
+    if (work) {
+        unsigned long long w = 0;
+        if (kernel == XRDT_KERNEL_FORWARD && ctx->d_work)
+            CK(cudaMemcpy(&w, ctx->d_work, sizeof w, cudaMemcpyDeviceToHost));
+        *work = (int64_t)w;
+    }
+    return XRDT_OK;
+}
+
 int32_t xrdt_ctx_destroy(xrdt_ctx *ctx)
 {
     if (!ctx) return XRDT_ERR_NULL;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    fold_pending(ctx);
+    if (ctx->d_work) cudaFree(ctx->d_work);
     for (void *p : ctx->buf)
         if (p) cudaFree(p);
     if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
@@ -482,8 +569,9 @@ int forward_impl(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, co
     B.s2u8 = (unsigned char *)tmp;
     B.atten_src = nullptr;
 
+    { ProfScope ps(ctx, XRDT_KERNEL_PREP_VOXELS);
     CK(launch_prep_voxels(P, (const int32_t *)d_seg, (const float *)d_a1, (const float *)d_a2, B, st,
-                          &ctx->launches));
+                          &ctx->launches)); }
     CK(cudaMemcpyAsync(ctx->h_counters, B.counters, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     const int nv = ctx->h_counters[0];
@@ -510,6 +598,7 @@ int forward_impl(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, co
             if (n_list) CK(cudaMemcpyAsync(dr, ray_list, sizeof(int64_t) * n_list, cudaMemcpyHostToDevice, st));
             d_rays = (const int64_t *)dr;
         }
+        ProfScope ps(ctx, XRDT_KERNEL_PLAIN);
         CK(launch_plain_forward(P, (const SrcGeom *)d_srcg, (const float *)d_spec, (const float *)d_ifine,
                                 (const int32_t *)d_seg, (const float *)d_a1, (const float *)d_a2,
                                 (const float *)d_S2, (const double *)tmp, d_rays, n_list, dN, dC, dA, st,
@@ -613,9 +702,13 @@ int forward_impl(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, co
 
         if ((rc = get_buf(ctx, S_ASRC, sizeof(float2) * (size_t)p->n_src * nv, &tmp))) return rc;
         B.atten_src = (float2 *)tmp;
-        CK(launch_prep_map(P, (const float *)d_a1, (const float *)d_a2, (const float *)d_S2, B, st, &ctx->launches));
-        CK(launch_src_atten(P, (const SrcGeom *)d_srcg, nv, B, st, &ctx->launches));
+        { ProfScope ps(ctx, XRDT_KERNEL_PREP_MAP);
+          CK(launch_prep_map(P, (const float *)d_a1, (const float *)d_a2, (const float *)d_S2, B, st, &ctx->launches)); }
+        { ProfScope ps(ctx, XRDT_KERNEL_SRC_ATTEN);
+          CK(launch_src_atten(P, (const SrcGeom *)d_srcg, nv, B, st, &ctx->launches)); }
+        T.work = ctx->profiling ? ctx->d_work : nullptr;
         if (!ray_list) {
+            ProfScope ps(ctx, XRDT_KERNEL_FORWARD);
             CK(launch_fast_forward(P, (const SrcGeom *)d_srcg, T, B, nv, (const float *)d_ifine, nullptr, 0, dN,
                                    dC, dA, st, &ctx->launches));
         } else if (n_list > 0) {
@@ -643,9 +736,11 @@ int forward_impl(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, co
             if (dA && (rc = get_buf(ctx, S_AC, sizeof(float) * ncomp * MW, &dAc))) return rc;
             CK(cudaMemcpyAsync(dpairs, pairs.data(), sizeof(int2) * np, cudaMemcpyHostToDevice, st));
             CK(cudaMemcpyAsync(didx, idx.data(), sizeof(int64_t) * n_list, cudaMemcpyHostToDevice, st));
-            CK(launch_fast_forward(P, (const SrcGeom *)d_srcg, T, B, nv, (const float *)d_ifine,
-                                   (const int2 *)dpairs, np, (float *)dNc, (float *)dCc, (float *)dAc, st,
-                                   &ctx->launches));
+            { ProfScope ps(ctx, XRDT_KERNEL_FORWARD);
+              CK(launch_fast_forward(P, (const SrcGeom *)d_srcg, T, B, nv, (const float *)d_ifine,
+                                     (const int2 *)dpairs, np, (float *)dNc, (float *)dCc, (float *)dAc, st,
+                                     &ctx->launches)); }
+            ProfScope ps(ctx, XRDT_KERNEL_GATHER);
             CK(launch_gather_rays((const int64_t *)didx, n_list, (const float *)dNc, (const float *)dCc,
                                   (const float *)dAc, (int)MW, dN, dC, dA, st, &ctx->launches));
             // the pair list and index buffers are read asynchronously

@@ -185,6 +185,7 @@ k_fwd(const FwdArgs args)
     const int lo_e = P.e_lo;
     __syncthreads();
 
+    unsigned int nexp = 0;   // exp2 evaluations of this lane (profiling only)
     float tn[kMaxRounds], tc[kMaxRounds];
 #pragma unroll
     for (int r = 0; r < kMaxRounds; r++) tn[r] = tc[r] = 0.f;
@@ -288,6 +289,7 @@ k_fwd(const FwdArgs args)
                     const float rs = rsqrtf(sig2);
                     const float cexp = -0.5f * kLog2e / sig2;
                     const float PP = exp2f(-(Xin + Xout) * kLog2e);
+                    nexp += 1;
                     const float pref = PP * Wg * rsqrt2pi * rs;
                     const float half = kSig * sig2 * rs;
                     if (WITH_N) {
@@ -298,6 +300,7 @@ k_fwd(const FwdArgs args)
                         jhi = min(jhi, P.nqf - 1);
                         float acc = 0.f;
                         if (jlo <= jhi) {
+                            nexp += (unsigned)(jhi - jlo + 1);
                             const float2 q0 = fq[jlo];
                             const float d0 = (w_hi - q0.x) + (w_lo - q0.y);
                             const float *Ir = Is + m * P.nqf;
@@ -324,6 +327,7 @@ k_fwd(const FwdArgs args)
                             }
                         }
                         float *tar = TA + ((size_t)(el - pe0) * P.n_mat + m) * P.nwt;
+                        nexp += (unsigned)max(0, khi - klo + 1);
                         for (int k = klo; k <= khi; k++) {
                             const float4 c = cq[k];
                             const float d = (w_hi - c.x) + (w_lo - c.y);
@@ -365,6 +369,7 @@ k_fwd(const FwdArgs args)
                             const float f2 = fmaf(kn2 * eout, eout, fmaf(kn1, eout, kn0));
                             const float Xc = Asx / f1 + Asy / f2;
                             const float Pc = exp2f(-(Xin + Xc) * kLog2e);
+                            nexp += 1;
                             const float Cf = eratio * eratio * (eratio + inv_er - 1.f + cos2) * 0.5f;
                             const float base = Pc * gp * Cf * a2now * (float)S2[nq + na * P.nq];
                             const float span = dEsf * inv_er;   // Eout2 - Eout1
@@ -411,6 +416,13 @@ k_fwd(const FwdArgs args)
             }
             __syncthreads();
         }
+    }
+
+    if (args.T.work) {
+        unsigned long long w = nexp;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+        if (lane == 0) atomicAdd(args.T.work, w);
     }
 
     // ---- outputs: ray index src + det*SRC + nrg*SRC*DET (:404) ----

@@ -85,6 +85,7 @@ struct FwdTables {
     const int *win_n;          // [nrg_src][2] detector bins whose window holds e
     const float2 *fine_q;      // [nqf] fine q axis as (hi, lo)
     const float4 *coarse_q;    // [nwt] (q_hi, q_lo, dq, 0)
+    unsigned long long *work;  // nullable: counts the exp2 evaluations
 };
 size_t fast_forward_smem(const DevProblem &P, int e_pass, bool with_n, bool with_a);
 // pairs (nullable): (src, det) of each block; outputs then go to the compact
