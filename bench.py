@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU baseline sample")
     ap.add_argument("--no-baselines", action="store_true", help="skip the CPU and plain-FP64 baselines")
+    ap.add_argument("--workload", type=int, default=WORKLOAD, choices=[0, 1, 2, 4],
+                    help="synthetic configuration (1 is the benchmark; 0 and 2 are small profiling cases)")
     return ap.parse_args()
 
 
@@ -190,7 +192,7 @@ def run_reference(args):
     if rank != 0:
         barrier(ws)
         return
-    inp = synth.config_inputs(WORKLOAD)
+    inp = synth.config_inputs(args.workload)
     from oracle import pyoracle
     pyoracle.build(ref=False)
     p = inp.problem
@@ -235,7 +237,7 @@ def run_ours(args):
     dev = torch.device("cuda", local)
     lib_build.build()
     lib_build.build_probe()
-    inp = synth.config_inputs(WORKLOAD)
+    inp = synth.config_inputs(args.workload)
     p = inp.problem
     stream = torch.cuda.Stream(dev)          # the library launches on this stream
     torch.cuda.set_stream(stream)

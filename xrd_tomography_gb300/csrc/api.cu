@@ -631,7 +631,7 @@ int forward_impl(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, co
             r.pad = 0.f;
         }
         const int same = (p->nrg_src == p->nrg_det && p->e_src_min == p->e_det_min && p->e_src_max == p->e_det_max);
-        std::vector<float> rfw((size_t)p->nrg_det * W), offs((size_t)p->nrg_det * W);
+        std::vector<float> rfw((size_t)p->nrg_det * W);
         std::vector<int> wlo(p->nrg_det), wn(2 * (size_t)p->nrg_src);
         for (int e = 0; e < p->nrg_src; e++) {
             wn[2 * e] = p->nrg_det;
@@ -648,15 +648,23 @@ int forward_impl(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, co
             int lo, hi;
             src_nrg_range(P, same, n, &lo, &hi);
             wlo[n] = lo;
-            const double Ed1 = P.e_det_min + (double)n * P.dEd;
             for (int j = 0; j < W; j++) {
                 rfw[(size_t)n * W + j] = spec_h[(lo + j) + (size_t)n * p->nrg_src];
-                offs[(size_t)n * W + j] = (float)((P.e_src_min + (double)(lo + j) * P.dEs) - Ed1);
                 const int e = lo + j;
                 if (n < wn[2 * e]) wn[2 * e] = n;
                 if (n > wn[2 * e + 1]) wn[2 * e + 1] = n;
             }
         }
+        // Compton slots: for source bin e, slot s is detector bin win_n(e) + s
+        int sl = 1;
+        for (int e = 0; e < p->nrg_src; e++)
+            if (wn[2 * e + 1] >= wn[2 * e]) sl = std::max(sl, wn[2 * e + 1] - wn[2 * e] + 1);
+        std::vector<float> offs_e((size_t)p->nrg_src * sl, 0.f);
+        for (int e = 0; e < p->nrg_src; e++)
+            for (int s = 0; s < sl; s++) {
+                const double Ed1 = P.e_det_min + (double)(wn[2 * e] + s) * P.dEd;
+                offs_e[(size_t)e * sl + s] = (float)((P.e_src_min + (double)e * P.dEs) - Ed1);
+            }
         std::vector<float2> fq(p->nqf);
         for (int j = 0; j < p->nqf; j++) {
             const double q = P.q_lo + P.dq_fine * (0.5 + (double)j);
@@ -684,9 +692,10 @@ int forward_impl(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, co
         if ((rc = get_buf(ctx, S_RFWIN, sizeof(float) * rfw.size(), &d))) return rc;
         CK(cudaMemcpyAsync(d, rfw.data(), sizeof(float) * rfw.size(), cudaMemcpyHostToDevice, st));
         T.rf_win = (const float *)d;
-        if ((rc = get_buf(ctx, S_OFFS, sizeof(float) * offs.size(), &d))) return rc;
-        CK(cudaMemcpyAsync(d, offs.data(), sizeof(float) * offs.size(), cudaMemcpyHostToDevice, st));
-        T.offs = (const float *)d;
+        if ((rc = get_buf(ctx, S_OFFS, sizeof(float) * offs_e.size(), &d))) return rc;
+        CK(cudaMemcpyAsync(d, offs_e.data(), sizeof(float) * offs_e.size(), cudaMemcpyHostToDevice, st));
+        T.offs_e = (const float *)d;
+        T.sl = sl;
         if ((rc = get_buf(ctx, S_WINLO, sizeof(int) * wlo.size(), &d))) return rc;
         CK(cudaMemcpyAsync(d, wlo.data(), sizeof(int) * wlo.size(), cudaMemcpyHostToDevice, st));
         T.win_lo = (const int *)d;

@@ -10,8 +10,8 @@
 //    response afterwards: Nphotons[nrg] = sum_{e in window(nrg)} RF[e,nrg] T[e].
 //    The reference evaluates each (voxel, e) pair once per detector bin whose
 //    window holds e (11 times).
-//  * Gaussian q-resolution sums (:299-315) run over the bins within 7 sigma of
-//    the wavevector transfer only (the dropped tail is below 3e-11 of the
+//  * Gaussian q-resolution sums (:299-315) run over the bins within 7.5 sigma
+//    of the wavevector transfer only (each dropped term is below 7e-13 of the
 //    peak); the reference sums every fine bin.
 //  * The detector-side line integral is a warp-cooperative walk over the
 //    bilinear cell map; the source-side one comes from a per-(source, voxel)
@@ -28,6 +28,7 @@
 // and lane = source energy evaluates the (voxel, energy) term, so each lane
 // keeps the running sum of its own energies in registers.
 #include "xrdt_device.cuh"
+#include "ff.cuh"
 #include "walk.cuh"
 
 namespace xrdt {
@@ -36,8 +37,7 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kMaxRounds = 4;           // source bins per block <= 128
-constexpr float kSig = 7.0f;            // Gaussian window, in sigma
+constexpr float kSig = 7.5f;            // Gaussian window, in sigma (tail below 7e-13)
 constexpr float kLog2e = 1.4426950408889634f;
 
 __device__ __forceinline__ void kahan_add(float &s, float &c, float x)
@@ -48,31 +48,149 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x)
     s = t;
 }
 
+// SFU approximations with denormals flushed (no denormal fix-up code; the
+// arguments here are far from the denormal range)
+__device__ __forceinline__ float ex2_approx(float x)
+{
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float lg2_approx(float x)
+{
+    float y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rsqrt_approx(float x)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// Compton table bin of integrate_diffraction.cu:331-337 decided in FP64, as
+// the oracle decides it; used only when the FP32 value lies within 2e-4 of a
+// bin edge.  Kept out of line so that the rare FP64 path is a real branch
+// and not predicated into every iteration of the energy loop.
+__device__ __noinline__ int compton_bin_f64(const DevProblem &P, double ein, float omc_hi, float omc_lo)
+{
+    const double omcd = (double)omc_hi + (double)omc_lo;
+    const double sd = sqrt(fabs(omcd) / 2.0);
+    const double erd = 1.0 + ein * omcd;
+    const double wd = ein * sd;
+    const double l2d = log2(wd * sqrt(erd + wd * wd) / erd);
+    return floor_to_int((l2d - P.q_min) / P.dq_tab);
+}
+
+// FP64 walk set-up out of line, for the same reason.
+__device__ __noinline__ void walk_setup_f64(const DevProblem &P, double ex, double ey, double vx, double vy,
+                                            WalkSetup *w)
+{
+    walk_setup(P, ex, ey, vx, vy, w);
+}
+
+// Per-(source, pixel) constants of the scattering geometry.
+struct PairGeom {
+    ff Rsx, Rsy, Rdx, Rdy, Rdz;   // source and detector positions
+    ff k1;                        // tan(geomphi/2) / |nsrc_xy|
+    ff nsx2, nsy2;                // in-plane source orientation as pairs
+    float nsx, nsy, nsz, ndx, ndy, sphi, cphi;
+    float k2;                     // tan(geomphi) / |nsrc_xy|
+    float tan_full, adet12, vox2, focal2_12;
+};
+
+// Per-voxel results of the scattering geometry.
+struct VoxGeom {
+    ff s;        // sin(theta/2)
+    ff omc;      // 1 - cos(theta)
+    float sg;    // (sS2 + vV2 + dD2) / (|a|^2 |b|^2)
+    float gp;    // geom_src2vox * geom_vox2det
+    float Wg;    // gp * Rayleigh factor
+    float cos2;  // cos^2(theta)
+};
+
+// integrate_diffraction.cu:196-255 for one voxel.  a = voxel - source and
+// b = detector - voxel as float pairs; 1 - cos(theta) from the cross product
+// |a x b|^2 / (|a||b| (|a||b| + a.b)), which has no cancellation at small
+// angles; the blur vectors S = ((a x b) x a)/|a|^2 = b - (a.b/|a|^2) a and
+// D = ((a x b) x b)/|b|^2 = -a + (a.b/|b|^2) b in FP32.
+__device__ __forceinline__ VoxGeom vox_geom(const PairGeom &G, float vx, float vy)
+{
+    const ff ax = ff_fsub(vx, G.Rsx), ay = ff_fsub(vy, G.Rsy);
+    const ff proj = ff_add(ff_mul(ax, G.nsx2), ff_mul(ay, G.nsy2));
+    const ff az = ff_neg(ff_mul(proj, G.k1));          // Rvox_z; Rsrc_z = 0
+    const float Hvox = proj.hi * G.k2;
+    const ff bx = ff_add(G.Rdx, ff{-vx, 0.f}), by = ff_add(G.Rdy, ff{-vy, 0.f});
+    const ff bz = ff_sub(G.Rdz, az);
+    const ff ab = ff_add(ff_add(ff_mul(ax, bx), ff_mul(ay, by)), ff_mul(az, bz));
+    const ff an = ff_add(ff_add(ff_sqr(ax), ff_sqr(ay)), ff_sqr(az));
+    const ff bn = ff_add(ff_add(ff_sqr(bx), ff_sqr(by)), ff_sqr(bz));
+    const ff cx = ff_sub(ff_mul(ay, bz), ff_mul(az, by));
+    const ff cy = ff_sub(ff_mul(az, bx), ff_mul(ax, bz));
+    const ff cz = ff_sub(ff_mul(ax, by), ff_mul(ay, bx));
+    const ff cn = ff_add(ff_add(ff_sqr(cx), ff_sqr(cy)), ff_sqr(cz));
+    const ff nab = ff_sqrt(ff_mul(an, bn));
+    VoxGeom r;
+    if (ab.hi > 0.f) r.omc = ff_div(cn, ff_mul(nab, ff_add(nab, ab)));
+    else r.omc = ff_fsub(1.f, ff_div(ab, nab));
+    r.s = ff_sqrt(ff_mulf(r.omc, 0.5f));
+    const float costh = 1.f - r.omc.hi;
+    r.cos2 = costh * costh;
+    // FP32 remainder of the geometry
+    const float Ax = ax.hi, Ay = ay.hi, Az = az.hi, Bx = bx.hi, By = by.hi, Bz = bz.hi;
+    const float Cx = cx.hi, Cy = cy.hi, Cz = cz.hi, An = an.hi, Bn = bn.hi;
+    const float ia = __fdividef(1.f, An), ib = __fdividef(1.f, Bn);
+    const float Sx = (Cy * Az - Cz * Ay) * ia, Sy = (Cz * Ax - Cx * Az) * ia, Sz = (Cx * Ay - Cy * Ax) * ia;
+    const float Dx = (Cy * Bz - Cz * By) * ib, Dy = (Cz * Bx - Cx * Bz) * ib, Dz = (Cx * By - Cy * Bx) * ib;
+    const float Vx = -(Sx + Dx), Vy = -(Sy + Dy), Vz = -(Sz + Dz);
+    const float Dndet = Dx * G.ndx + Dy * G.ndy;
+    const float Snsrc = Sx * G.nsx + Sy * G.nsy + Sz * G.nsz;
+    const float dD2 = (Dx * Dx + Dy * Dy + Dz * Dz - Dndet * Dndet) * G.adet12;
+    const float vV2 = (G.vox2 * (Vx * Vx + Vy * Vy) + Hvox * Hvox * Vz * Vz) * (1.f / 12.f);
+    const float sS2 = (Sx * Sx + Sy * Sy + Sz * Sz - Snsrc * Snsrc) * G.focal2_12;
+    const float Rdotn = -G.sphi * Ax + G.cphi * Ay;
+    const float cospsi = Rdotn * rsqrtf(Ax * Ax + Ay * Ay);
+    const float gsv = cospsi * rsqrtf(An) * G.tan_full;
+    const float gvd = -(G.ndx * Bx + G.ndy * By) * rsqrtf(Bn * Bn * Bn);
+    r.gp = gsv * gvd;
+    r.Wg = r.gp * ((1.f + r.cos2) * 0.5f);
+    r.sg = (sS2 + vV2 + dD2) * ia * ib;
+    return r;
+}
+
 struct Layout {
-    size_t en, rf, offs, winlo, wn, ifine, fq, cq, s2, tn, cw, ck, ta, total;
+    size_t en, rf, offse, winlo, wn, ifine, fq, cq, s2, tn, tns, cs, ck, ta, total;
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
 // Shared-memory layout; identical on host and device.
-__host__ __device__ inline Layout fwd_layout(const DevProblem &P, int E, int e_pass, bool with_n,
+__host__ __device__ inline Layout fwd_layout(const DevProblem &P, int E, int SL, int e_pass, bool with_n,
                                              bool with_a)
 {
     Layout L;
     const int W = 2 * P.dnrg + 1;
     size_t o = 0;
     L.tn = o; o = align16(o + sizeof(double) * E);
+    L.tns = o; o = align16(o + sizeof(float2) * kWarps * E);
     L.ck = o; o = align16(o + sizeof(float2) * kWarps * P.nrg_det);
     L.en = o; o = align16(o + sizeof(float) * 9 * E);
     L.rf = o; o = align16(o + sizeof(float) * P.nrg_det * W);
-    L.offs = o; o = align16(o + sizeof(float) * P.nrg_det * W);
+    L.offse = o; o = align16(o + sizeof(float) * E * SL);
     L.winlo = o; o = align16(o + sizeof(int) * P.nrg_det);
     L.wn = o; o = align16(o + sizeof(int) * 2 * E);
-    L.cw = o; o = align16(o + sizeof(float) * kWarps * P.nrg_det);
-    L.ifine = o; if (with_n) o = align16(o + sizeof(float) * P.n_mat * P.nqf);
+    L.cs = o; o = align16(o + sizeof(float) * kWarps * E * SL);
+    L.ifine = o; if (with_n) o = align16(o + sizeof(float) * P.n_mat * (P.nqf + 1));
     L.fq = o; if (with_n) o = align16(o + sizeof(float2) * P.nqf);
     L.cq = o; if (with_a) o = align16(o + sizeof(float4) * P.nwt);
-    L.s2 = o; o = align16(o + (size_t)P.nq * P.na);
+    L.s2 = o; o = align16(o + sizeof(float) * (size_t)P.nq * P.na);
     L.ta = o; if (with_a) o = align16(o + sizeof(float) * (size_t)e_pass * P.n_mat * P.nwt);
     L.total = o;
     return L;
@@ -91,33 +209,36 @@ struct FwdArgs {
     float *N, *C, *A;
     const int2 *pairs;
     int n_pairs;
-    int nv, E, e_pass;
+    int nv, E, e_pass, sl;
     float qpar_a, qpar_b;   // coarse grid inversion: edge(n) = q_lo + b n + a n^2
 };
 
 template <bool WITH_N, bool WITH_A>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 3)
 k_fwd(const FwdArgs args)
 {
     extern __shared__ __align__(16) unsigned char sm[];
     const DevProblem &P = args.P;
     const int E = args.E;
     const int W = 2 * P.dnrg + 1;
-    const Layout L = fwd_layout(P, E, args.e_pass, WITH_N, WITH_A);
+    const int SL = args.sl;
+    const Layout L = fwd_layout(P, E, SL, args.e_pass, WITH_N, WITH_A);
     double *TN = (double *)(sm + L.tn);
+    float2 *TNs = (float2 *)(sm + L.tns);
     float2 *Ck = (float2 *)(sm + L.ck);
     float *en = (float *)(sm + L.en);   // SoA: 9 rows of E
     float *en_if1 = en, *en_if2 = en + E, *en_wh = en + 2 * E, *en_wl = en + 3 * E;
-    float *en_c1 = en + 4 * E, *en_c2 = en + 5 * E, *en_ein = en + 6 * E;
+    float *en_c1 = en + 4 * E, *en_c2 = en + 5 * E, *en_ein = en + 6 * E, *en_e1 = en + 7 * E;
+    float *en_wn0f = en + 8 * E;   // first detector bin of wn as a float
     float *rf = (float *)(sm + L.rf);
-    float *offs = (float *)(sm + L.offs);
+    float *offse = (float *)(sm + L.offse);   // [E][SL] Esrc1(e) - Edet1(wn_lo(e) + s)
     int *winlo = (int *)(sm + L.winlo);
     int *wn = (int *)(sm + L.wn);
-    float *Cw = (float *)(sm + L.cw);
+    float *CS = (float *)(sm + L.cs);         // [warp][E][SL] Compton sums of the current chunk
     float *Is = (float *)(sm + L.ifine);
     float2 *fq = (float2 *)(sm + L.fq);
     float4 *cq = (float4 *)(sm + L.cq);
-    unsigned char *S2 = sm + L.s2;
+    float *S2 = (float *)(sm + L.s2);   // quantised table as floats (no u8 conversion in the loop)
     float *TA = (float *)(sm + L.ta);
 
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -146,49 +267,73 @@ k_fwd(const FwdArgs args)
         en_c1[i] = r.sig_c1;
         en_c2[i] = r.sig_c2;
         en_ein[i] = r.einf;
+        en_e1[i] = r.Esrc1f;
         TN[i] = 0.0;
+        for (int w = 0; w < kWarps; w++) TNs[w * E + i] = make_float2(0.f, 0.f);
         wn[2 * i] = args.T.win_n[2 * (P.e_lo + i)];
+        en_wn0f[i] = (float)wn[2 * i];
         wn[2 * i + 1] = args.T.win_n[2 * (P.e_lo + i) + 1];
     }
-    for (int i = tid; i < P.nrg_det * W; i += kThreads) {
-        rf[i] = args.T.rf_win[i];
-        offs[i] = args.T.offs[i];
-    }
+    for (int i = tid; i < P.nrg_det * W; i += kThreads) rf[i] = args.T.rf_win[i];
+    for (int i = tid; i < E * SL; i += kThreads) offse[i] = args.T.offs_e[P.e_lo * SL + i];
+    for (int i = tid; i < kWarps * E * SL; i += kThreads) CS[i] = 0.f;
     for (int i = tid; i < P.nrg_det; i += kThreads) winlo[i] = args.T.win_lo[i];
-    for (int i = tid; i < kWarps * P.nrg_det; i += kThreads) {
-        Cw[i] = 0.f;
-        Ck[i] = make_float2(0.f, 0.f);
-    }
+    for (int i = tid; i < kWarps * P.nrg_det; i += kThreads) Ck[i] = make_float2(0.f, 0.f);
     if (WITH_N) {
-        for (int i = tid; i < P.n_mat * P.nqf; i += kThreads) Is[i] = __ldg(args.Ifine + i);
+        // rows of nqf + 1: each material's pattern and a zero pad
+        for (int i = tid; i < P.n_mat * (P.nqf + 1); i += kThreads) {
+            const int mm = i / (P.nqf + 1), j = i - mm * (P.nqf + 1);
+            Is[i] = j < P.nqf ? __ldg(args.Ifine + mm * P.nqf + j) : 0.f;
+        }
         for (int i = tid; i < P.nqf; i += kThreads) fq[i] = args.T.fine_q[i];
     }
     if (WITH_A)
         for (int i = tid; i < P.nwt; i += kThreads) cq[i] = args.T.coarse_q[i];
-    for (int i = tid; i < P.nq * P.na; i += kThreads) S2[i] = args.s2u8[i];
+    for (int i = tid; i < P.nq * P.na; i += kThreads) S2[i] = (float)args.s2u8[i];
 
     // ---- per-(source, pixel) geometry, integrate_diffraction.cu:81-128 ----
     const SrcGeom g = args.sg[src];
     double Rdet_x, Rdet_y, Rdet_z;
     det_position(P, g.sphi, g.cphi, det, &Rdet_x, &Rdet_y, &Rdet_z);
-    const double ndet_x = g.sphi, ndet_y = -g.cphi;
-    const double nsrc_x = -g.sphi * P.sta, nsrc_y = g.cphi * P.sta, nsrc_z = -P.cta;
-    const double nsrc_xy = sqrt(nsrc_x * nsrc_x + nsrc_y * nsrc_y);
+    PairGeom G;
+    G.Rsx = ff_from_double(g.Rsrc_x);
+    G.Rsy = ff_from_double(g.Rsrc_y);
+    G.Rdx = ff_from_double(Rdet_x);
+    G.Rdy = ff_from_double(Rdet_y);
+    G.Rdz = ff_from_double(Rdet_z);
+    {
+        const double nsx = -g.sphi * P.sta, nsy = g.cphi * P.sta, nsz = -P.cta;
+        const double nsxy = sqrt(nsx * nsx + nsy * nsy);
+        G.nsx = (float)nsx;
+        G.nsy = (float)nsy;
+        G.nsx2 = ff_from_double(nsx);
+        G.nsy2 = ff_from_double(nsy);
+        G.nsz = (float)nsz;
+        G.k1 = ff_from_double(P.tan_half / nsxy);
+        G.k2 = (float)(P.tan_full / nsxy);
+    }
+    G.ndx = (float)g.sphi;
+    G.ndy = (float)(-g.cphi);
+    G.sphi = (float)g.sphi;
+    G.cphi = (float)g.cphi;
+    G.tan_full = (float)P.tan_full;
+    G.adet12 = (float)(P.geomAdet / 12.0);
+    G.vox2 = (float)(P.vox * P.vox);
+    G.focal2_12 = (float)(P.focal * P.focal / 12.0);
+    const float Rdxf = (float)Rdet_x, Rdyf = (float)Rdet_y;
     const float rsqrt2pi = (float)P.rsqrt2pi;
-    const float DQf = (float)P.DQ;
+    const float DQf = (float)P.DQ, inv_DQ = (float)(1.0 / P.DQ);
     const float dqf_hi = (float)P.dq_fine, dqf_lo = (float)(P.dq_fine - (double)dqf_hi);
     const float inv_dqf = (float)(1.0 / P.dq_fine), qlo_f = (float)P.q_lo;
     const float kn0 = (float)P.kn0, kn1 = (float)P.kn1, kn2 = (float)P.kn2;
     const float edmin = (float)P.e_det_min, inv_dEd = (float)(1.0 / P.dEd), dEdf = (float)P.dEd;
-    const float dEsf = (float)P.dEs;
+    const float dEsf = (float)P.dEs, esmin = (float)P.e_src_min;
     const float qmin_t = (float)P.q_min, inv_dqt = (float)(1.0 / P.dq_tab);
     const int lo_e = P.e_lo;
     __syncthreads();
 
     unsigned int nexp = 0;   // exp2 evaluations of this lane (profiling only)
-    float tn[kMaxRounds], tc[kMaxRounds];
-#pragma unroll
-    for (int r = 0; r < kMaxRounds; r++) tn[r] = tc[r] = 0.f;
+    float2 *TNw = TNs + wid * E;   // this warp's Kahan sums per source energy
 
     const int nv = args.nv;
     const int nchunks = (nv + 31) >> 5;
@@ -199,50 +344,19 @@ k_fwd(const FwdArgs args)
             __syncthreads();
         }
         for (int chunk = wid; chunk < nchunks; chunk += kWarps) {
-            // ---- lane = voxel: FP64 geometry (integrate_diffraction.cu:192-255) ----
-            const int v = chunk * 32 + lane;
-            const bool valid = v < nv;
-            const int vv = valid ? v : nv - 1;
-            const int xy = args.vox_xy[vv];
-            const double vx = ((double)(xy & 0xffff) + 0.5) * P.vox;
-            const double vy = ((double)(xy >> 16) + 0.5) * P.vox;
-            const double ax = vx - g.Rsrc_x, ay = vy - g.Rsrc_y;
-            const double proj = ax * nsrc_x + ay * nsrc_y;
-            const double Rvox_z = -proj / nsrc_xy * P.tan_half;
-            const double Hvox = proj / nsrc_xy * P.tan_full;
-            const double az = Rvox_z;
-            const double bx = Rdet_x - vx, by = Rdet_y - vy, bz = Rdet_z - Rvox_z;
-            const double ab = ax * bx + ay * by + az * bz;
-            const double anorm2 = ax * ax + ay * ay + az * az;
-            const double bnorm2 = bx * bx + by * by + bz * bz;
-            const double costheta = ab * (1.0 / sqrt(anorm2)) * (1.0 / sqrt(bnorm2));
-            const double omc = 1.0 - costheta;
-            const double sth = sqrt(fabs(omc) / 2.0);
-            const double Sx = bx - ab * ax / anorm2, Sy = by - ab * ay / anorm2, Sz = bz - ab * az / anorm2;
-            const double Dx = -ax + ab * bx / bnorm2, Dy = -ay + ab * by / bnorm2, Dz = -az + ab * bz / bnorm2;
-            const double Vx = -(Sx + Dx), Vy = -(Sy + Dy), Vz = -(Sz + Dz);
-            const double Dndet = Dx * ndet_x + Dy * ndet_y;
-            const double Snsrc = Sx * nsrc_x + Sy * nsrc_y + Sz * nsrc_z;
-            const double dD2 = (Dx * Dx + Dy * Dy + Dz * Dz - Dndet * Dndet) * P.geomAdet / 12.0;
-            const double vV2 = (P.vox * P.vox * (Vx * Vx + Vy * Vy) + Hvox * Hvox * Vz * Vz) / 12.0;
-            const double sS2 = (Sx * Sx + Sy * Sy + Sz * Sz - Snsrc * Snsrc) * P.focal * P.focal / 12.0;
-            const double Rdotn = -g.sphi * ax + g.cphi * ay;
-            const double cospsi = Rdotn * (1.0 / sqrt(ax * ax + ay * ay));
-            const double gsv = cospsi * (1.0 / sqrt(anorm2)) * P.tan_full;
-            const double gvd = -(ndet_x * bx + ndet_y * by) * (1.0 / sqrt(bnorm2 * bnorm2 * bnorm2));
-            const double gpd = gsv * gvd;
-            const float s_hi = (float)sth, s_lo = (float)(sth - (double)s_hi);
-            const float omc_hi = (float)omc, omc_lo = (float)(omc - (double)omc_hi);
-            const float sgv = (float)((sS2 + vV2 + dD2) / anorm2 / bnorm2);
-            const float gpv = (float)gpd;
-            const float Wgv = (float)(gpd * ((1.0 + costheta * costheta) / 2.0));
-            const float cos2v = (float)(costheta * costheta);
-            const int mv = args.vox_mat[vv];
-            const int nav = args.vox_na[vv];
-            const float a2v = args.vox_a2[vv];
-            const float2 Asv = args.atten_src[(int64_t)src * nv + vv];
+            // ---- lane = voxel: scattering geometry (integrate_diffraction.cu:192-255) ----
+            const int v = min(chunk * 32 + lane, nv - 1);
+            const int xy = args.vox_xy[v];
+            const float vx = ((float)(xy & 0xffff) + 0.5f) * (float)P.vox;
+            const float vy = ((float)(xy >> 16) + 0.5f) * (float)P.vox;
+            const VoxGeom vg = vox_geom(G, vx, vy);
+            const int mv = args.vox_mat[v];
+            const int nav = args.vox_na[v];
+            const float a2v = args.vox_a2[v];
+            const float2 Asv = args.atten_src[(int64_t)src * nv + v];
             WalkSetup ws;
-            walk_setup(P, Rdet_x, Rdet_y, vx, vy, &ws);
+            if (!walk_setup_f32(P, Rdxf, Rdyf, vx, vy, inv_DQ, &ws))
+                walk_setup_f64(P, Rdet_x, Rdet_y, (double)vx, (double)vy, &ws);
 
             const int nin = min(32, nv - chunk * 32);
             for (int i = 0; i < nin; i++) {
@@ -255,24 +369,23 @@ k_fwd(const FwdArgs args)
                 // labels as at integrate_diffraction.cu:259-260: the detector-side
                 // integral feeds Pin, the source-side one Pout.
                 const float2 Ad = walk_coop(args.cells, P.nx, P.ny, wi, DQf, lane);
-                const float sh = __shfl_sync(0xffffffffu, s_hi, i);
-                const float sl = __shfl_sync(0xffffffffu, s_lo, i);
-                const float oh = __shfl_sync(0xffffffffu, omc_hi, i);
-                const float ol = __shfl_sync(0xffffffffu, omc_lo, i);
-                const float sg = __shfl_sync(0xffffffffu, sgv, i);
-                const float gp = __shfl_sync(0xffffffffu, gpv, i);
-                const float Wg = __shfl_sync(0xffffffffu, Wgv, i);
-                const float cos2 = __shfl_sync(0xffffffffu, cos2v, i);
+                const float sh = __shfl_sync(0xffffffffu, vg.s.hi, i);
+                const float sl = __shfl_sync(0xffffffffu, vg.s.lo, i);
+                const float oh = __shfl_sync(0xffffffffu, vg.omc.hi, i);
+                const float ol = __shfl_sync(0xffffffffu, vg.omc.lo, i);
+                const float sg = __shfl_sync(0xffffffffu, vg.sg, i);
+                const float gp = __shfl_sync(0xffffffffu, vg.gp, i);
+                const float Wg = __shfl_sync(0xffffffffu, vg.Wg, i);
+                const float cos2 = __shfl_sync(0xffffffffu, vg.cos2, i);
                 const int m = __shfl_sync(0xffffffffu, mv, i);
                 const int na = __shfl_sync(0xffffffffu, nav, i);
                 const float a2now = __shfl_sync(0xffffffffu, a2v, i);
                 const float Asx = __shfl_sync(0xffffffffu, Asv.x, i);
                 const float Asy = __shfl_sync(0xffffffffu, Asv.y, i);
                 const float s2f = sh * sh;
-#pragma unroll
-                for (int r = 0; r < kMaxRounds; r++) {
-                    const int el = lane + 32 * r;
-                    if (el < pe0 || el >= pe1) continue;
+                const float sg_s2 = __fdividef(sg, s2f);
+#pragma unroll 1
+                for (int el = pe0 + lane; el < pe1; el += 32) {
                     // ---- (voxel, source energy) term, :266-356 ----
                     const float if1 = en_if1[el], if2 = en_if2[el];
                     const float Xin = fmaf(Ad.x, if1, Ad.y * if2);
@@ -285,32 +398,45 @@ k_fwd(const FwdArgs args)
                         w_lo = w_lo - (t - w_hi);
                         w_hi = t;
                     }
-                    const float sig2 = fmaf(en_c1[el], s2f, en_c2[el] * sg / s2f);
+                    const float sig2 = fmaf(en_c1[el], s2f, en_c2[el] * sg_s2);
                     const float rs = rsqrtf(sig2);
-                    const float cexp = -0.5f * kLog2e / sig2;
-                    const float PP = exp2f(-(Xin + Xout) * kLog2e);
+                    const float cexp = -0.5f * kLog2e * rs * rs;
+                    const float PP = ex2_approx(-(Xin + Xout) * kLog2e);
                     nexp += 1;
                     const float pref = PP * Wg * rsqrt2pi * rs;
                     const float half = kSig * sig2 * rs;
                     if (WITH_N) {
                         const float jc = (w_hi - qlo_f) * inv_dqf - 0.5f;
-                        int jlo = (int)ceilf(jc - half * inv_dqf);
-                        int jhi = (int)floorf(jc + half * inv_dqf);
-                        jlo = max(jlo, 0);
-                        jhi = min(jhi, P.nqf - 1);
+                        const int jlo = max(ceil_nc(jc - half * inv_dqf), 0);
+                        int jhi = min(floor_nc(jc + half * inv_dqf), P.nqf - 1);
                         float acc = 0.f;
                         if (jlo <= jhi) {
+                            // an even number of bins, so the pair loop has no tail: an
+                            // odd window takes one more bin (an exact term of the full
+                            // sum, or the zero pad after the last bin).  A tail would make
+                            // the compiler rebuild the float counter from the trip count
+                            // through an int-to-float conversion, which this GPU issues
+                            // on its FP64 pipe.
+                            jhi += (jhi - jlo + 1) & 1;
                             nexp += (unsigned)(jhi - jlo + 1);
                             const float2 q0 = fq[jlo];
                             const float d0 = (w_hi - q0.x) + (w_lo - q0.y);
-                            const float *Ir = Is + m * P.nqf;
-                            float t = 0.f;
-                            for (int j = jlo; j <= jhi; j++, t += 1.f) {
-                                const float d = fmaf(-t, dqf_lo, fmaf(-t, dqf_hi, d0));
-                                acc = fmaf(exp2f(cexp * d * d), Ir[j], acc);
+                            const float *Ir = Is + m * (P.nqf + 1) + jlo;
+                            const float *Iend = Ir + (jhi - jlo + 1);
+                            float acc2 = 0.f;
+                            float t0 = 0.f;   // bin offset as a float: no conversion in the loop
+                            for (; Ir < Iend; Ir += 2, t0 += 2.f) {
+                                const float t1 = t0 + 1.f;
+                                const float da = fmaf(-t0, dqf_lo, fmaf(-t0, dqf_hi, d0));
+                                const float db = fmaf(-t1, dqf_lo, fmaf(-t1, dqf_hi, d0));
+                                acc = fmaf(ex2_approx(cexp * da * da), Ir[0], acc);
+                                acc2 = fmaf(ex2_approx(cexp * db * db), Ir[1], acc2);
                             }
+                            acc += acc2;
                         }
-                        kahan_add(tn[r], tc[r], pref * dqf_hi * acc);
+                        float2 k = TNw[el];
+                        kahan_add(k.x, k.y, pref * dqf_hi * acc);
+                        TNw[el] = k;
                     }
                     if (WITH_A) {
                         // coarse bins near w: invert edge(n) = q_lo + b n + a n^2
@@ -322,8 +448,8 @@ k_fwd(const FwdArgs args)
                             if (da >= 0.f && db >= 0.f) {
                                 const float na_ = 2.f * qa / (b + sqrtf(da));
                                 const float nb_ = 2.f * qb / (b + sqrtf(db));
-                                klo = max(klo, (int)floorf(na_) - 1);
-                                khi = min(khi, (int)floorf(nb_) + 1);
+                                klo = max(klo, floor_nc(na_) - 1);
+                                khi = min(khi, floor_nc(nb_) + 1);
                             }
                         }
                         float *tar = TA + ((size_t)(el - pe0) * P.n_mat + m) * P.nwt;
@@ -331,7 +457,7 @@ k_fwd(const FwdArgs args)
                         for (int k = klo; k <= khi; k++) {
                             const float4 c = cq[k];
                             const float d = (w_hi - c.x) + (w_lo - c.y);
-                            atomicAdd(tar + k, pref * c.z * exp2f(cexp * d * d));
+                            atomicAdd(tar + k, pref * c.z * ex2_approx(cexp * d * d));
                         }
                     }
                     // ---- Compton, :318-356 ----
@@ -339,61 +465,76 @@ k_fwd(const FwdArgs args)
                         const float ein = en_ein[el];
                         const float x = ein * oh;                 // eratio - 1
                         const float eratio = 1.f + x;
-                        const float inv_er = 1.f / eratio;
+                        const float inv_er = rcp_approx(eratio);
                         const int eg = lo_e + el;
                         // detector bins whose window holds e and whose channel the
                         // outgoing range [E1, E2]/eratio can overlap
-                        const float Eo_lo = (float)(P.e_src_min) + (float)eg * dEsf;
-                        int n0 = max(wn[2 * el], (int)floorf((Eo_lo * inv_er - edmin) * inv_dEd) - 1);
-                        int n1 = min(wn[2 * el + 1], (int)floorf(((Eo_lo + dEsf) * inv_er - edmin) * inv_dEd) + 1);
+                        const float Eo_lo = en_e1[el];
+                        float fn0;
+                        int n0 = floor_nc((Eo_lo * inv_er - edmin) * inv_dEd, &fn0) - 1;
+                        fn0 -= 1.f;
+                        if (n0 < wn[2 * el]) {
+                            n0 = wn[2 * el];
+                            fn0 = en_wn0f[el];
+                        }
+                        const int n1 = min(wn[2 * el + 1], floor_nc(((Eo_lo + dEsf) * inv_er - edmin) * inv_dEd) + 1);
                         if (n0 <= n1) {
                             const float wC = ein * sh;
-                            const float l2 = log2f(wC * sqrtf(eratio + wC * wC) * inv_er);
+                            const float arg = eratio + wC * wC;
+                            const float l2 = lg2_approx(wC * arg * rsqrt_approx(arg) * inv_er);
                             const float tq = (l2 - qmin_t) * inv_dqt;
-                            const float fr = tq - floorf(tq);
-                            int nq;
-                            if (fr > 2e-4f && fr < 1.f - 2e-4f) {
-                                nq = (int)floorf(tq);
-                            } else {  // near a bin edge: decide in FP64 as the oracle does
-                                const double eind = args.T.energy[eg].ein;
-                                const double omcd = (double)oh + (double)ol;
-                                const double sd = sqrt(fabs(omcd) / 2.0);
-                                const double erd = 1.0 + eind * omcd;
-                                const double wd = eind * sd;
-                                const double l2d = log2(wd * sqrt(erd + wd * wd) / erd);
-                                nq = floor_to_int((l2d - P.q_min) / P.dq_tab);
-                            }
+                            float ftq;
+                            int nq = floor_nc(tq, &ftq);
+                            const float fr = tq - ftq;
+                            if (!(fr > 2e-4f && fr < 1.f - 2e-4f))  // near a table edge
+                                nq = compton_bin_f64(P, args.T.energy[eg].ein, oh, ol);
                             nq = nq < 0 ? 0 : (nq >= P.nq ? P.nq - 1 : nq);
                             const float eout = ein * inv_er;
                             const float f1 = eout * eout * eout;
                             const float f2 = fmaf(kn2 * eout, eout, fmaf(kn1, eout, kn0));
-                            const float Xc = Asx / f1 + Asy / f2;
-                            const float Pc = exp2f(-(Xin + Xc) * kLog2e);
+                            const float Xc = fmaf(Asx, rcp_approx(f1), Asy * rcp_approx(f2));
+                            const float Pc = ex2_approx(-(Xin + Xc) * kLog2e);
                             nexp += 1;
                             const float Cf = eratio * eratio * (eratio + inv_er - 1.f + cos2) * 0.5f;
-                            const float base = Pc * gp * Cf * a2now * (float)S2[nq + na * P.nq];
+                            const float base = Pc * gp * Cf * a2now * S2[nq + na * P.nq];
                             const float span = dEsf * inv_er;   // Eout2 - Eout1
-                            for (int n = n0; n <= n1; n++) {
-                                const int j = eg - winlo[n];
-                                const float Ed1 = edmin + (float)n * dEdf;
+                            const float inv_span = rcp_approx(span);
+                            // this lane's (warp, energy) row of chunk sums, indexed by n;
+                            // the spectrum weight RF[e, n] is applied when the chunk is
+                            // flushed, so no two lanes ever write the same word
+                            const int wlo = wn[2 * el];
+                            float *cs = CS + ((size_t)wid * E + el) * SL - wlo;
+                            const float *oe = offse + (size_t)el * SL - wlo;
+                            const float bs = base * inv_span;
+                            float Ed1 = fmaf(fn0, dEdf, edmin);
+                            for (int n = n0; n <= n1; n++, Ed1 += dEdf) {
                                 // outgoing range relative to the channel's left edge:
                                 // u1 = Eout1 - Edet1 = ((Esrc1 - Edet1) - Edet1*x)/eratio
-                                const float u1 = fmaf(-Ed1, x, offs[n * W + j]) * inv_er;
+                                const float u1 = fmaf(-Ed1, x, oe[n]) * inv_er;
                                 const float u2 = u1 + span;
                                 const float ov = fminf(u2, dEdf) - fmaxf(u1, 0.f);
-                                if (ov > 0.f)
-                                    atomicAdd(&Cw[wid * P.nrg_det + n], ov / span * rf[n * W + j] * base);
+                                if (ov > 0.f) cs[n] += ov * bs;
                             }
                         }
                     }
                 }
             }
+            // flush the chunk's Compton sums: lane = detector bin n gathers the
+            // (energy, slot) cells that map to n, weights them with RF[e, n]
+            // and adds the result to its compensated total
             __syncwarp();
             for (int n = lane; n < P.nrg_det; n += 32) {
+                float s = 0.f;
+                for (int j = 0; j < W; j++) {
+                    const int el = winlo[n] + j - lo_e;
+                    if (el < pe0 || el >= pe1) continue;
+                    float *c = CS + ((size_t)wid * E + el) * SL + (n - wn[2 * el]);
+                    s = fmaf(*c, rf[n * W + j], s);
+                    *c = 0.f;
+                }
                 float2 k = Ck[wid * P.nrg_det + n];
-                kahan_add(k.x, k.y, Cw[wid * P.nrg_det + n]);
+                kahan_add(k.x, k.y, s);
                 Ck[wid * P.nrg_det + n] = k;
-                Cw[wid * P.nrg_det + n] = 0.f;
             }
             __syncwarp();
         }
@@ -426,10 +567,11 @@ k_fwd(const FwdArgs args)
     }
 
     // ---- outputs: ray index src + det*SRC + nrg*SRC*DET (:404) ----
-#pragma unroll
-    for (int r = 0; r < kMaxRounds; r++) {
-        const int el = lane + 32 * r;
-        if (el < E) atomicAdd(&TN[el], (double)tn[r] - (double)tc[r]);
+    __syncthreads();
+    for (int el = tid; el < E; el += kThreads) {
+        double s = 0.0;
+        for (int w = 0; w < kWarps; w++) s += (double)TNs[w * E + el].x - (double)TNs[w * E + el].y;
+        TN[el] = s;
     }
     __syncthreads();
     for (int n = tid; n < P.nrg_det; n += kThreads) {
@@ -485,10 +627,10 @@ cudaError_t launch_gather_rays(const int64_t *idx, int64_t n, const float *Nc, c
     return cudaGetLastError();
 }
 
-size_t fast_forward_smem(const DevProblem &P, int e_pass, bool with_n, bool with_a)
+size_t fast_forward_smem(const DevProblem &P, int sl, int e_pass, bool with_n, bool with_a)
 {
     const int E = P.e_hi - P.e_lo + 1;
-    return fwd_layout(P, E, e_pass, with_n, with_a).total;
+    return fwd_layout(P, E, sl, e_pass, with_n, with_a).total;
 }
 
 cudaError_t launch_fast_forward(const DevProblem &P, const SrcGeom *d_src, const FwdTables &T,
@@ -515,6 +657,7 @@ cudaError_t launch_fast_forward(const DevProblem &P, const SrcGeom *d_src, const
     a.A = A;
     a.nv = nv;
     a.E = P.e_hi - P.e_lo + 1;
+    a.sl = T.sl;
     const double NWT = (double)P.nwt;
     a.qpar_b = (float)P.dq0;
     a.qpar_a = (float)((P.q_hi - P.q_lo - P.dq0 * NWT) / (NWT * NWT));
@@ -524,10 +667,10 @@ cudaError_t launch_fast_forward(const DevProblem &P, const SrcGeom *d_src, const
     // would push the block past ~110 KB of shared memory
     int e_pass = a.E;
     if (with_a) {
-        while (e_pass > 1 && fwd_layout(P, a.E, e_pass, with_n, true).total > 110 * 1024) e_pass = (e_pass + 1) / 2;
+        while (e_pass > 1 && fwd_layout(P, a.E, a.sl, e_pass, with_n, true).total > 110 * 1024) e_pass = (e_pass + 1) / 2;
     }
     a.e_pass = e_pass;
-    const size_t smem = fwd_layout(P, a.E, e_pass, with_n, with_a).total;
+    const size_t smem = fwd_layout(P, a.E, a.sl, e_pass, with_n, with_a).total;
     if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
     if (launches) (*launches)++;
     if (nv == 0) {

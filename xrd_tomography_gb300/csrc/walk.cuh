@@ -47,15 +47,74 @@ __device__ inline void walk_setup(const DevProblem &P, double ex, double ey, dou
     w->n = (int)n;
 }
 
+// FP32 version of walk_setup for the endpoint (ex, ey) rounded to float.
+// Returns false when a decision is too close to its threshold for FP32 to be
+// trusted -- a nearly edge-parallel ray, a ray through an ROI corner, or a
+// length within a few FP32 errors of a multiple of DQ (axis-aligned rays hit
+// the latter exactly) -- and the caller then decides in FP64 with
+// walk_setup.  Endpoint rounding (|e| ~ 300 voxels -> 1.5e-5) dominates the
+// FP32 error; the guards are several times that.
+__device__ __forceinline__ bool walk_setup_f32(const DevProblem &P, float ex, float ey, float vx, float vy,
+                                               float inv_DQ, WalkSetup *w)
+{
+    const float NX = (float)P.nx, NY = (float)P.ny;
+    const float eps = 0.00001f;
+    const float G = 2e-4f;
+    const float dx = vx - ex, dy = vy - ey;
+    float rx = 0.f, ry = 0.f;
+    bool found = false;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const float x3 = (i == 1 || i == 2) ? NX : 0.f;
+        const float x4 = (i == 0 || i == 1) ? NX : 0.f;
+        const float y3 = (i >= 2) ? NY : 0.f;
+        const float y4 = (i == 1 || i == 2) ? NY : 0.f;
+        const float x4_x3 = x4 - x3, y3_y1 = y3 - ey, y4_y3 = y4 - y3, x3_x1 = x3 - ex;
+        const float den = x4_x3 * dy - dx * y4_y3;
+        if (fabsf(den) < 1e-2f) return false;     // edge-parallel within FP32 error
+        const float inv = __fdividef(1.f, den);
+        const float ua = (x4_x3 * y3_y1 - x3_x1 * y4_y3) * inv;
+        if (fabsf(ua + eps) < G || fabsf(ua - (1.f + eps)) < G) return false;
+        if (ua > -eps && ua < 1.f + eps) {
+            const float ub = (dx * y3_y1 - x3_x1 * dy) * inv;
+            if (fabsf(ub + eps) < G || fabsf(ub - (1.f + eps)) < G) return false;
+            if (ub > -eps && ub < 1.f + eps) {
+                rx = fmaf(dx, ua, ex);
+                ry = fmaf(dy, ua, ey);
+                found = true;
+                break;
+            }
+        }
+    }
+    if (!found) return false;
+    float Lx = vx - rx, Ly = vy - ry;
+    const float L2 = fmaf(Lx, Lx, Ly * Ly);
+    const float rL = rsqrtf(L2);
+    const float t = sqrtf(L2) * inv_DQ;
+    float ft;
+    const int it = floor_nc(t, &ft);
+    const float fr = t - ft;
+    const float gt = fmaf(4e-7f, t, 1e-3f);
+    if (fr < gt || fr > 1.f - gt) return false;
+    long long n = (long long)it + 1;
+    if (n > P.kmax) n = P.kmax;
+    w->rx = rx;
+    w->ry = ry;
+    w->Lx = Lx * rL;
+    w->Ly = Ly * rL;
+    w->n = (int)n;
+    return true;
+}
+
 // One bilinear sample of the cell map at (x, y) in voxel units (the
 // texture's unnormalised coordinates).  Returns (a1, a2).
 __device__ __forceinline__ float2 cell_sample(const float4 *__restrict__ cells, int nx, int ny, float x,
                                               float y)
 {
     const float xb = x - 0.5f, yb = y - 0.5f;
-    const float fx = floorf(xb), fy = floorf(yb);
+    float fx, fy;
+    int ci = floor_nc(xb, &fx) + 1, cj = floor_nc(yb, &fy) + 1;
     const float ux = xb - fx, uy = yb - fy;
-    int ci = (int)fx + 1, cj = (int)fy + 1;
     ci = min(max(ci, 0), nx);
     cj = min(max(cj, 0), ny);
     const float4 *c = cells + 2 * ((int64_t)ci + (int64_t)cj * (nx + 1));
@@ -70,8 +129,10 @@ __device__ __forceinline__ float2 walk_coop(const float4 *__restrict__ cells, in
                                             const WalkSetup &w, float DQ, int lane)
 {
     float s1 = 0.f, s2 = 0.f;
-    for (int k = lane; k < w.n; k += 32) {
-        const float qr = DQ * (float)k;
+    // the sample index carried as a float: no int-to-float conversion per sample
+    float kf = __int_as_float(0x4B000000 | lane) - 8388608.f;   // (float)lane
+    for (int k = lane; k < w.n; k += 32, kf += 32.f) {
+        const float qr = DQ * kf;
         const float2 v = cell_sample(cells, nx, ny, fmaf(w.Lx, qr, w.rx), fmaf(w.Ly, qr, w.ry));
         s1 += v.x;
         s2 += v.y;

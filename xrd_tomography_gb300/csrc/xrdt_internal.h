@@ -80,14 +80,16 @@ cudaError_t launch_src_atten(const DevProblem &P, const SrcGeom *d_src, int nv, 
 struct FwdTables {
     const EnergyRow *energy;   // [nrg_src]
     const float *rf_win;       // [nrg_det][2*dnrg+1] spectrum window per detector bin
-    const float *offs;         // [nrg_det][2*dnrg+1] Esrc1(window bin) - Edet1(nrg)
+    const float *offs_e;       // [nrg_src][sl] Esrc1(e) - Edet1(win_n(e) + s)
+    int sl;                    // slots per source bin: max over e of the number of
+                               // detector bins whose window holds e
     const int *win_lo;         // [nrg_det] first source bin of each window
     const int *win_n;          // [nrg_src][2] detector bins whose window holds e
     const float2 *fine_q;      // [nqf] fine q axis as (hi, lo)
     const float4 *coarse_q;    // [nwt] (q_hi, q_lo, dq, 0)
     unsigned long long *work;  // nullable: counts the exp2 evaluations
 };
-size_t fast_forward_smem(const DevProblem &P, int e_pass, bool with_n, bool with_a);
+size_t fast_forward_smem(const DevProblem &P, int sl, int e_pass, bool with_n, bool with_a);
 // pairs (nullable): (src, det) of each block; outputs then go to the compact
 // layout [nrg_det][n_pairs] (and [nrg_det][n_pairs][n_mat*nwt] for A).
 cudaError_t launch_fast_forward(const DevProblem &P, const SrcGeom *d_src, const FwdTables &T,
