@@ -226,6 +226,53 @@ def run_reference(args):
 
 # ---- GPU leg -------------------------------------------------------------------
 
+def hbm_peak_gbs():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        return float(json.load(open(path))["hbm_gbs"]), "measured (MEASURED_PEAKS.json)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def mlem_stored_bench(xt, synth, ctx, stream, dev, iters=200):
+    """MLEM of main.m:154-176 with the explicit model matrix of the 64x64
+    workload (131072 rays x 256 coefficients, 134 MB): iterations per second
+    and the HBM throughput of its passes (each iteration reads A once)."""
+    import torch
+    inp = synth.config_inputs(0)
+    p = inp.problem
+    K = p.nwt * p.n_mat
+    N = torch.empty(p.rays, dtype=torch.float32, device=dev)
+    C = torch.empty_like(N)
+    A = torch.empty(p.amatrix_elems, dtype=torch.float32, device=dev)
+    xt.forward(p, *inp.args(), Nphotons=N, Cphotons=C, Amatrix=A, ctx=ctx)
+    torch.cuda.synchronize(dev)
+    gen = torch.Generator(device="cpu").manual_seed(7)
+    y = torch.poisson((N + C).cpu(), generator=gen).to(dev)
+    x = torch.full((K,), 10.0, dtype=torch.float32, device=dev)
+    xt.mlem_matrix(A, y, C, x, 3, ctx=ctx)           # warm-up (and graph capture)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    ev[0].record(stream)
+    xt.mlem_matrix(A, y, C, x, 0, ctx=ctx)           # sensitivity pass only
+    ev[1].record(stream)
+    ev[2].record(stream)
+    xt.mlem_matrix(A, y, C, x, iters, ctx=ctx)
+    ev[3].record(stream)
+    torch.cuda.synchronize(dev)
+    t0 = ev[0].elapsed_time(ev[1])
+    t1 = ev[2].elapsed_time(ev[3])
+    per_iter_ms = (t1 - t0) / iters
+    a_bytes = A.numel() * 4
+    traffic = a_bytes + 2 * p.rays * 4               # A, y and c per iteration
+    peak, src = hbm_peak_gbs()
+    gbs = traffic / (per_iter_ms * 1e-3) / 1e9
+    return {"workload": f"explicit model matrix of the 64x64 workload: {p.rays} rays x {K} coefficients "
+                        f"({a_bytes / 1e6:.0f} MB), {iters} iterations, CUDA-graph replay",
+            "iter_per_s": 1e3 / per_iter_ms, "ms_per_iter": per_iter_ms,
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                         "traffic": None, "algorithmic_bytes_per_iter": traffic, "peak_source": src}}
+
+
 def run_ours(args):
     import torch
     import xrd_tomography_gb300 as xt
@@ -321,6 +368,8 @@ def run_ours(args):
         "kernel_ms_per_step": {k: v[1] / max(1, args.steps) for k, v in kstats.items()},
     }
 
+    if rank == 0 and not args.no_baselines:
+        line["mlem"] = mlem_stored_bench(xt, synth, ctx, stream, dev)
     if rank == 0:
         # roofline of the dominant kernel: the forward kernel's exponentials
         # (Gaussian q terms, attenuation and Compton factors) on the SFU

@@ -145,7 +145,8 @@ int64_t xrdt_ctx_launch_count(const xrdt_ctx *ctx);
 #define XRDT_KERNEL_FORWARD     3  /* factored forward projector                     */
 #define XRDT_KERNEL_PLAIN       4  /* FP64 kernel at the reference launch shape      */
 #define XRDT_KERNEL_GATHER      5  /* ray-subset gather                              */
-#define XRDT_KERNEL_COUNT       6
+#define XRDT_KERNEL_MLEM        6  /* MLEM passes and updates                        */
+#define XRDT_KERNEL_COUNT       7
 /* With profiling on, every launch is bracketed by CUDA events on the
  * context's stream and the forward kernel counts the exponentials it
  * evaluates.  Off by default; turning it on or off clears the statistics. */
@@ -192,6 +193,21 @@ int32_t xrdt_forward_rays(xrdt_ctx *ctx, const xrdt_problem *p,
                           const int64_t *rays, int64_t n_rays,
                           float *Nphotons, float *Cphotons, float *A_rows,
                           uint32_t flags);
+
+/* ---- MLEM with an explicit model matrix (main.m:154-176) --------------- */
+/* Runs `iters` iterations of
+ *     x <- x .* (A' * (y ./ (A*x + c + 1e-20))) ./ (sum(A,1)' + 1e-7)
+ *     x(~isfinite(x)) = 0;  x(x < 0) = 0
+ * in place on x[K], with A the [rays x K] model matrix stored as rays rows of
+ * K contiguous floats -- exactly the Amatrix buffer xrdt_forward writes, K =
+ * nwt*n_mat, rays = xrdt_problem_rays (main.m:140 uses its transpose
+ * reshape).  y[rays] are measured counts, c[rays] the Compton bias
+ * (main.m:162 uses Cphotons(:)).  K must be a multiple of 4, at most 1024.
+ * The iteration body is a fused pass over A (one read of A per iteration)
+ * and an FP64 reduction/update, replayed as a CUDA graph. */
+int32_t xrdt_mlem_matrix(xrdt_ctx *ctx, const float *A, int64_t rays, int32_t K,
+                         const float *y, const float *c, float *x, int32_t iters,
+                         uint32_t flags);
 
 #ifdef __cplusplus
 }

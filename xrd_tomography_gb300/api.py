@@ -24,7 +24,8 @@ LIB_PATH = os.path.join(HERE, "libxrdt.so")
 
 FWD_PLAIN_FP64 = 0x1
 FWD_NO_SYNC = 0x2
-KERNEL_PREP_MAP, KERNEL_PREP_VOXELS, KERNEL_SRC_ATTEN, KERNEL_FORWARD, KERNEL_PLAIN, KERNEL_GATHER = range(6)
+(KERNEL_PREP_MAP, KERNEL_PREP_VOXELS, KERNEL_SRC_ATTEN, KERNEL_FORWARD, KERNEL_PLAIN, KERNEL_GATHER,
+ KERNEL_MLEM) = range(7)
 
 _P = ctypes.POINTER(Problem)
 _vp = ctypes.c_void_p
@@ -47,6 +48,8 @@ SIGNATURES = {
                                                ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)]),
     "xrdt_forward": (ctypes.c_int32, [_vp, _P, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_float, ctypes.c_float,
                                       ctypes.c_float, ctypes.c_float, _vp, _vp, _vp, ctypes.c_uint32]),
+    "xrdt_mlem_matrix": (ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp, _vp, ctypes.c_int32,
+                                          ctypes.c_uint32]),
     "xrdt_forward_rays": (ctypes.c_int32, [_vp, _P, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_float,
                                            ctypes.c_float, ctypes.c_float, ctypes.c_float, _vp, ctypes.c_int64,
                                            _vp, _vp, _vp, ctypes.c_uint32]),
@@ -212,6 +215,27 @@ def forward_rays(p: Problem, rays, spectrum, Ifine, seg, a1, a2, S2, q_min, q_ma
                                  A.ctypes.data if A is not None else None, FWD_PLAIN_FP64 if plain else 0)
     _check(rc, ctx.h)
     return N, C, A
+
+
+def mlem_matrix(A, y, c, x0, iters: int, K: int | None = None, ctx: Context | None = None):
+    """xrdt_mlem_matrix: MLEM of main.m:154-176 on the model matrix A
+    ([rays, K] rows, the Amatrix layout).  x0 is updated in place when it is a
+    torch CUDA tensor; numpy inputs return a new array."""
+    ctx = ctx or default_context()
+    if K is None:
+        K = int(x0.numel() if hasattr(x0, "numel") else np.size(x0))
+    pa, ka = _ptr(A, np.float32)
+    py, ky = _ptr(y, np.float32)
+    pc, kc = _ptr(c, np.float32)
+    if hasattr(x0, "data_ptr"):
+        x = x0
+        px = x.data_ptr()
+    else:
+        x = np.array(x0, dtype=np.float32, copy=True)
+        px = x.ctypes.data
+    rays = int(ky.numel() if hasattr(ky, "numel") else ky.size)
+    _check(lib().xrdt_mlem_matrix(ctx.h, pa, rays, K, py, pc, px, iters, 0), ctx.h)
+    return x
 
 
 def Forward_XRD(spectrum, Ifine, segmentation, a1, a2, S2, q_min, q_max, a_min, a_max,

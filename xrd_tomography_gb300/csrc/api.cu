@@ -38,6 +38,11 @@ struct xrdt_ctx {
     int64_t prof_launches[XRDT_KERNEL_COUNT] = {};
     double prof_ms[XRDT_KERNEL_COUNT] = {};
     unsigned long long *d_work = nullptr;  // exp2 evaluations of the forward kernel
+    // MLEM iteration captured as a graph, keyed by its arguments
+    cudaGraphExec_t mlem_exec = nullptr;
+    const void *mlem_key[6] = {};
+    long long mlem_rays = 0;
+    int mlem_K = 0;
 };
 
 namespace xrdt {
@@ -61,6 +66,7 @@ enum Slot {
     S_CELLS, S_VXY, S_VMAT, S_VNA, S_VA2, S_CNT, S_ASRC, S_S2U8,
     S_SRCG, S_ENERGY, S_RFWIN, S_OFFS, S_WINLO, S_WINN, S_FINEQ, S_COARSEQ, S_COARSEQD,
     S_RAYS, S_PAIRS, S_NC, S_CC, S_AC,
+    S_MA, S_MY, S_MC, S_MX, S_MPART, S_MSENS,
     S_COUNT
 };
 
@@ -461,6 +467,7 @@ int32_t xrdt_ctx_destroy(xrdt_ctx *ctx)
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     fold_pending(ctx);
+    if (ctx->mlem_exec) cudaGraphExecDestroy(ctx->mlem_exec);
     if (ctx->d_work) cudaFree(ctx->d_work);
     for (void *p : ctx->buf)
         if (p) cudaFree(p);
@@ -787,6 +794,75 @@ int32_t xrdt_forward_rays(xrdt_ctx *ctx, const xrdt_problem *p, const float *spe
     static const int64_t none = 0;
     return forward_impl(ctx, p, spectrum, Ifine, seg, a1, a2, S2, q_min, q_max, a_min, a_max,
                         rays ? rays : &none, n_rays, Nphotons, Cphotons, A_rows, flags);
+}
+
+int32_t xrdt_mlem_matrix(xrdt_ctx *ctx, const float *A, int64_t rays, int32_t K, const float *y, const float *c,
+                         float *x, int32_t iters, uint32_t flags)
+{
+    if (!ctx) return XRDT_ERR_NULL;
+    ctx->err.clear();
+    if (!A || !y || !c || !x) return fail(ctx, XRDT_ERR_NULL, "a required array pointer is NULL");
+    if (rays < 1 || K < 4 || K > 1024 || (K & 3) || iters < 0)
+        return fail(ctx, XRDT_ERR_DIMS, "need rays >= 1, K a multiple of 4 in [4, 1024], iters >= 0");
+    if (flags) return fail(ctx, XRDT_ERR_UNSUPPORTED, "unknown flag bits");
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    int rc;
+    const void *dA, *dy, *dc;
+    if ((rc = stage_in(ctx, S_MA, A, sizeof(float) * (size_t)rays * K, &dA))) return rc;
+    if ((rc = stage_in(ctx, S_MY, y, sizeof(float) * (size_t)rays, &dy))) return rc;
+    if ((rc = stage_in(ctx, S_MC, c, sizeof(float) * (size_t)rays, &dc))) return rc;
+    const bool hostX = !is_device_ptr(x);
+    float *dx = x;
+    void *tmp;
+    if (hostX) {
+        if ((rc = get_buf(ctx, S_MX, sizeof(float) * K, &tmp))) return rc;
+        dx = (float *)tmp;
+        CK(cudaMemcpyAsync(dx, x, sizeof(float) * K, cudaMemcpyHostToDevice, st));
+    }
+    int sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    const int nparts = mlem_pass_blocks(sms, K);
+    void *dpart, *dsens;
+    if ((rc = get_buf(ctx, S_MPART, sizeof(float) * (size_t)nparts * K, &dpart))) return rc;
+    if ((rc = get_buf(ctx, S_MSENS, sizeof(double) * K, &dsens))) return rc;
+    {
+        ProfScope ps(ctx, XRDT_KERNEL_MLEM);
+        CK(launch_mlem_sensitivity((const float *)dA, rays, K, (float *)dpart, nparts, (double *)dsens, st,
+                                   &ctx->launches));
+    }
+    if (iters > 0) {
+        const void *key[6] = {dA, dy, dc, dx, dpart, dsens};
+        bool same = ctx->mlem_exec && ctx->mlem_rays == rays && ctx->mlem_K == K;
+        for (int i = 0; i < 6 && same; i++) same = ctx->mlem_key[i] == key[i];
+        if (!same) {
+            if (ctx->mlem_exec) {
+                cudaGraphExecDestroy(ctx->mlem_exec);
+                ctx->mlem_exec = nullptr;
+            }
+            cudaGraph_t graph;
+            CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            int64_t dummy = 0;
+            cudaError_t le = launch_mlem_iteration((const float *)dA, rays, K, (const float *)dy,
+                                                   (const float *)dc, dx, (float *)dpart, nparts,
+                                                   (const double *)dsens, st, &dummy);
+            cudaError_t ce = cudaStreamEndCapture(st, &graph);
+            if (le != cudaSuccess) return fail(ctx, XRDT_ERR_CUDA, fmt("MLEM capture: %s", cudaGetErrorString(le)));
+            CK(ce);
+            cudaError_t ie = cudaGraphInstantiate(&ctx->mlem_exec, graph, 0);
+            cudaGraphDestroy(graph);
+            CK(ie);
+            for (int i = 0; i < 6; i++) ctx->mlem_key[i] = key[i];
+            ctx->mlem_rays = rays;
+            ctx->mlem_K = K;
+        }
+        ProfScope ps(ctx, XRDT_KERNEL_MLEM);
+        for (int it = 0; it < iters; it++) CK(cudaGraphLaunch(ctx->mlem_exec, st));
+        ctx->launches += 2 * (int64_t)iters;
+    }
+    if (hostX) CK(cudaMemcpyAsync(x, dx, sizeof(float) * K, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return XRDT_OK;
 }
 
 } // extern "C"

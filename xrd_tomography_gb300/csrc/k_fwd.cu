@@ -355,7 +355,7 @@ k_fwd(const FwdArgs args)
             const float a2v = args.vox_a2[v];
             const float2 Asv = args.atten_src[(int64_t)src * nv + v];
             WalkSetup ws;
-            if (!walk_setup_f32(P, Rdxf, Rdyf, vx, vy, inv_DQ, &ws))
+            if (!walk_setup_f32(P, Rdxf, Rdyf, vx, vy, DQf, inv_DQ, &ws))
                 walk_setup_f64(P, Rdet_x, Rdet_y, (double)vx, (double)vy, &ws);
 
             const int nin = min(32, nv - chunk * 32);
@@ -410,7 +410,8 @@ k_fwd(const FwdArgs args)
                         const int jlo = max(ceil_nc(jc - half * inv_dqf), 0);
                         int jhi = min(floor_nc(jc + half * inv_dqf), P.nqf - 1);
                         float acc = 0.f;
-                        if (jlo <= jhi) {
+                        // pref == 0: the attenuation factor underflowed, every term is 0
+                        if (jlo <= jhi && pref != 0.f) {
                             // an even number of bins, so the pair loop has no tail: an
                             // odd window takes one more bin (an exact term of the full
                             // sum, or the zero pad after the last bin).  A tail would make
@@ -470,14 +471,15 @@ k_fwd(const FwdArgs args)
                         // detector bins whose window holds e and whose channel the
                         // outgoing range [E1, E2]/eratio can overlap
                         const float Eo_lo = en_e1[el];
+                        // channels overlapped by [E1, E2]/eratio (an FP32 misjudgement at a
+                        // channel edge drops an overlap below 1e-6 of the bin width)
                         float fn0;
-                        int n0 = floor_nc((Eo_lo * inv_er - edmin) * inv_dEd, &fn0) - 1;
-                        fn0 -= 1.f;
+                        int n0 = floor_nc((Eo_lo * inv_er - edmin) * inv_dEd, &fn0);
                         if (n0 < wn[2 * el]) {
                             n0 = wn[2 * el];
                             fn0 = en_wn0f[el];
                         }
-                        const int n1 = min(wn[2 * el + 1], floor_nc(((Eo_lo + dEsf) * inv_er - edmin) * inv_dEd) + 1);
+                        const int n1 = min(wn[2 * el + 1], floor_nc(((Eo_lo + dEsf) * inv_er - edmin) * inv_dEd));
                         if (n0 <= n1) {
                             const float wC = ein * sh;
                             const float arg = eratio + wC * wC;
@@ -495,6 +497,7 @@ k_fwd(const FwdArgs args)
                             const float Xc = fmaf(Asx, rcp_approx(f1), Asy * rcp_approx(f2));
                             const float Pc = ex2_approx(-(Xin + Xc) * kLog2e);
                             nexp += 1;
+                            if (Pc == 0.f) continue;   // underflow: no contribution
                             const float Cf = eratio * eratio * (eratio + inv_er - 1.f + cos2) * 0.5f;
                             const float base = Pc * gp * Cf * a2now * S2[nq + na * P.nq];
                             const float span = dEsf * inv_er;   // Eout2 - Eout1

@@ -2,9 +2,10 @@
 //
 //  * k_build_cells: the (a1,a2) map as bilinear cells.  Replaces Copy2Vector
 //    (Copy2Vector.cu:9-23) and the cudaArray/texture set-up of
-//    Forward_XRD.cu:209-237: cell (ci,cj) holds the four texels
-//    (ci-1..ci, cj-1..cj) of a zero-bordered map as two float4, so one
-//    bilinear sample is two 16-byte loads with no border tests.  Also
+//    Forward_XRD.cu:209-237: cell (ci,cj) holds the bilinear coefficients of
+//    the four texels (ci-1..ci, cj-1..cj) of a zero-bordered map as two
+//    float4, so one sample is two 16-byte loads and three FMAs per component
+//    with no border tests.  Also
 //    quantises the Compton table to u8 (integrate_diffraction.cu:66-74).
 //  * k_compact_voxels: non-empty voxels in the reference's loop order
 //    (nx outer, ny inner; integrate_diffraction.cu:173-178) and the material
@@ -39,8 +40,16 @@ __global__ void k_build_cells(int nx, int ny, const float *__restrict__ a1, cons
                 v[dj][di][0] = in ? a1[idx] : 0.f;
                 v[dj][di][1] = in ? a2[idx] : 0.f;
             }
-        cells[2 * c] = make_float4(v[0][0][0], v[0][0][1], v[0][1][0], v[0][1][1]);
-        cells[2 * c + 1] = make_float4(v[1][0][0], v[1][0][1], v[1][1][0], v[1][1][1]);
+        // bilinear coefficients per component q: f(u,v) = c00 + c10 u + c01 v + c11 u v
+        float c00[2], c10[2], c01[2], c11[2];
+        for (int q = 0; q < 2; q++) {
+            c00[q] = v[0][0][q];
+            c10[q] = v[0][1][q] - v[0][0][q];
+            c01[q] = v[1][0][q] - v[0][0][q];
+            c11[q] = (v[1][1][q] - v[1][0][q]) - (v[0][1][q] - v[0][0][q]);
+        }
+        cells[2 * c] = make_float4(c00[0], c00[1], c10[0], c10[1]);
+        cells[2 * c + 1] = make_float4(c01[0], c01[1], c11[0], c11[1]);
     }
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ns2; i += stride) {
         const int q = floor_to_int((double)S2[i]);

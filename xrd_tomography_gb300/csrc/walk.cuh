@@ -13,8 +13,8 @@
 namespace xrdt {
 
 struct WalkSetup {
-    float rx, ry;   // ROI entry point (GetIntersection)
-    float Lx, Ly;   // unit direction entry -> voxel
+    float rx, ry;   // ROI entry point (GetIntersection) minus one voxel in x and y
+    float Lx, Ly;   // DQ times the unit direction entry -> voxel
     int n;          // number of samples: k = 0 .. n-1
 };
 
@@ -40,10 +40,10 @@ __device__ inline void walk_setup(const DevProblem &P, double ex, double ey, dou
         n = k + 1;
         if (n > P.kmax) n = P.kmax;
     }
-    w->rx = (float)rx;
-    w->ry = (float)ry;
-    w->Lx = (float)Lx;
-    w->Ly = (float)Ly;
+    w->rx = (float)(rx - 1.0);
+    w->ry = (float)(ry - 1.0);
+    w->Lx = (float)(Lx * P.DQ);
+    w->Ly = (float)(Ly * P.DQ);
     w->n = (int)n;
 }
 
@@ -55,7 +55,7 @@ __device__ inline void walk_setup(const DevProblem &P, double ex, double ey, dou
 // walk_setup.  Endpoint rounding (|e| ~ 300 voxels -> 1.5e-5) dominates the
 // FP32 error; the guards are several times that.
 __device__ __forceinline__ bool walk_setup_f32(const DevProblem &P, float ex, float ey, float vx, float vy,
-                                               float inv_DQ, WalkSetup *w)
+                                               float DQ, float inv_DQ, WalkSetup *w)
 {
     const float NX = (float)P.nx, NY = (float)P.ny;
     const float eps = 0.00001f;
@@ -98,47 +98,61 @@ __device__ __forceinline__ bool walk_setup_f32(const DevProblem &P, float ex, fl
     if (fr < gt || fr > 1.f - gt) return false;
     long long n = (long long)it + 1;
     if (n > P.kmax) n = P.kmax;
-    w->rx = rx;
-    w->ry = ry;
-    w->Lx = Lx * rL;
-    w->Ly = Ly * rL;
+    w->rx = rx - 1.f;
+    w->ry = ry - 1.f;
+    w->Lx = Lx * rL * DQ;
+    w->Ly = Ly * rL * DQ;
     w->n = (int)n;
     return true;
 }
 
-// One bilinear sample of the cell map at (x, y) in voxel units (the
-// texture's unnormalised coordinates).  Returns (a1, a2).
-__device__ __forceinline__ float2 cell_sample(const float4 *__restrict__ cells, int nx, int ny, float x,
-                                              float y)
+// One bilinear sample of the cell map at texture coordinates (X+1, Y+1).
+// Cell (ci, cj) holds the bilinear coefficients of the texels (ci-1..ci,
+// cj-1..cj) of the zero-bordered map: f(u,v) = c00 + c10 u + c01 v + c11 u v.
+// The base texel is round(X) instead of floor(X + 0.5): the interpolant is
+// continuous, so any base with weights u, v in [0, 1] gives the same value,
+// and rounding through the float mantissa (adding 1.5 * 2^23) needs no
+// conversion instruction.  Valid for |X| < 2^22; the cell index is clamped
+// for memory safety.
+__device__ __forceinline__ float2 cell_sample(const float4 *__restrict__ cells, int nx, unsigned ncell_m1,
+                                              float X, float Y)
 {
-    const float xb = x - 0.5f, yb = y - 0.5f;
-    float fx, fy;
-    int ci = floor_nc(xb, &fx) + 1, cj = floor_nc(yb, &fy) + 1;
-    const float ux = xb - fx, uy = yb - fy;
-    ci = min(max(ci, 0), nx);
-    cj = min(max(cj, 0), ny);
-    const float4 *c = cells + 2 * ((int64_t)ci + (int64_t)cj * (nx + 1));
-    const float4 c0 = __ldg(c), c1 = __ldg(c + 1);
-    const float b0 = fmaf(ux, c0.z - c0.x, c0.x), b1 = fmaf(ux, c1.z - c1.x, c1.x);
-    const float d0 = fmaf(ux, c0.w - c0.y, c0.y), d1 = fmaf(ux, c1.w - c1.y, c1.y);
-    return make_float2(fmaf(uy, b1 - b0, b0), fmaf(uy, d1 - d0, d0));
+    const float tx = X + 12582912.f, ty = Y + 12582912.f;
+    const int ix = __float_as_int(tx) - 0x4B400000, iy = __float_as_int(ty) - 0x4B400000;
+    const float u = (X - (tx - 12582912.f)) + 0.5f;
+    const float v = (Y - (ty - 12582912.f)) + 0.5f;
+    const unsigned c = min((unsigned)(ix + 1 + (iy + 1) * (nx + 1)), ncell_m1);
+    const float4 c0 = __ldg(cells + 2 * c), c1 = __ldg(cells + 2 * c + 1);
+    return make_float2(fmaf(u, fmaf(v, c1.z, c0.z), fmaf(v, c1.x, c0.x)),
+                       fmaf(u, fmaf(v, c1.w, c0.w), fmaf(v, c1.y, c0.y)));
 }
 
-// Sum of the n samples times DQ; every lane returns the total.
+// Sum of the n samples times DQ; every lane returns the total.  Lane l takes
+// samples l, l+32, l+64, ... two per iteration; the sample index is carried
+// as a float (no int-to-float conversion per sample).
 __device__ __forceinline__ float2 walk_coop(const float4 *__restrict__ cells, int nx, int ny,
                                             const WalkSetup &w, float DQ, int lane)
 {
-    float s1 = 0.f, s2 = 0.f;
-    // the sample index carried as a float: no int-to-float conversion per sample
+    const unsigned ncell_m1 = (unsigned)((nx + 1) * (ny + 1) - 1);
+    float s1 = 0.f, s2 = 0.f, t1 = 0.f, t2 = 0.f;
     float kf = __int_as_float(0x4B000000 | lane) - 8388608.f;   // (float)lane
-    for (int k = lane; k < w.n; k += 32, kf += 32.f) {
-        const float qr = DQ * kf;
-        const float2 v = cell_sample(cells, nx, ny, fmaf(w.Lx, qr, w.rx), fmaf(w.Ly, qr, w.ry));
-        s1 += v.x;
-        s2 += v.y;
+    int k = lane;
+    for (; k + 32 < w.n; k += 64, kf += 64.f) {
+        const float2 a = cell_sample(cells, nx, ncell_m1, fmaf(w.Lx, kf, w.rx), fmaf(w.Ly, kf, w.ry));
+        const float kg = kf + 32.f;
+        const float2 b = cell_sample(cells, nx, ncell_m1, fmaf(w.Lx, kg, w.rx), fmaf(w.Ly, kg, w.ry));
+        s1 += a.x;
+        s2 += a.y;
+        t1 += b.x;
+        t2 += b.y;
     }
-    s1 = warp_sum(s1);
-    s2 = warp_sum(s2);
+    if (k < w.n) {
+        const float2 a = cell_sample(cells, nx, ncell_m1, fmaf(w.Lx, kf, w.rx), fmaf(w.Ly, kf, w.ry));
+        s1 += a.x;
+        s2 += a.y;
+    }
+    s1 = warp_sum(s1 + t1);
+    s2 = warp_sum(s2 + t2);
     return make_float2(s1 * DQ, s2 * DQ);
 }
 

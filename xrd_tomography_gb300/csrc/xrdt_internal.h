@@ -101,4 +101,13 @@ cudaError_t launch_gather_rays(const int64_t *idx, int64_t n, const float *Nc, c
                                const float *Ac, int mw, float *N, float *C, float *A, cudaStream_t s,
                                int64_t *launches);
 
+// k_mlem.cu: MLEM with an explicit model matrix (rows of K floats, K % 4 == 0,
+// K <= 1024); partial holds nparts rows of K floats.
+int mlem_pass_blocks(int sm_count, int K);
+cudaError_t launch_mlem_sensitivity(const float *A, long long rays, int K, float *partial, int nparts,
+                                    double *sens, cudaStream_t s, int64_t *launches);
+cudaError_t launch_mlem_iteration(const float *A, long long rays, int K, const float *y, const float *c,
+                                  float *x, float *partial, int nparts, const double *sens, cudaStream_t s,
+                                  int64_t *launches);
+
 } // namespace xrdt
