@@ -209,6 +209,22 @@ int32_t xrdt_mlem_matrix(xrdt_ctx *ctx, const float *A, int64_t rays, int32_t K,
                          const float *y, const float *c, float *x, int32_t iters,
                          uint32_t flags);
 
+/* The same MLEM for callers that cannot allocate device memory (a host
+ * framework that owns the device pool, a real-time loop that must not risk
+ * an allocation or its implicit synchronisation, an embedder that only hands
+ * over buffers).  No counterpart in the reference.  It allocates nothing: its
+ * scratch is a fixed 2 MiB + 8 KiB array in the library that every device
+ * using it keeps until process exit; K is limited to 1024 as in
+ * xrdt_mlem_matrix (larger K: XRDT_ERR_DIMS).  A, y, c and x must be device
+ * memory (else XRDT_ERR_UNSUPPORTED); work is queued on `stream` (a
+ * cudaStream_t, NULL for the default stream) on the current device and the
+ * call returns after the stream has finished.  The first call on a device
+ * looks up the scratch address, so make it before any stream capture.  All
+ * calls share the scratch: calls that overlap on the GPU race. */
+int32_t xrdt_mlem_matrix_noalloc(const float *A, int64_t rays, int32_t K,
+                                 const float *y, const float *c, float *x,
+                                 int32_t iters, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -50,6 +50,8 @@ SIGNATURES = {
                                       ctypes.c_float, ctypes.c_float, _vp, _vp, _vp, ctypes.c_uint32]),
     "xrdt_mlem_matrix": (ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp, _vp, ctypes.c_int32,
                                           ctypes.c_uint32]),
+    "xrdt_mlem_matrix_noalloc": (ctypes.c_int32, [_vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp, _vp, ctypes.c_int32,
+                                                  _vp]),
     "xrdt_forward_rays": (ctypes.c_int32, [_vp, _P, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_float,
                                            ctypes.c_float, ctypes.c_float, ctypes.c_float, _vp, ctypes.c_int64,
                                            _vp, _vp, _vp, ctypes.c_uint32]),
@@ -235,6 +237,18 @@ def mlem_matrix(A, y, c, x0, iters: int, K: int | None = None, ctx: Context | No
         px = x.ctypes.data
     rays = int(ky.numel() if hasattr(ky, "numel") else ky.size)
     _check(lib().xrdt_mlem_matrix(ctx.h, pa, rays, K, py, pc, px, iters, 0), ctx.h)
+    return x
+
+
+def mlem_matrix_noalloc(A, y, c, x, iters: int, stream: int | None = None):
+    """xrdt_mlem_matrix_noalloc: the same MLEM for callers that cannot
+    allocate; every array must already be a torch CUDA tensor, x is updated in
+    place, the library allocates nothing."""
+    for t in (A, y, c, x):
+        if not hasattr(t, "data_ptr") or not t.is_cuda or not t.is_contiguous():
+            raise ValueError("xrdt_mlem_matrix_noalloc takes contiguous CUDA tensors only")
+    _check(lib().xrdt_mlem_matrix_noalloc(A.data_ptr(), int(y.numel()), int(x.numel()), y.data_ptr(),
+                                          c.data_ptr(), x.data_ptr(), iters, _vp(stream) if stream else None))
     return x
 
 
