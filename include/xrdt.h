@@ -146,7 +146,10 @@ int64_t xrdt_ctx_launch_count(const xrdt_ctx *ctx);
 #define XRDT_KERNEL_PLAIN       4  /* FP64 kernel at the reference launch shape      */
 #define XRDT_KERNEL_GATHER      5  /* ray-subset gather                              */
 #define XRDT_KERNEL_MLEM        6  /* MLEM passes and updates                        */
-#define XRDT_KERNEL_COUNT       7
+#define XRDT_KERNEL_VOX_FORWARD 7  /* per-voxel operator: forward (and MLEM ratios)  */
+#define XRDT_KERNEL_VOX_ADJOINT 8  /* per-voxel operator: adjoint                    */
+#define XRDT_KERNEL_VOX_UPDATE  9  /* per-voxel operator: sums, update, staging      */
+#define XRDT_KERNEL_COUNT       10
 /* With profiling on, every launch is bracketed by CUDA events on the
  * context's stream and the forward kernel counts the exponentials it
  * evaluates.  Off by default; turning it on or off clears the statistics. */
@@ -208,6 +211,43 @@ int32_t xrdt_forward_rays(xrdt_ctx *ctx, const xrdt_problem *p,
 int32_t xrdt_mlem_matrix(xrdt_ctx *ctx, const float *A, int64_t rays, int32_t K,
                          const float *y, const float *c, float *x, int32_t iters,
                          uint32_t flags);
+
+/* ---- per-voxel-coefficient operator: forward, adjoint, MLEM -----------
+ * The reference's unknowns are per material: Amatrix[k, m, ray] sums the
+ * coarse-q term of integrate_diffraction.cu:311-315 over the voxels of
+ * material m (Forward_XRD.cu:160), and main.m:154-176 reconstructs NWT*MAT
+ * numbers.  An operator gives every non-empty voxel its own coarse-q
+ * pattern, x[k + NWT*(ix + NX*iy)], and computes matrix-free
+ *   y[ray] = sum_{v,k} Av[ray, v, k] x[v, k]          (xrdt_op_forward)
+ *   g[v,k] = sum_ray  w[ray] Av[ray, v, k]            (xrdt_op_adjoint)
+ * where Av is that term for voxel v alone; summing Av over the voxels of a
+ * material gives Amatrix.  Rays are ordered as Nphotons, src + det*SRC +
+ * nrg*SRC*DET.  The operator is the forward/backward context: creating it
+ * stages the attenuation maps, the voxel list, the (source, pixel) pairs and
+ * the source-side line integrals once; every forward or adjoint walks the
+ * detector-side attenuation of each (pair, voxel) again instead of storing
+ * it.  Arrays may be host or device memory; calls synchronise the context's
+ * stream before they return.  The context must outlive the operator. */
+typedef struct xrdt_op xrdt_op;
+/* Requires NWT <= 1024 and at most 128 source bins in the spectrum windows. */
+int32_t xrdt_op_create(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum,
+                       const int32_t *seg, const float *a1, const float *a2,
+                       xrdt_op **op);
+int32_t xrdt_op_destroy(xrdt_op *op);
+/* Number of non-empty voxels (the voxels that carry unknowns), or -1. */
+int64_t xrdt_op_voxels(const xrdt_op *op);
+/* y [rays] = Av x; x [NX*NY*NWT] (entries of empty voxels are ignored). */
+int32_t xrdt_op_forward(xrdt_op *op, const float *x, float *y, uint32_t flags);
+/* g [NX*NY*NWT] = Av^T w; w [rays]; g is 0 at empty voxels. */
+int32_t xrdt_op_adjoint(xrdt_op *op, const float *w, float *g, uint32_t flags);
+/* iters MLEM updates of main.m:162-176 with per-voxel unknowns:
+ *   x <- x .* Av^T(y ./ (Av x + c + 1e-20)) ./ (Av^T 1 + 1e-7),
+ * non-finite entries and negatives set to 0.  y, c [rays]; x [NX*NY*NWT] is
+ * the starting estimate and receives the result (0 at empty voxels once
+ * iters >= 1, where the sensitivity is 0).  Each iteration is one CUDA
+ * graph launch of three kernels: forward with the ratios, adjoint, update. */
+int32_t xrdt_op_mlem(xrdt_op *op, const float *y, const float *c, float *x,
+                     int32_t iters, uint32_t flags);
 
 /* The same MLEM for callers that cannot allocate device memory (a host
  * framework that owns the device pool, a real-time loop that must not risk

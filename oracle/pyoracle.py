@@ -44,6 +44,7 @@ def lib():
             build(ref=False)
         _lib = ctypes.CDLL(LIB)
         _lib.xrdt_oracle_forward_rays.restype = ctypes.c_int32
+        _lib.xrdt_oracle_vox_rays.restype = ctypes.c_int32
         _lib.xrdt_oracle_attenuator.restype = ctypes.c_int64
         _lib.xrdt_oracle_get_intersection.restype = ctypes.c_int32
     return _lib
@@ -88,6 +89,37 @@ def forward_rays(inp, rays, want_a=False, want_av=False, threads=0):
     if rc != 0:
         raise ValueError("oracle rejected the input (material id above n_mat)")
     return N, C, A, Av
+
+
+def vox_rays(inp, rays, x=None, w=None, threads=0):
+    """The per-voxel-coefficient model of the given rays in FP64.
+
+    x: coefficients [NY, NX, NWT] (C order; voxel index nx + ny*NX, the layout
+    of the library's per-voxel operator) -> y[i] = sum Av[rays[i]] * x.
+    w: weights [n_rays] -> g[NY, NX, NWT] = sum_i w[i] Av[rays[i]].
+    Returns (y, g); an entry is None when its input was not given."""
+    p = inp.problem
+    rays = np.ascontiguousarray(rays, np.int64)
+    n = rays.size
+    xd = None if x is None else np.ascontiguousarray(x, np.float64).reshape(-1)
+    wd = None if w is None else np.ascontiguousarray(w, np.float64).reshape(-1)
+    if xd is not None and xd.size != p.nx * p.ny * p.nwt:
+        raise ValueError("x must hold nx*ny*nwt coefficients")
+    if wd is not None and wd.size != n:
+        raise ValueError("w must hold one weight per ray")
+    y = np.zeros(n) if xd is not None else None
+    g = np.zeros(p.nx * p.ny * p.nwt) if wd is not None else None
+    keep = [np.ascontiguousarray(a, np.float32) for a in (inp.spectrum, inp.a1, inp.a2)]
+    seg = np.ascontiguousarray(inp.seg, np.int32)
+    rc = lib().xrdt_oracle_vox_rays(
+        ctypes.byref(p), keep[0].ctypes.data_as(_f), seg.ctypes.data_as(_i32), keep[1].ctypes.data_as(_f),
+        keep[2].ctypes.data_as(_f), xd.ctypes.data_as(_d) if xd is not None else None,
+        wd.ctypes.data_as(_d) if wd is not None else None, rays.ctypes.data_as(_i64), ctypes.c_int64(n),
+        y.ctypes.data_as(_d) if y is not None else None, g.ctypes.data_as(_d) if g is not None else None,
+        ctypes.c_int32(threads))
+    if rc != 0:
+        raise ValueError(f"oracle rejected the input ({rc})")
+    return y, (None if g is None else g.reshape(p.ny, p.nx, p.nwt))
 
 
 def ref_forward_rays(inp, rays, threads=0):

@@ -180,8 +180,10 @@ static void forward_one_ray(const xrdt_problem *p, const float *spectrum, const 
                             const unsigned char *S2u8, const coarse_bin *cb,
                             double q_min, double q_max, double a_min, double a_max,
                             int64_t ray, double *N_out, double *C_out, double *A_row,
-                            double *Av_row)
+                            double *Av_row, const double *xv, double *yv, double *gv, double wgt)
 {
+    /* Per-voxel mode (xv or gv set): only the coarse-q model row matters. */
+    const int want_nc = !(xv || gv);
     const int NX = p->nx, NY = p->ny;
     const int SRC = p->n_src, COL = p->n_col, DET = p->n_col * p->n_row;
     const int NWT = p->nwt, NQF = p->nqf, MAT = p->n_mat, NQ = p->nq, NA = p->na;
@@ -300,24 +302,28 @@ static void forward_one_ray(const xrdt_problem *p, const float *spectrum, const 
                 double Pout = exp(-(Av2d_x / f1 + Av2d_y / f2));
 
                 /* Fine-q Rayleigh sum, :299-308 (all NQF bins). */
-                const float *Im = Ifine + (int64_t)matID * NQF;
-                for (int qf = 0; qf < NQF; qf++) {
+                const float *Im = want_nc ? Ifine + (int64_t)matID * NQF : NULL;
+                for (int qf = 0; want_nc && qf < NQF; qf++) {
                     double qaxis_fine = p->q_lo + dq_fine * (0.5 + (double)qf);
                     double Rq = RF * exp(-(wvt - qaxis_fine) * (wvt - qaxis_fine) / (2.0 * sigma_wvt2)) *
                                 p->rsqrt2pi / sqrt(sigma_wvt2) * dq_fine;
                     Nnow += Pin * Pout * geomproduct * Rq * (double)Im[qf] * Rayleigh_factor;
                 }
                 /* Coarse-q model row, :311-315. */
-                if (A_row || Av_row) {
+                if (A_row || Av_row || xv || gv) {
+                    const int64_t vrow = ((int64_t)nx + (int64_t)ny * NX) * NWT;
                     for (int k = 0; k < NWT; k++) {
                         double d = wvt - cb[k].qnow;
                         double Rq = RF * exp(-d * d / (2.0 * sigma_wvt2)) * p->rsqrt2pi /
                                     sqrt(sigma_wvt2) * cb[k].dqnow;
                         double t = Pin * Pout * geomproduct * Rq * Rayleigh_factor;
                         if (A_row) A_row[(int64_t)matID * NWT + k] += t;
-                        if (Av_row) Av_row[((int64_t)nx + (int64_t)ny * NX) * NWT + k] += t;
+                        if (Av_row) Av_row[vrow + k] += t;
+                        if (xv) *yv += t * xv[vrow + k];
+                        if (gv) gv[vrow + k] += wgt * t;
                     }
                 }
+                if (!want_nc) continue;
                 /* Compton, :318-356. */
                 double eratio = 1.0 + ein * (1.0 - costheta);
                 double eout = ein / eratio;
@@ -379,9 +385,58 @@ int32_t xrdt_oracle_forward_rays(const xrdt_problem *p,
         if (Av_row) memset(Av_row, 0, sizeof(double) * (size_t)avrow);
         forward_one_ray(p, spectrum, Ifine, seg, a1, a2, S2u8, cb,
                         (double)q_min, (double)q_max, (double)a_min, (double)a_max,
-                        rays[i], &N_out[i], &C_out[i], A_row, Av_row);
+                        rays[i], &N_out[i], &C_out[i], A_row, Av_row, NULL, NULL, NULL, 0.0);
     }
     free(cb);
     free(S2u8);
+    return 0;
+}
+
+int32_t xrdt_oracle_vox_rays(const xrdt_problem *p, const float *spectrum, const int32_t *seg,
+                             const float *a1, const float *a2, const double *x, const double *w,
+                             const int64_t *rays, int64_t n_rays, double *y_out, double *g_out,
+                             int32_t n_threads)
+{
+    const int64_t nvox = (int64_t)p->nx * p->ny;
+    for (int64_t i = 0; i < nvox; i++)
+        if (seg[i] > p->n_mat) return -1;
+    if ((x == NULL) != (y_out == NULL) || (w == NULL) != (g_out == NULL)) return -2;
+    coarse_bin *cb = (coarse_bin *)malloc(sizeof(coarse_bin) * (size_t)p->nwt);
+    for (int k = 0; k < p->nwt; k++) xrdt_oracle_wvt_value(p, k, &cb[k].qnow, &cb[k].dqnow);
+    const int64_t ng = nvox * p->nwt;
+    int nt = 1;
+#ifdef _OPENMP
+    if (n_threads > 0) omp_set_num_threads(n_threads);
+    nt = omp_get_max_threads();
+#endif
+    /* one adjoint accumulator per thread, summed in thread order */
+    double *gpriv = g_out ? (double *)calloc((size_t)nt * (size_t)ng, sizeof(double)) : NULL;
+    if (g_out && !gpriv) {
+        free(cb);
+        return -3;
+    }
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+    for (int64_t i = 0; i < n_rays; i++) {
+        int t = 0;
+#ifdef _OPENMP
+        t = omp_get_thread_num();
+#endif
+        double nn = 0.0, cc = 0.0, yy = 0.0;
+        /* one pass per ray: the forward sum and the adjoint accumulation */
+        forward_one_ray(p, spectrum, NULL, seg, a1, a2, NULL, cb, 0.0, 1.0, 0.0, 1.0, rays[i], &nn, &cc,
+                        NULL, NULL, x, &yy, gpriv ? gpriv + (size_t)t * (size_t)ng : NULL, w ? w[i] : 0.0);
+        if (y_out) y_out[i] = yy;
+    }
+    if (g_out) {
+        for (int64_t j = 0; j < ng; j++) {
+            double s = 0.0;
+            for (int t = 0; t < nt; t++) s += gpriv[(size_t)t * (size_t)ng + (size_t)j];
+            g_out[j] = s;
+        }
+        free(gpriv);
+    }
+    free(cb);
     return 0;
 }

@@ -55,6 +55,17 @@ int32_t xrdt_oracle_forward_rays(const xrdt_problem *p,
                                  double *N_out, double *C_out, double *A_out,
                                  double *Av_out, int32_t n_threads);
 
+/* The per-voxel-coefficient model of the same rays: Av[r][v][k] is the
+ * coarse-q model term of integrate_diffraction.cu:311-315 for voxel v alone
+ * (the Amatrix row before it is summed per material).  With x [nx*ny][nwt]
+ * (voxel index nx+ny*NX) it writes y_out[i] = sum_{v,k} Av[rays[i]][v][k] x[v][k];
+ * with w [n_rays] it writes g_out[v][k] = sum_i w[i] Av[rays[i]][v][k].  Either
+ * pair may be NULL.  Returns 0, or a negative value for invalid input. */
+int32_t xrdt_oracle_vox_rays(const xrdt_problem *p, const float *spectrum, const int32_t *seg,
+                             const float *a1, const float *a2, const double *x, const double *w,
+                             const int64_t *rays, int64_t n_rays, double *y_out, double *g_out,
+                             int32_t n_threads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,229 @@
+"""The per-voxel-coefficient operator (xrdt_op_*): forward, adjoint and MLEM
+against the FP64 oracle, the reference's per-material model matrix, and the
+size-independent properties of a linear operator and its transpose."""
+import numpy as np
+import pytest
+
+import xrd_tomography_gb300 as xt
+from xrd_tomography_gb300 import synth
+from tests.tolerances import FAST_RTOL, max_rel_err
+
+pytestmark = pytest.mark.gpu
+
+MLEM_RTOL = 1e-4   # FP32 iterates with FP64 sums, after tens of iterations
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+@pytest.fixture(scope="module")
+def ctx(torch_cuda):
+    c = xt.Context(0)
+    yield c
+    c.close()
+
+
+def make_op(inp, ctx):
+    return xt.Operator(inp.problem, inp.spectrum, inp.seg, inp.a1, inp.a2, ctx=ctx)
+
+
+def rand_x(inp, seed):
+    """Random coefficients on the non-empty voxels, 0 elsewhere."""
+    p = inp.problem
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(0.0, 1.0, (p.nx * p.ny, p.nwt)).astype(np.float32)
+    x[np.asarray(inp.seg).reshape(-1) == 0] = 0.0
+    return x.reshape(-1)
+
+
+def test_tiny_forward_adjoint_match_oracle(ctx, oracle_lib):
+    inp = synth.make_inputs(synth.tiny_problem(), 7)
+    p = inp.problem
+    op = make_op(inp, ctx)
+    assert op.voxels == int((np.asarray(inp.seg) > 0).sum())
+    x = rand_x(inp, 1)
+    rays = np.arange(p.rays)
+    w = np.random.default_rng(2).uniform(0.0, 2.0, p.rays).astype(np.float32)
+    y_ref, g_ref = oracle_lib.vox_rays(inp, rays, x=x, w=w)
+    y = op.forward(x)
+    g = op.adjoint(w)
+    assert max_rel_err(y, y_ref) < FAST_RTOL
+    assert max_rel_err(g, g_ref.reshape(-1)) < FAST_RTOL
+    # empty voxels carry no unknowns: nothing flows back to them
+    empty = np.repeat(np.asarray(inp.seg).reshape(-1) == 0, p.nwt)
+    assert not np.any(g[empty])
+    op.close()
+
+
+def test_sub_phantom_adjoint_against_oracle_and_finite_differences(ctx, oracle_lib):
+    """16x16 sub-phantom in the 128^2 workload's scanner: the adjoint on a
+    sparse set of rays against the oracle, and finite differences of the
+    forward along random directions against the adjoint (the model is
+    linear, so a central difference is exact up to rounding)."""
+    inp = synth.sub_phantom_inputs()
+    p = inp.problem
+    op = make_op(inp, ctx)
+    rng = np.random.default_rng(11)
+    sel = np.sort(rng.choice(p.rays, 96, replace=False))
+    w = np.zeros(p.rays, np.float32)
+    w[sel] = rng.uniform(0.5, 1.5, sel.size)
+    _, g_ref = oracle_lib.vox_rays(inp, sel, w=w[sel])
+    g = op.adjoint(w)
+    assert max_rel_err(g, g_ref.reshape(-1)) < FAST_RTOL
+    x = rand_x(inp, 3)
+    y_ref, _ = oracle_lib.vox_rays(inp, sel, x=x)
+    y = op.forward(x)
+    assert max_rel_err(y[sel], y_ref) < FAST_RTOL
+    wfull = rng.uniform(0.0, 1.0, p.rays).astype(np.float32)
+    gfull = op.adjoint(wfull).astype(np.float64)
+    for seed in range(3):
+        d = rand_x(inp, 100 + seed)
+        h = 0.25
+        fd = (op.forward(x + h * d).astype(np.float64) - op.forward(x - h * d).astype(np.float64)) / (2 * h)
+        lhs = float(wfull.astype(np.float64) @ fd)
+        rhs = float(gfull @ d.astype(np.float64))
+        assert abs(lhs - rhs) <= 1e-5 * abs(rhs), (seed, lhs, rhs)
+    op.close()
+
+
+def test_voxel_sums_reproduce_the_model_matrix(ctx):
+    """Setting every voxel to its material's pattern makes the per-voxel
+    forward equal Amatrix times the patterns, and the per-material sums of
+    the adjoint equal Amatrix^T w (Amatrix from xrdt_forward)."""
+    inp = synth.config_inputs(0)
+    p = inp.problem
+    N, C, A = xt.forward(p, *inp.args(), ctx=ctx)
+    A = np.asarray(A, np.float64).reshape(p.rays, p.n_mat, p.nwt)
+    rng = np.random.default_rng(4)
+    xm = rng.uniform(0.0, 1.0, (p.n_mat, p.nwt))
+    seg = np.asarray(inp.seg).reshape(-1)
+    x = np.zeros((seg.size, p.nwt), np.float32)
+    x[seg > 0] = xm[seg[seg > 0] - 1]
+    op = make_op(inp, ctx)
+    y = op.forward(x.reshape(-1))
+    y_ref = np.einsum("rmk,mk->r", A, xm)
+    assert max_rel_err(y, y_ref) < FAST_RTOL
+    w = rng.uniform(0.0, 1.0, p.rays)
+    g = op.adjoint(w.astype(np.float32)).astype(np.float64).reshape(seg.size, p.nwt)
+    gm = np.stack([g[seg == m + 1].sum(axis=0) for m in range(p.n_mat)])
+    gm_ref = np.einsum("r,rmk->mk", w, A)
+    assert max_rel_err(gm, gm_ref) < FAST_RTOL
+    op.close()
+
+
+def test_full_size_dot_product_and_linearity(ctx, torch_cuda):
+    """128^2 phantom, every ray, device buffers: <A x, w> = <x, A^T w>,
+    and A(a x1 + b x2) = a A x1 + b A x2."""
+    torch = torch_cuda
+    inp = synth.config_inputs(2)
+    p = inp.problem
+    op = make_op(inp, ctx)
+    x1 = torch.from_numpy(rand_x(inp, 5)).cuda()
+    x2 = torch.from_numpy(rand_x(inp, 6)).cuda()
+    w = torch.rand(p.rays, generator=torch.Generator().manual_seed(7)).cuda()
+    y1 = op.forward(x1, torch.empty(p.rays, device="cuda"))
+    y2 = op.forward(x2, torch.empty(p.rays, device="cuda"))
+    g = op.adjoint(w, torch.empty(op.unknowns, device="cuda"))
+    lhs = float((y1.double() * w.double()).sum())
+    rhs = float((g.double() * x1.double()).sum())
+    assert abs(lhs - rhs) <= 1e-5 * abs(rhs)
+    y12 = op.forward(2.0 * x1 + 0.5 * x2, torch.empty(p.rays, device="cuda"))
+    assert max_rel_err(y12.cpu().numpy(), (2.0 * y1.double() + 0.5 * y2.double()).cpu().numpy()) < FAST_RTOL
+    # the same call twice gives the same bits
+    y1b = op.forward(x1, torch.empty(p.rays, device="cuda"))
+    assert torch.equal(y1, y1b)
+    op.close()
+
+
+def mlem_dense(A, y, c, x0, iters):
+    """main.m:162-176 with a dense per-voxel matrix, in FP64."""
+    x = np.asarray(x0, np.float64).copy()
+    sens = A.sum(axis=0)
+    for _ in range(iters):
+        r = y / (A @ x + c + 1e-20)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            x = x * (A.T @ r) / (sens + 1e-7)
+        x[~np.isfinite(x)] = 0.0
+        x[x < 0] = 0.0
+    return x
+
+
+def test_tiny_mlem_matches_dense_restatement(ctx, oracle_lib):
+    inp = synth.make_inputs(synth.tiny_problem(), 9)
+    p = inp.problem
+    rays = np.arange(p.rays)
+    _, _, _, Av = oracle_lib.forward_rays(inp, rays, want_av=True)
+    A = Av.reshape(p.rays, -1)
+    xt_true = synth.vox_truth(inp).astype(np.float64)
+    ybar = A @ xt_true
+    c = np.full(p.rays, 0.05 * ybar.mean())
+    y = np.random.default_rng(1).poisson(ybar / ybar.max() * 1e3 + c).astype(np.float64) * (ybar.max() / 1e3)
+    c = c * (ybar.max() / 1e3)
+    x0 = np.where(np.repeat(np.asarray(inp.seg).reshape(-1) > 0, p.nwt), 1.0, 0.0)
+    op = make_op(inp, ctx)
+    for iters in (1, 5, 20):
+        x = op.mlem(y.astype(np.float32), c.astype(np.float32), x0.astype(np.float32), iters)
+        xr = mlem_dense(A, y, c, x0, iters)
+        assert max_rel_err(x, xr, floor=1e-4) < MLEM_RTOL, iters
+    op.close()
+
+
+def test_full_size_mlem_graph_equals_composed_calls(ctx, torch_cuda):
+    """The captured MLEM iteration against the same update composed from the
+    public forward and adjoint calls, on the 128^2 workload."""
+    torch = torch_cuda
+    inp = synth.config_inputs(2)
+    p = inp.problem
+    op = make_op(inp, ctx)
+    xtrue = torch.from_numpy(synth.vox_truth(inp)).cuda()
+    ybar = op.forward(xtrue, torch.empty(p.rays, device="cuda")).double()
+    scale = 1e3 / float(ybar.max())
+    c = torch.full_like(ybar, 0.05 * float(ybar.mean()) * scale).float()
+    y = torch.poisson(ybar * scale + c.double(), generator=torch.Generator(device="cuda").manual_seed(3)).float()
+    on = torch.from_numpy(np.repeat(np.asarray(inp.seg).reshape(-1) > 0, p.nwt)).cuda()
+    x0 = torch.where(on, 1.0, 0.0).float()
+    sens = op.adjoint(torch.ones(p.rays, device="cuda"), torch.empty(op.unknowns, device="cuda")).double()
+    xr = x0.clone()
+    for _ in range(3):
+        ax = op.forward(xr, torch.empty(p.rays, device="cuda")).double()
+        r = (y.double() / (ax + c.double() + 1e-20)).float()
+        g = op.adjoint(r, torch.empty(op.unknowns, device="cuda")).double()
+        xn = xr.double() * g / (sens + 1e-7)
+        xn[~torch.isfinite(xn)] = 0
+        xr = xn.clamp_min(0).float()
+    x = x0.clone()
+    op.mlem(y, c, x, 3)
+    torch.cuda.synchronize()
+    assert max_rel_err(x.cpu().numpy(), xr.cpu().numpy(), floor=1e-4) < MLEM_RTOL
+    # the estimate moves towards the data: the Poisson log-likelihood rises
+    def loglik(xx):
+        m = op.forward(xx, torch.empty(p.rays, device="cuda")).double() + c.double()
+        return float((y.double() * torch.log(m) - m).sum())
+    assert loglik(x) > loglik(x0)
+    op.close()
+
+
+def test_operator_errors(ctx):
+    inp = synth.make_inputs(synth.tiny_problem(), 7)
+    p = inp.problem
+    bad = inp.seg.copy()
+    bad[3] = p.n_mat + 1
+    with pytest.raises(xt.XrdtError) as e:
+        xt.Operator(p, inp.spectrum, bad, inp.a1, inp.a2, ctx=ctx)
+    assert e.value.status == 4
+    op = make_op(inp, ctx)
+    with pytest.raises(xt.XrdtError):
+        op.mlem(np.ones(p.rays, np.float32), np.zeros(p.rays, np.float32), np.ones(op.unknowns, np.float32), -1)
+    op.close()
+    empty = synth.make_inputs(synth.tiny_problem(), 7)
+    empty.seg[:] = 0
+    op = make_op(empty, ctx)
+    assert op.voxels == 0
+    assert not op.forward(np.ones(op.unknowns, np.float32)).any()
+    assert not op.adjoint(np.ones(p.rays, np.float32)).any()
+    op.close()

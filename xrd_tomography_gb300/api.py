@@ -25,7 +25,7 @@ LIB_PATH = os.path.join(HERE, "libxrdt.so")
 FWD_PLAIN_FP64 = 0x1
 FWD_NO_SYNC = 0x2
 (KERNEL_PREP_MAP, KERNEL_PREP_VOXELS, KERNEL_SRC_ATTEN, KERNEL_FORWARD, KERNEL_PLAIN, KERNEL_GATHER,
- KERNEL_MLEM) = range(7)
+ KERNEL_MLEM, KERNEL_VOX_FORWARD, KERNEL_VOX_ADJOINT, KERNEL_VOX_UPDATE) = range(10)
 
 _P = ctypes.POINTER(Problem)
 _vp = ctypes.c_void_p
@@ -52,6 +52,12 @@ SIGNATURES = {
                                           ctypes.c_uint32]),
     "xrdt_mlem_matrix_noalloc": (ctypes.c_int32, [_vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp, _vp, ctypes.c_int32,
                                                   _vp]),
+    "xrdt_op_create": (ctypes.c_int32, [_vp, _P, _vp, _vp, _vp, _vp, ctypes.POINTER(_vp)]),
+    "xrdt_op_destroy": (ctypes.c_int32, [_vp]),
+    "xrdt_op_voxels": (ctypes.c_int64, [_vp]),
+    "xrdt_op_forward": (ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_uint32]),
+    "xrdt_op_adjoint": (ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_uint32]),
+    "xrdt_op_mlem": (ctypes.c_int32, [_vp, _vp, _vp, _vp, ctypes.c_int32, ctypes.c_uint32]),
     "xrdt_forward_rays": (ctypes.c_int32, [_vp, _P, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_float,
                                            ctypes.c_float, ctypes.c_float, ctypes.c_float, _vp, ctypes.c_int64,
                                            _vp, _vp, _vp, ctypes.c_uint32]),
@@ -250,6 +256,77 @@ def mlem_matrix_noalloc(A, y, c, x, iters: int, stream: int | None = None):
     _check(lib().xrdt_mlem_matrix_noalloc(A.data_ptr(), int(y.numel()), int(x.numel()), y.data_ptr(),
                                           c.data_ptr(), x.data_ptr(), iters, _vp(stream) if stream else None))
     return x
+
+
+class Operator:
+    """xrdt_op: the model with one coarse-q pattern per voxel, as a
+    forward/backward context (include/xrdt.h).
+
+    Coefficients x and gradients g have NX*NY*NWT entries, voxel index
+    ix + NX*iy, coarse bin fastest; ray vectors have p.rays entries in the
+    Nphotons order.  Arrays may be numpy (host) or contiguous torch CUDA
+    tensors; outputs default to new numpy arrays."""
+
+    def __init__(self, p: Problem, spectrum, seg, a1, a2, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self.p = p
+        keep = [_ptr(a, dt) for a, dt in ((spectrum, np.float32), (seg, np.int32), (a1, np.float32),
+                                          (a2, np.float32))]
+        h = _vp()
+        _check(lib().xrdt_op_create(self.ctx.h, ctypes.byref(p), *[k[0] for k in keep], ctypes.byref(h)),
+               self.ctx.h)
+        self.h = h
+
+    @property
+    def voxels(self) -> int:
+        return int(lib().xrdt_op_voxels(self.h))
+
+    @property
+    def unknowns(self) -> int:
+        return self.p.nx * self.p.ny * self.p.nwt
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().xrdt_op_destroy(self.h)
+            self.h = None
+
+    def __del__(self):  # pragma: no cover - interpreter shutdown order
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def forward(self, x, y=None):
+        """y = Av x."""
+        px, kx = _ptr(x, np.float32)
+        if y is None:
+            y = np.empty(self.p.rays, np.float32)
+        py, ky = _ptr(y, np.float32)
+        _check(lib().xrdt_op_forward(self.h, px, py, 0), self.ctx.h)
+        return ky
+
+    def adjoint(self, w, g=None):
+        """g = Av^T w."""
+        pw, kw = _ptr(w, np.float32)
+        if g is None:
+            g = np.empty(self.unknowns, np.float32)
+        pg, kg = _ptr(g, np.float32)
+        _check(lib().xrdt_op_adjoint(self.h, pw, pg, 0), self.ctx.h)
+        return kg
+
+    def mlem(self, y, c, x0, iters: int):
+        """iters MLEM updates from x0 (main.m:162-176 with per-voxel unknowns).
+        A torch CUDA x0 is updated in place; numpy returns a new array."""
+        py, ky = _ptr(y, np.float32)
+        pc, kc = _ptr(c, np.float32)
+        if hasattr(x0, "data_ptr"):
+            x = x0
+            px = x.data_ptr()
+        else:
+            x = np.array(x0, dtype=np.float32, copy=True).reshape(-1)
+            px = x.ctypes.data
+        _check(lib().xrdt_op_mlem(self.h, py, pc, px, iters, 0), self.ctx.h)
+        return x
 
 
 def Forward_XRD(spectrum, Ifine, segmentation, a1, a2, S2, q_min, q_max, a_min, a_max,

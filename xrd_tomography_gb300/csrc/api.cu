@@ -14,36 +14,9 @@
 #include <string>
 #include <vector>
 
-#include "xrdt_device.cuh"
+#include "ctx.h"
 
 using namespace xrdt;
-
-struct xrdt_ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    std::string err;
-    int64_t launches = 0;
-    // grow-only device buffers, one per slot
-    std::vector<void *> buf;
-    std::vector<size_t> cap;
-    int *h_counters = nullptr;  // pinned
-    // profiling: events bracketing launches, folded into totals on query
-    bool profiling = false;
-    struct Pending {
-        int kernel;
-        cudaEvent_t a, b;
-    };
-    std::vector<Pending> pending;
-    int64_t prof_launches[XRDT_KERNEL_COUNT] = {};
-    double prof_ms[XRDT_KERNEL_COUNT] = {};
-    unsigned long long *d_work = nullptr;  // exp2 evaluations of the forward kernel
-    // MLEM iteration captured as a graph, keyed by its arguments
-    cudaGraphExec_t mlem_exec = nullptr;
-    const void *mlem_key[6] = {};
-    long long mlem_rays = 0;
-    int mlem_K = 0;
-};
 
 namespace xrdt {
 
@@ -75,26 +48,6 @@ int fail(xrdt_ctx *c, int status, const std::string &msg)
     if (c) c->err = msg;
     return status;
 }
-
-// Brackets one kernel group with events when profiling is on.
-struct ProfScope {
-    xrdt_ctx *ctx;
-    int kernel;
-    cudaEvent_t a = nullptr, b = nullptr;
-    ProfScope(xrdt_ctx *c, int k) : ctx(c), kernel(k)
-    {
-        if (!ctx->profiling) return;
-        cudaEventCreate(&a);
-        cudaEventCreate(&b);
-        cudaEventRecord(a, ctx->stream);
-    }
-    ~ProfScope()
-    {
-        if (!a) return;
-        cudaEventRecord(b, ctx->stream);
-        ctx->pending.push_back({kernel, a, b});
-    }
-};
 
 void fold_pending(xrdt_ctx *ctx)
 {
@@ -144,16 +97,6 @@ int get_buf(xrdt_ctx *ctx, int slot, size_t bytes, void **out)
     }
     *out = ctx->buf[slot];
     return XRDT_OK;
-}
-
-bool is_device_ptr(const void *p)
-{
-    cudaPointerAttributes a;
-    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
-        cudaGetLastError();
-        return false;
-    }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
 // Device view of an input: the pointer itself, or a staged copy.
@@ -271,6 +214,84 @@ int build_dev_problem(const xrdt_problem *p, float q_min, float q_max, float a_m
     d->e_hi = hi_all;
     (void)err;
     return XRDT_OK;
+}
+
+void build_host_tables(const xrdt_problem *p, const DevProblem &P, const float *spec_h, HostTables *t)
+{
+    const int W = 2 * p->dnrg + 1;
+    // energy rows
+    t->energy.resize(p->nrg_src);
+    for (int e = 0; e < p->nrg_src; e++) {
+        EnergyRow &r = t->energy[e];
+        r.Esrc1 = P.e_src_min + (double)e * P.dEs;
+        r.Esrc2 = P.e_src_min + (double)(e + 1) * P.dEs;
+        r.Esrc = 0.5 * (r.Esrc1 + r.Esrc2);
+        r.ein = r.Esrc / P.mec2;
+        const double f1 = r.ein * r.ein * r.ein, f2 = P.kn0 + P.kn1 * r.ein + P.kn2 * r.ein * r.ein;
+        r.inv_f1 = (float)(1.0 / f1);
+        r.inv_f2 = (float)(1.0 / f2);
+        const double wf = 2.0 * r.Esrc / P.hbarc;
+        r.wfac_hi = (float)wf;
+        r.wfac_lo = (float)(wf - (double)r.wfac_hi);
+        r.sig_c1 = (float)((2.0 / P.hbarc) * (2.0 / P.hbarc) * P.dEs * P.dEs / 12.0);
+        r.sig_c2 = (float)((r.Esrc / P.hbarc) * (r.Esrc / P.hbarc) / 4.0);
+        r.einf = (float)r.ein;
+        r.Esrc1f = (float)r.Esrc1;
+        r.Esrc2f = (float)r.Esrc2;
+        r.pad = 0.f;
+    }
+    // spectrum windows: detector bin n takes source bins win_lo[n] .. + W-1
+    // with weights RF = spectrum[e + n*nrg_src]; win_n[e] = the detector bins
+    // whose window holds e
+    const int same = (p->nrg_src == p->nrg_det && p->e_src_min == p->e_det_min && p->e_src_max == p->e_det_max);
+    t->rf_win.assign((size_t)p->nrg_det * W, 0.f);
+    t->win_lo.assign(p->nrg_det, 0);
+    t->win_n.assign(2 * (size_t)p->nrg_src, 0);
+    for (int e = 0; e < p->nrg_src; e++) {
+        t->win_n[2 * e] = p->nrg_det;
+        t->win_n[2 * e + 1] = -1;
+    }
+    for (int n = 0; n < p->nrg_det; n++) {
+        int lo, hi;
+        src_nrg_range(P, same, n, &lo, &hi);
+        t->win_lo[n] = lo;
+        for (int j = 0; j < W; j++) {
+            t->rf_win[(size_t)n * W + j] = spec_h[(lo + j) + (size_t)n * p->nrg_src];
+            const int e = lo + j;
+            if (n < t->win_n[2 * e]) t->win_n[2 * e] = n;
+            if (n > t->win_n[2 * e + 1]) t->win_n[2 * e + 1] = n;
+        }
+    }
+    // Compton slots: for source bin e, slot s is detector bin win_n(e) + s
+    t->sl = 1;
+    for (int e = 0; e < p->nrg_src; e++)
+        if (t->win_n[2 * e + 1] >= t->win_n[2 * e]) t->sl = std::max(t->sl, t->win_n[2 * e + 1] - t->win_n[2 * e] + 1);
+    t->offs_e.assign((size_t)p->nrg_src * t->sl, 0.f);
+    for (int e = 0; e < p->nrg_src; e++)
+        for (int s = 0; s < t->sl; s++) {
+            const double Ed1 = P.e_det_min + (double)(t->win_n[2 * e] + s) * P.dEd;
+            t->offs_e[(size_t)e * t->sl + s] = (float)((P.e_src_min + (double)e * P.dEs) - Ed1);
+        }
+    t->fine_q.resize(p->nqf);
+    for (int j = 0; j < p->nqf; j++) {
+        const double q = P.q_lo + P.dq_fine * (0.5 + (double)j);
+        t->fine_q[j].x = (float)q;
+        t->fine_q[j].y = (float)(q - (double)t->fine_q[j].x);
+    }
+    // coarse bins of wvt_value.cu:8-22: centre as a pair, width
+    t->coarse_q.resize(p->nwt);
+    for (int k = 0; k < p->nwt; k++) {
+        const double NWT = (double)p->nwt;
+        const double e1 = p->q_lo + (double)k * p->dq0 +
+                          (p->q_hi - p->q_lo - p->dq0 * NWT) * (double)((int64_t)k * k) / (NWT * NWT);
+        const double e2 = p->q_lo + (double)(k + 1) * p->dq0 +
+                          (p->q_hi - p->q_lo - p->dq0 * NWT) * (double)((int64_t)(k + 1) * (k + 1)) / (NWT * NWT);
+        const double q = 0.5 * (e1 + e2);
+        t->coarse_q[k].x = (float)q;
+        t->coarse_q[k].y = (float)(q - (double)t->coarse_q[k].x);
+        t->coarse_q[k].z = (float)(e2 - e1);
+        t->coarse_q[k].w = 0.f;
+    }
 }
 
 } // namespace xrdt
@@ -523,7 +544,6 @@ int forward_impl(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, co
     const int64_t nvox = (int64_t)p->nx * p->ny;
     const int64_t all_rays = xrdt_problem_rays(p);
     const int64_t MW = (int64_t)p->nwt * p->n_mat;
-    const int W = 2 * p->dnrg + 1;
     if (ray_list) {
         if (n_list < 0 || n_list > 2147483647LL) return fail(ctx, XRDT_ERR_DIMS, "bad ray count");
         if (is_device_ptr(ray_list)) return fail(ctx, XRDT_ERR_UNSUPPORTED, "the ray list must be host memory");
@@ -616,34 +636,6 @@ int forward_impl(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, co
         CK(cudaMemsetAsync(dC, 0, sizeof(float) * rays, st));
         if (dA) CK(cudaMemsetAsync(dA, 0, sizeof(float) * aelems, st));
     } else {
-        // energy rows
-        std::vector<EnergyRow> er(p->nrg_src);
-        for (int e = 0; e < p->nrg_src; e++) {
-            EnergyRow &r = er[e];
-            r.Esrc1 = P.e_src_min + (double)e * P.dEs;
-            r.Esrc2 = P.e_src_min + (double)(e + 1) * P.dEs;
-            r.Esrc = 0.5 * (r.Esrc1 + r.Esrc2);
-            r.ein = r.Esrc / P.mec2;
-            const double f1 = r.ein * r.ein * r.ein, f2 = P.kn0 + P.kn1 * r.ein + P.kn2 * r.ein * r.ein;
-            r.inv_f1 = (float)(1.0 / f1);
-            r.inv_f2 = (float)(1.0 / f2);
-            const double wf = 2.0 * r.Esrc / P.hbarc;
-            r.wfac_hi = (float)wf;
-            r.wfac_lo = (float)(wf - (double)r.wfac_hi);
-            r.sig_c1 = (float)((2.0 / P.hbarc) * (2.0 / P.hbarc) * P.dEs * P.dEs / 12.0);
-            r.sig_c2 = (float)((r.Esrc / P.hbarc) * (r.Esrc / P.hbarc) / 4.0);
-            r.einf = (float)r.ein;
-            r.Esrc1f = (float)r.Esrc1;
-            r.Esrc2f = (float)r.Esrc2;
-            r.pad = 0.f;
-        }
-        const int same = (p->nrg_src == p->nrg_det && p->e_src_min == p->e_det_min && p->e_src_max == p->e_det_max);
-        std::vector<float> rfw((size_t)p->nrg_det * W);
-        std::vector<int> wlo(p->nrg_det), wn(2 * (size_t)p->nrg_src);
-        for (int e = 0; e < p->nrg_src; e++) {
-            wn[2 * e] = p->nrg_det;
-            wn[2 * e + 1] = -1;
-        }
         std::vector<float> hspec;
         const float *spec_h = spectrum;
         if (is_device_ptr(spectrum)) {
@@ -651,46 +643,14 @@ int forward_impl(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, co
             CK(cudaMemcpy(hspec.data(), spectrum, sizeof(float) * hspec.size(), cudaMemcpyDeviceToHost));
             spec_h = hspec.data();
         }
-        for (int n = 0; n < p->nrg_det; n++) {
-            int lo, hi;
-            src_nrg_range(P, same, n, &lo, &hi);
-            wlo[n] = lo;
-            for (int j = 0; j < W; j++) {
-                rfw[(size_t)n * W + j] = spec_h[(lo + j) + (size_t)n * p->nrg_src];
-                const int e = lo + j;
-                if (n < wn[2 * e]) wn[2 * e] = n;
-                if (n > wn[2 * e + 1]) wn[2 * e + 1] = n;
-            }
-        }
-        // Compton slots: for source bin e, slot s is detector bin win_n(e) + s
-        int sl = 1;
-        for (int e = 0; e < p->nrg_src; e++)
-            if (wn[2 * e + 1] >= wn[2 * e]) sl = std::max(sl, wn[2 * e + 1] - wn[2 * e] + 1);
-        std::vector<float> offs_e((size_t)p->nrg_src * sl, 0.f);
-        for (int e = 0; e < p->nrg_src; e++)
-            for (int s = 0; s < sl; s++) {
-                const double Ed1 = P.e_det_min + (double)(wn[2 * e] + s) * P.dEd;
-                offs_e[(size_t)e * sl + s] = (float)((P.e_src_min + (double)e * P.dEs) - Ed1);
-            }
-        std::vector<float2> fq(p->nqf);
-        for (int j = 0; j < p->nqf; j++) {
-            const double q = P.q_lo + P.dq_fine * (0.5 + (double)j);
-            fq[j].x = (float)q;
-            fq[j].y = (float)(q - (double)fq[j].x);
-        }
-        std::vector<float4> cqf(p->nwt);
-        for (int k = 0; k < p->nwt; k++) {
-            const double NWT = (double)p->nwt;
-            const double e1 = p->q_lo + (double)k * p->dq0 +
-                              (p->q_hi - p->q_lo - p->dq0 * NWT) * (double)((int64_t)k * k) / (NWT * NWT);
-            const double e2 = p->q_lo + (double)(k + 1) * p->dq0 +
-                              (p->q_hi - p->q_lo - p->dq0 * NWT) * (double)((int64_t)(k + 1) * (k + 1)) / (NWT * NWT);
-            const double q = 0.5 * (e1 + e2);
-            cqf[k].x = (float)q;
-            cqf[k].y = (float)(q - (double)cqf[k].x);
-            cqf[k].z = (float)(e2 - e1);
-            cqf[k].w = 0.f;
-        }
+        HostTables ht;
+        build_host_tables(p, P, spec_h, &ht);
+        const std::vector<EnergyRow> &er = ht.energy;
+        const std::vector<float> &rfw = ht.rf_win, &offs_e = ht.offs_e;
+        const std::vector<int> &wlo = ht.win_lo, &wn = ht.win_n;
+        const std::vector<float2> &fq = ht.fine_q;
+        const std::vector<float4> &cqf = ht.coarse_q;
+        const int sl = ht.sl;
         FwdTables T;
         void *d;
         if ((rc = get_buf(ctx, S_ENERGY, sizeof(EnergyRow) * er.size(), &d))) return rc;

@@ -27,9 +27,7 @@
 // for each voxel of the chunk the warp walks its detector-side ray together
 // and lane = source energy evaluates the (voxel, energy) term, so each lane
 // keeps the running sum of its own energies in registers.
-#include "xrdt_device.cuh"
-#include "ff.cuh"
-#include "walk.cuh"
+#include "scatter.cuh"
 
 namespace xrdt {
 
@@ -37,43 +35,6 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr float kSig = 7.5f;            // Gaussian window, in sigma (tail below 7e-13)
-constexpr float kLog2e = 1.4426950408889634f;
-
-__device__ __forceinline__ void kahan_add(float &s, float &c, float x)
-{
-    const float y = x - c;
-    const float t = s + y;
-    c = (t - s) - y;
-    s = t;
-}
-
-// SFU approximations with denormals flushed (no denormal fix-up code; the
-// arguments here are far from the denormal range)
-__device__ __forceinline__ float ex2_approx(float x)
-{
-    float y;
-    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-__device__ __forceinline__ float rcp_approx(float x)
-{
-    float y;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-__device__ __forceinline__ float lg2_approx(float x)
-{
-    float y;
-    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-__device__ __forceinline__ float rsqrt_approx(float x)
-{
-    float y;
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
 
 // Compton table bin of integrate_diffraction.cu:331-337 decided in FP64, as
 // the oracle decides it; used only when the FP32 value lies within 2e-4 of a
@@ -87,82 +48,6 @@ __device__ __noinline__ int compton_bin_f64(const DevProblem &P, double ein, flo
     const double wd = ein * sd;
     const double l2d = log2(wd * sqrt(erd + wd * wd) / erd);
     return floor_to_int((l2d - P.q_min) / P.dq_tab);
-}
-
-// FP64 walk set-up out of line, for the same reason.
-__device__ __noinline__ void walk_setup_f64(const DevProblem &P, double ex, double ey, double vx, double vy,
-                                            WalkSetup *w)
-{
-    walk_setup(P, ex, ey, vx, vy, w);
-}
-
-// Per-(source, pixel) constants of the scattering geometry.
-struct PairGeom {
-    ff Rsx, Rsy, Rdx, Rdy, Rdz;   // source and detector positions
-    ff k1;                        // tan(geomphi/2) / |nsrc_xy|
-    ff nsx2, nsy2;                // in-plane source orientation as pairs
-    float nsx, nsy, nsz, ndx, ndy, sphi, cphi;
-    float k2;                     // tan(geomphi) / |nsrc_xy|
-    float tan_full, adet12, vox2, focal2_12;
-};
-
-// Per-voxel results of the scattering geometry.
-struct VoxGeom {
-    ff s;        // sin(theta/2)
-    ff omc;      // 1 - cos(theta)
-    float sg;    // (sS2 + vV2 + dD2) / (|a|^2 |b|^2)
-    float gp;    // geom_src2vox * geom_vox2det
-    float Wg;    // gp * Rayleigh factor
-    float cos2;  // cos^2(theta)
-};
-
-// integrate_diffraction.cu:196-255 for one voxel.  a = voxel - source and
-// b = detector - voxel as float pairs; 1 - cos(theta) from the cross product
-// |a x b|^2 / (|a||b| (|a||b| + a.b)), which has no cancellation at small
-// angles; the blur vectors S = ((a x b) x a)/|a|^2 = b - (a.b/|a|^2) a and
-// D = ((a x b) x b)/|b|^2 = -a + (a.b/|b|^2) b in FP32.
-__device__ __forceinline__ VoxGeom vox_geom(const PairGeom &G, float vx, float vy)
-{
-    const ff ax = ff_fsub(vx, G.Rsx), ay = ff_fsub(vy, G.Rsy);
-    const ff proj = ff_add(ff_mul(ax, G.nsx2), ff_mul(ay, G.nsy2));
-    const ff az = ff_neg(ff_mul(proj, G.k1));          // Rvox_z; Rsrc_z = 0
-    const float Hvox = proj.hi * G.k2;
-    const ff bx = ff_add(G.Rdx, ff{-vx, 0.f}), by = ff_add(G.Rdy, ff{-vy, 0.f});
-    const ff bz = ff_sub(G.Rdz, az);
-    const ff ab = ff_add(ff_add(ff_mul(ax, bx), ff_mul(ay, by)), ff_mul(az, bz));
-    const ff an = ff_add(ff_add(ff_sqr(ax), ff_sqr(ay)), ff_sqr(az));
-    const ff bn = ff_add(ff_add(ff_sqr(bx), ff_sqr(by)), ff_sqr(bz));
-    const ff cx = ff_sub(ff_mul(ay, bz), ff_mul(az, by));
-    const ff cy = ff_sub(ff_mul(az, bx), ff_mul(ax, bz));
-    const ff cz = ff_sub(ff_mul(ax, by), ff_mul(ay, bx));
-    const ff cn = ff_add(ff_add(ff_sqr(cx), ff_sqr(cy)), ff_sqr(cz));
-    const ff nab = ff_sqrt(ff_mul(an, bn));
-    VoxGeom r;
-    if (ab.hi > 0.f) r.omc = ff_div(cn, ff_mul(nab, ff_add(nab, ab)));
-    else r.omc = ff_fsub(1.f, ff_div(ab, nab));
-    r.s = ff_sqrt(ff_mulf(r.omc, 0.5f));
-    const float costh = 1.f - r.omc.hi;
-    r.cos2 = costh * costh;
-    // FP32 remainder of the geometry
-    const float Ax = ax.hi, Ay = ay.hi, Az = az.hi, Bx = bx.hi, By = by.hi, Bz = bz.hi;
-    const float Cx = cx.hi, Cy = cy.hi, Cz = cz.hi, An = an.hi, Bn = bn.hi;
-    const float ia = __fdividef(1.f, An), ib = __fdividef(1.f, Bn);
-    const float Sx = (Cy * Az - Cz * Ay) * ia, Sy = (Cz * Ax - Cx * Az) * ia, Sz = (Cx * Ay - Cy * Ax) * ia;
-    const float Dx = (Cy * Bz - Cz * By) * ib, Dy = (Cz * Bx - Cx * Bz) * ib, Dz = (Cx * By - Cy * Bx) * ib;
-    const float Vx = -(Sx + Dx), Vy = -(Sy + Dy), Vz = -(Sz + Dz);
-    const float Dndet = Dx * G.ndx + Dy * G.ndy;
-    const float Snsrc = Sx * G.nsx + Sy * G.nsy + Sz * G.nsz;
-    const float dD2 = (Dx * Dx + Dy * Dy + Dz * Dz - Dndet * Dndet) * G.adet12;
-    const float vV2 = (G.vox2 * (Vx * Vx + Vy * Vy) + Hvox * Hvox * Vz * Vz) * (1.f / 12.f);
-    const float sS2 = (Sx * Sx + Sy * Sy + Sz * Sz - Snsrc * Snsrc) * G.focal2_12;
-    const float Rdotn = -G.sphi * Ax + G.cphi * Ay;
-    const float cospsi = Rdotn * rsqrtf(Ax * Ax + Ay * Ay);
-    const float gsv = cospsi * rsqrtf(An) * G.tan_full;
-    const float gvd = -(G.ndx * Bx + G.ndy * By) * rsqrtf(Bn * Bn * Bn);
-    r.gp = gsv * gvd;
-    r.Wg = r.gp * ((1.f + r.cos2) * 0.5f);
-    r.sg = (sS2 + vV2 + dD2) * ia * ib;
-    return r;
 }
 
 struct Layout {
@@ -293,33 +178,9 @@ k_fwd(const FwdArgs args)
 
     // ---- per-(source, pixel) geometry, integrate_diffraction.cu:81-128 ----
     const SrcGeom g = args.sg[src];
-    double Rdet_x, Rdet_y, Rdet_z;
-    det_position(P, g.sphi, g.cphi, det, &Rdet_x, &Rdet_y, &Rdet_z);
+    double Rdet_x, Rdet_y;
     PairGeom G;
-    G.Rsx = ff_from_double(g.Rsrc_x);
-    G.Rsy = ff_from_double(g.Rsrc_y);
-    G.Rdx = ff_from_double(Rdet_x);
-    G.Rdy = ff_from_double(Rdet_y);
-    G.Rdz = ff_from_double(Rdet_z);
-    {
-        const double nsx = -g.sphi * P.sta, nsy = g.cphi * P.sta, nsz = -P.cta;
-        const double nsxy = sqrt(nsx * nsx + nsy * nsy);
-        G.nsx = (float)nsx;
-        G.nsy = (float)nsy;
-        G.nsx2 = ff_from_double(nsx);
-        G.nsy2 = ff_from_double(nsy);
-        G.nsz = (float)nsz;
-        G.k1 = ff_from_double(P.tan_half / nsxy);
-        G.k2 = (float)(P.tan_full / nsxy);
-    }
-    G.ndx = (float)g.sphi;
-    G.ndy = (float)(-g.cphi);
-    G.sphi = (float)g.sphi;
-    G.cphi = (float)g.cphi;
-    G.tan_full = (float)P.tan_full;
-    G.adet12 = (float)(P.geomAdet / 12.0);
-    G.vox2 = (float)(P.vox * P.vox);
-    G.focal2_12 = (float)(P.focal * P.focal / 12.0);
+    pair_geom(P, g, det, &G, &Rdet_x, &Rdet_y);
     const float Rdxf = (float)Rdet_x, Rdyf = (float)Rdet_y;
     const float rsqrt2pi = (float)P.rsqrt2pi;
     const float DQf = (float)P.DQ, inv_DQ = (float)(1.0 / P.DQ);
@@ -327,7 +188,7 @@ k_fwd(const FwdArgs args)
     const float inv_dqf = (float)(1.0 / P.dq_fine), qlo_f = (float)P.q_lo;
     const float kn0 = (float)P.kn0, kn1 = (float)P.kn1, kn2 = (float)P.kn2;
     const float edmin = (float)P.e_det_min, inv_dEd = (float)(1.0 / P.dEd), dEdf = (float)P.dEd;
-    const float dEsf = (float)P.dEs, esmin = (float)P.e_src_min;
+    const float dEsf = (float)P.dEs;
     const float qmin_t = (float)P.q_min, inv_dqt = (float)(1.0 / P.dq_tab);
     const int lo_e = P.e_lo;
     __syncthreads();
@@ -440,19 +301,8 @@ k_fwd(const FwdArgs args)
                         TNw[el] = k;
                     }
                     if (WITH_A) {
-                        // coarse bins near w: invert edge(n) = q_lo + b n + a n^2
-                        int klo = 0, khi = P.nwt - 1;
-                        {
-                            const float qa = w_hi - half - qlo_f, qb = w_hi + half - qlo_f;
-                            const float a = args.qpar_a, b = args.qpar_b;
-                            const float da = fmaf(4.f * a, qa, b * b), db = fmaf(4.f * a, qb, b * b);
-                            if (da >= 0.f && db >= 0.f) {
-                                const float na_ = 2.f * qa / (b + sqrtf(da));
-                                const float nb_ = 2.f * qb / (b + sqrtf(db));
-                                klo = max(klo, floor_nc(na_) - 1);
-                                khi = min(khi, floor_nc(nb_) + 1);
-                            }
-                        }
+                        int klo, khi;
+                        coarse_window(w_hi, half, qlo_f, args.qpar_a, args.qpar_b, P.nwt, &klo, &khi);
                         float *tar = TA + ((size_t)(el - pe0) * P.n_mat + m) * P.nwt;
                         nexp += (unsigned)max(0, khi - klo + 1);
                         for (int k = klo; k <= khi; k++) {

@@ -169,6 +169,14 @@ cudaError_t launch_prep_voxels(const DevProblem &P, const int32_t *seg, const fl
     return cudaGetLastError();
 }
 
+cudaError_t launch_compact_voxels(const DevProblem &P, const int32_t *seg, PrepBuffers &B, cudaStream_t s,
+                                  int64_t *launches)
+{
+    k_compact_voxels<<<1, 1024, 0, s>>>(P.nx, P.ny, P.n_mat, seg, B.vox_xy, B.vox_mat, B.counters);
+    if (launches) (*launches)++;
+    return cudaGetLastError();
+}
+
 cudaError_t launch_src_atten(const DevProblem &P, const SrcGeom *d_src, int nv, PrepBuffers &B,
                              cudaStream_t s, int64_t *launches)
 {

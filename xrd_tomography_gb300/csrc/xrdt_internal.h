@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string>
+#include <vector>
 
 #include "../../include/xrdt.h"
 
@@ -45,6 +46,20 @@ struct EnergyRow {
 };
 
 std::string fmt(const char *f, ...);
+
+// Per-call tables of the factored kernels, built on the host in double.
+struct HostTables {
+    std::vector<EnergyRow> energy;  // [nrg_src]
+    std::vector<float> rf_win;      // [nrg_det][2*dnrg+1]
+    std::vector<int> win_lo;        // [nrg_det]
+    std::vector<int> win_n;         // [nrg_src][2]
+    int sl = 1;
+    std::vector<float> offs_e;      // [nrg_src][sl]
+    std::vector<float2> fine_q;     // [nqf]
+    std::vector<float4> coarse_q;   // [nwt]
+};
+// spectrum: host copy [nrg_src][nrg_det] column-major as passed to Forward_XRD.
+void build_host_tables(const xrdt_problem *p, const DevProblem &P, const float *spectrum, HostTables *t);
 
 // ---- host-side builders (api.cu) ----
 int build_dev_problem(const xrdt_problem *p, float q_min, float q_max, float a_min,
@@ -109,5 +124,42 @@ cudaError_t launch_mlem_sensitivity(const float *A, long long rays, int K, float
 cudaError_t launch_mlem_iteration(const float *A, long long rays, int K, const float *y, const float *c,
                                   float *x, float *partial, int nparts, const double *sens, cudaStream_t s,
                                   int64_t *launches);
+
+// k_vox.cu: the per-voxel-coefficient model (forward, adjoint, MLEM update).
+struct PairRec;
+size_t pair_rec_bytes();
+struct VoxOp {
+    DevProblem P;
+    int nv;                    // non-empty voxels
+    const PairRec *pairs;      // [n_src * n_det]
+    const EnergyRow *energy;
+    const float *rf_win;
+    const int *win_lo, *win_n;
+    const float4 *coarse_q;
+    const int *vox_xy;
+    const float4 *cells;
+    const float2 *atten_src;
+};
+cudaError_t launch_compact_voxels(const DevProblem &P, const int32_t *seg, PrepBuffers &B, cudaStream_t s,
+                                  int64_t *launches);
+cudaError_t launch_pair_table(const DevProblem &P, const SrcGeom *sg, PairRec *out, cudaStream_t s,
+                              int64_t *launches);
+// Opts the operator kernels in to max_smem bytes of dynamic shared memory.
+cudaError_t vox_set_attributes(int max_smem);
+size_t vox_fwd_smem(const DevProblem &P);
+int vox_adj_warps(int K);
+size_t vox_adj_smem(const DevProblem &P, int warps);
+int vox_adj_groups(const VoxOp &op, int sm_count);
+// y = Av x (what == NULL), or the MLEM per-energy weights of y/(Av x + c).
+cudaError_t launch_vox_forward(const VoxOp &op, const float *xd, float *y, const float *ymeas, const float *cbg,
+                               float *what, cudaStream_t s, int64_t *launches);
+cudaError_t launch_vox_wtab(const VoxOp &op, const float *w, float *what, cudaStream_t s, int64_t *launches);
+cudaError_t launch_vox_adjoint(const VoxOp &op, const float *what, float *part, int groups, cudaStream_t s,
+                               int64_t *launches);
+cudaError_t launch_vox_reduce(const VoxOp &op, const float *part, int groups, int mode, double *sens, float *xc,
+                              float *xd, float *g, cudaStream_t s, int64_t *launches);
+cudaError_t launch_vox_gather(const VoxOp &op, const float *x, float *xc, float *xd, cudaStream_t s,
+                              int64_t *launches);
+cudaError_t launch_vox_scatter(const VoxOp &op, const float *xc, float *x, cudaStream_t s, int64_t *launches);
 
 } // namespace xrdt

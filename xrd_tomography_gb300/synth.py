@@ -214,3 +214,40 @@ def config_problem(index: int) -> Problem:
 
 def config_inputs(index: int) -> Inputs:
     return make_inputs(config_problem(index), SEED_BASE + index)
+
+
+def sub_phantom_inputs(side: int = 16, seed: int = SEED_BASE + 20) -> Inputs:
+    """A side x side phantom in the scanner of the 128^2 adjoint workload
+    (32 views, 128 px x 32 energy bins, 32 coarse bins): the size the adjoint
+    is checked on against the oracle."""
+    p = config_problem(2).copy(nx=side, ny=side)
+    p = scanner(p, 2.0, 300.0, 200.0, 1.0)
+    return make_inputs(p, seed, n_ellipses=3)
+
+
+def vox_truth(inp: Inputs) -> np.ndarray:
+    """Per-voxel coarse-q coefficients of the phantom: each non-empty voxel
+    carries its material's pattern averaged over the fine bins of each
+    coarse bin (wvt_value.cu:8-22 edges), times the voxel's density proxy
+    a2 / median(a2).  Layout [NX*NY*NWT], voxel index ix + NX*iy."""
+    p = inp.problem
+    nw = p.nwt
+    k = np.arange(nw + 1, dtype=np.float64)
+    a = (p.q_hi - p.q_lo - p.dq0 * nw) / (nw * nw)
+    edges = p.q_lo + p.dq0 * k + a * k * k
+    qf = p.q_lo + (p.q_hi - p.q_lo) / p.nqf * (np.arange(p.nqf) + 0.5)
+    I = np.asarray(inp.Ifine, np.float64).reshape(p.n_mat, p.nqf)
+    coarse = np.zeros((p.n_mat, nw))
+    for j in range(nw):
+        sel = (qf >= edges[j]) & (qf < edges[j + 1])
+        if sel.any():
+            coarse[:, j] = I[:, sel].mean(axis=1)
+        else:
+            coarse[:, j] = np.array([np.interp(0.5 * (edges[j] + edges[j + 1]), qf, I[m]) for m in range(p.n_mat)])
+    seg = np.asarray(inp.seg).reshape(-1)
+    a2 = np.asarray(inp.a2, np.float64).reshape(-1)
+    x = np.zeros((seg.size, nw))
+    on = seg > 0
+    dens = a2[on] / np.median(a2[on]) if on.any() else a2[on]
+    x[on] = coarse[seg[on] - 1] * dens[:, None]
+    return x.astype(np.float32).reshape(-1)
