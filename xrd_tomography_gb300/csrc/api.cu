@@ -216,6 +216,35 @@ int build_dev_problem(const xrdt_problem *p, float q_min, float q_max, float a_m
     return XRDT_OK;
 }
 
+F32Consts make_f32_consts(const DevProblem &P)
+{
+    F32Consts c;
+    c.vox = (float)P.vox;
+    c.DQ = (float)P.DQ;
+    c.inv_DQ = (float)(1.0 / P.DQ);
+    c.nxf = (float)P.nx;
+    c.nyf = (float)P.ny;
+    c.rsqrt2pi = (float)P.rsqrt2pi;
+    c.dqf_hi = (float)P.dq_fine;
+    c.dqf_lo = (float)(P.dq_fine - (double)c.dqf_hi);
+    c.inv_dqf = (float)(1.0 / P.dq_fine);
+    c.q_lo = (float)P.q_lo;
+    c.q_hi = (float)P.q_hi;
+    c.kn0 = (float)P.kn0;
+    c.kn1 = (float)P.kn1;
+    c.kn2 = (float)P.kn2;
+    c.edmin = (float)P.e_det_min;
+    c.inv_dEd = (float)(1.0 / P.dEd);
+    c.dEd = (float)P.dEd;
+    c.dEs = (float)P.dEs;
+    c.qmin_t = (float)P.q_min;
+    c.inv_dqt = P.dq_tab > 0 ? (float)(1.0 / P.dq_tab) : 0.f;
+    const double NWT = (double)P.nwt;
+    c.qpar_b = (float)P.dq0;
+    c.qpar_a = (float)((P.q_hi - P.q_lo - P.dq0 * NWT) / (NWT * NWT));
+    return c;
+}
+
 void build_host_tables(const xrdt_problem *p, const DevProblem &P, const float *spec_h, HostTables *t)
 {
     const int W = 2 * p->dnrg + 1;

@@ -95,7 +95,7 @@ struct FwdArgs {
     const int2 *pairs;
     int n_pairs;
     int nv, E, e_pass, sl;
-    float qpar_a, qpar_b;   // coarse grid inversion: edge(n) = q_lo + b n + a n^2
+    F32Consts c;
 };
 
 template <bool WITH_N, bool WITH_A>
@@ -103,7 +103,9 @@ __global__ void __launch_bounds__(kThreads, 3)
 k_fwd(const FwdArgs args)
 {
     extern __shared__ __align__(16) unsigned char sm[];
+    __shared__ PairRec pair;   // the block's (source, pixel) constants
     const DevProblem &P = args.P;
+    const F32Consts &c = args.c;
     const int E = args.E;
     const int W = 2 * P.dnrg + 1;
     const int SL = args.sl;
@@ -177,19 +179,16 @@ k_fwd(const FwdArgs args)
     for (int i = tid; i < P.nq * P.na; i += kThreads) S2[i] = (float)args.s2u8[i];
 
     // ---- per-(source, pixel) geometry, integrate_diffraction.cu:81-128 ----
-    const SrcGeom g = args.sg[src];
-    double Rdet_x, Rdet_y;
-    PairGeom G;
-    pair_geom(P, g, det, &G, &Rdet_x, &Rdet_y);
-    const float Rdxf = (float)Rdet_x, Rdyf = (float)Rdet_y;
-    const float rsqrt2pi = (float)P.rsqrt2pi;
-    const float DQf = (float)P.DQ, inv_DQ = (float)(1.0 / P.DQ);
-    const float dqf_hi = (float)P.dq_fine, dqf_lo = (float)(P.dq_fine - (double)dqf_hi);
-    const float inv_dqf = (float)(1.0 / P.dq_fine), qlo_f = (float)P.q_lo;
-    const float kn0 = (float)P.kn0, kn1 = (float)P.kn1, kn2 = (float)P.kn2;
-    const float edmin = (float)P.e_det_min, inv_dEd = (float)(1.0 / P.dEd), dEdf = (float)P.dEd;
-    const float dEsf = (float)P.dEs;
-    const float qmin_t = (float)P.q_min, inv_dqt = (float)(1.0 / P.dq_tab);
+    if (tid == 0) pair_geom(P, args.sg[src], det, &pair.G, &pair.Rdx, &pair.Rdy);
+    const PairGeom &G = pair.G;
+    const float rsqrt2pi = c.rsqrt2pi;
+    const float DQf = c.DQ;
+    const float dqf_hi = c.dqf_hi, dqf_lo = c.dqf_lo;
+    const float inv_dqf = c.inv_dqf, qlo_f = c.q_lo;
+    const float kn0 = c.kn0, kn1 = c.kn1, kn2 = c.kn2;
+    const float edmin = c.edmin, inv_dEd = c.inv_dEd, dEdf = c.dEd;
+    const float dEsf = c.dEs;
+    const float qmin_t = c.qmin_t, inv_dqt = c.inv_dqt;
     const int lo_e = P.e_lo;
     __syncthreads();
 
@@ -208,16 +207,16 @@ k_fwd(const FwdArgs args)
             // ---- lane = voxel: scattering geometry (integrate_diffraction.cu:192-255) ----
             const int v = min(chunk * 32 + lane, nv - 1);
             const int xy = args.vox_xy[v];
-            const float vx = ((float)(xy & 0xffff) + 0.5f) * (float)P.vox;
-            const float vy = ((float)(xy >> 16) + 0.5f) * (float)P.vox;
+            const float vx = ((float)(xy & 0xffff) + 0.5f) * c.vox;
+            const float vy = ((float)(xy >> 16) + 0.5f) * c.vox;
             const VoxGeom vg = vox_geom(G, vx, vy);
             const int mv = args.vox_mat[v];
             const int nav = args.vox_na[v];
             const float a2v = args.vox_a2[v];
             const float2 Asv = args.atten_src[(int64_t)src * nv + v];
             WalkSetup ws;
-            if (!walk_setup_f32(P, Rdxf, Rdyf, vx, vy, DQf, inv_DQ, &ws))
-                walk_setup_f64(P, Rdet_x, Rdet_y, (double)vx, (double)vy, &ws);
+            if (!walk_setup_f32(P, c, G.Rdx.hi, G.Rdy.hi, vx, vy, &ws))
+                walk_setup_f64(P, pair.Rdx, pair.Rdy, (double)vx, (double)vy, &ws);
 
             const int nin = min(32, nv - chunk * 32);
             for (int i = 0; i < nin; i++) {
@@ -302,7 +301,7 @@ k_fwd(const FwdArgs args)
                     }
                     if (WITH_A) {
                         int klo, khi;
-                        coarse_window(w_hi, half, qlo_f, args.qpar_a, args.qpar_b, P.nwt, &klo, &khi);
+                        coarse_window(w_hi, half, qlo_f, c.qpar_a, c.qpar_b, P.nwt, &klo, &khi);
                         float *tar = TA + ((size_t)(el - pe0) * P.n_mat + m) * P.nwt;
                         nexp += (unsigned)max(0, khi - klo + 1);
                         for (int k = klo; k <= khi; k++) {
@@ -511,9 +510,7 @@ cudaError_t launch_fast_forward(const DevProblem &P, const SrcGeom *d_src, const
     a.nv = nv;
     a.E = P.e_hi - P.e_lo + 1;
     a.sl = T.sl;
-    const double NWT = (double)P.nwt;
-    a.qpar_b = (float)P.dq0;
-    a.qpar_a = (float)((P.q_hi - P.q_lo - P.dq0 * NWT) / (NWT * NWT));
+    a.c = make_f32_consts(P);
     const bool with_n = (N != nullptr);
     const bool with_a = (A != nullptr);
     // energies per pass: all of them unless the model-matrix accumulator
@@ -524,7 +521,7 @@ cudaError_t launch_fast_forward(const DevProblem &P, const SrcGeom *d_src, const
     }
     a.e_pass = e_pass;
     const size_t smem = fwd_layout(P, a.E, a.sl, e_pass, with_n, with_a).total;
-    if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
+    if (smem + sizeof(PairRec) > 227 * 1024) return cudaErrorInvalidConfiguration;   // dynamic + static
     if (launches) (*launches)++;
     if (nv == 0) {
         // empty phantom: the reference writes zeros (integrate_diffraction.cu:364-409)

@@ -47,7 +47,7 @@ struct VoxArgs {
     const float4 *cells;
     const float2 *atten_src;  // [n_src][nv]
     int nv, E;
-    float qpar_a, qpar_b;
+    F32Consts c;
 };
 
 // Per-(voxel, energy) factors shared by the forward and the adjoint:
@@ -130,7 +130,9 @@ k_vox_fwd(const VoxArgs a, const float *__restrict__ xd, float *__restrict__ y, 
           const float *__restrict__ cbg, float *__restrict__ what)
 {
     extern __shared__ __align__(16) unsigned char sm[];
+    __shared__ PairRec pair;
     const DevProblem &P = a.P;
+    const F32Consts &c = a.c;
     const int E = a.E, K = P.nwt, W = 2 * P.dnrg + 1;
     const FwdLayout L = vox_fwd_layout(P, E);
     double *TN = (double *)(sm + L.tn);
@@ -154,11 +156,12 @@ k_vox_fwd(const VoxArgs a, const float *__restrict__ xd, float *__restrict__ y, 
     for (int i = tid; i < P.nrg_det; i += kFwdThreads) winlo[i] = a.win_lo[i];
     for (int i = tid; i < K; i += kFwdThreads) cq[i] = a.coarse_q[i];
 
-    const PairRec pr = a.pairs[pidx];
-    const float Rdxf = (float)pr.Rdx, Rdyf = (float)pr.Rdy;
-    const float rsqrt2pi = (float)P.rsqrt2pi;
-    const float DQf = (float)P.DQ, inv_DQ = (float)(1.0 / P.DQ);
-    const float qlo_f = (float)P.q_lo;
+    if (tid < (int)(sizeof(PairRec) / 4))
+        reinterpret_cast<int *>(&pair)[tid] = reinterpret_cast<const int *>(a.pairs + pidx)[tid];
+    const PairRec &pr = pair;
+    const float rsqrt2pi = c.rsqrt2pi;
+    const float DQf = c.DQ;
+    const float qlo_f = c.q_lo;
     __syncthreads();
 
     float2 *TNw = TNs + wid * E;
@@ -167,12 +170,12 @@ k_vox_fwd(const VoxArgs a, const float *__restrict__ xd, float *__restrict__ y, 
     for (int chunk = wid; chunk < nchunks; chunk += kFwdWarps) {
         const int v = min(chunk * 32 + lane, nv - 1);
         const int xy = a.vox_xy[v];
-        const float vx = ((float)(xy & 0xffff) + 0.5f) * (float)P.vox;
-        const float vy = ((float)(xy >> 16) + 0.5f) * (float)P.vox;
+        const float vx = ((float)(xy & 0xffff) + 0.5f) * c.vox;
+        const float vy = ((float)(xy >> 16) + 0.5f) * c.vox;
         const VoxGeom vg = vox_geom(pr.G, vx, vy);
         const float2 Asv = a.atten_src[(int64_t)src * nv + v];
         WalkSetup ws;
-        if (!walk_setup_f32(P, Rdxf, Rdyf, vx, vy, DQf, inv_DQ, &ws))
+        if (!walk_setup_f32(P, c, pr.G.Rdx.hi, pr.G.Rdy.hi, vx, vy, &ws))
             walk_setup_f64(P, pr.Rdx, pr.Rdy, (double)vx, (double)vy, &ws);
 
         const int nin = min(32, nv - chunk * 32);
@@ -199,7 +202,7 @@ k_vox_fwd(const VoxArgs a, const float *__restrict__ xd, float *__restrict__ y, 
                 const EnergyTerm t = energy_term(en, E, el, Ad.x, Ad.y, Asx, Asy, sh, sl, s2f, sg_s2, Wg, rsqrt2pi);
                 if (t.pref == 0.f) continue;   // attenuation underflow: no contribution
                 int klo, khi;
-                coarse_window(t.w_hi, t.half, qlo_f, a.qpar_a, a.qpar_b, K, &klo, &khi);
+                coarse_window(t.w_hi, t.half, qlo_f, c.qpar_a, c.qpar_b, K, &klo, &khi);
                 float acc = 0.f;
                 for (int k = klo; k <= khi; k++) {
                     const float4 c = cq[k];
@@ -249,6 +252,7 @@ k_vox_adj(const VoxArgs a, const float *__restrict__ what, int pairs_per_group, 
 {
     extern __shared__ __align__(16) unsigned char sm[];
     const DevProblem &P = a.P;
+    const F32Consts &c = a.c;
     const int E = a.E, K = P.nwt;
     const int nwarps = blockDim.x >> 5;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -256,8 +260,10 @@ k_vox_adj(const VoxArgs a, const float *__restrict__ what, int pairs_per_group, 
     float4 *cq = (float4 *)(sm + al16(sizeof(float) * 6 * E));          // [K]
     float4 *rows = cq + K;                                              // [warps][E]
     float2 *gacc = (float2 *)(rows + (size_t)nwarps * E);               // [warps][32][K]
+    PairRec *prs = (PairRec *)(gacc + (size_t)nwarps * 32 * K);         // [warps]
     float4 *rw = rows + (size_t)wid * E;
     float2 *gw = gacc + (size_t)wid * 32 * K;
+    PairRec &pr = prs[wid];
 
     stage_energy_rows(a, en, tid, blockDim.x);
     for (int i = tid; i < K; i += blockDim.x) cq[i] = a.coarse_q[i];
@@ -270,22 +276,25 @@ k_vox_adj(const VoxArgs a, const float *__restrict__ what, int pairs_per_group, 
     const int64_t npairs = (int64_t)P.n_src * P.n_det;
     const int64_t p0 = (int64_t)blockIdx.y * pairs_per_group;
     const int64_t p1 = min(npairs, p0 + pairs_per_group);
-    const float rsqrt2pi = (float)P.rsqrt2pi;
-    const float DQf = (float)P.DQ, inv_DQ = (float)(1.0 / P.DQ);
-    const float q_lo = (float)P.q_lo, q_hi = (float)P.q_hi;
+    const float rsqrt2pi = c.rsqrt2pi;
+    const float DQf = c.DQ;
+    const float q_lo = c.q_lo, q_hi = c.q_hi;
     const int nin = min(32, nv - chunk * 32);
     const int v = chunk * 32 + min(lane, nin - 1);
     const int xy = a.vox_xy[v];
-    const float vx = ((float)(xy & 0xffff) + 0.5f) * (float)P.vox;
-    const float vy = ((float)(xy >> 16) + 0.5f) * (float)P.vox;
+    const float vx = ((float)(xy & 0xffff) + 0.5f) * c.vox;
+    const float vy = ((float)(xy >> 16) + 0.5f) * c.vox;
 
     for (int64_t p = p0; p < p1; p++) {
-        const PairRec pr = a.pairs[p];
+        __syncwarp();   // the previous pair's constants are no longer read
+        if (lane < (int)(sizeof(PairRec) / 4))
+            reinterpret_cast<int *>(&pr)[lane] = reinterpret_cast<const int *>(a.pairs + p)[lane];
+        __syncwarp();
         const int src = (int)(p % P.n_src);
         const VoxGeom vg = vox_geom(pr.G, vx, vy);
         const float2 Asv = a.atten_src[(int64_t)src * nv + v];
         WalkSetup ws;
-        if (!walk_setup_f32(P, (float)pr.Rdx, (float)pr.Rdy, vx, vy, DQf, inv_DQ, &ws))
+        if (!walk_setup_f32(P, c, pr.G.Rdx.hi, pr.G.Rdy.hi, vx, vy, &ws))
             walk_setup_f64(P, pr.Rdx, pr.Rdy, (double)vx, (double)vy, &ws);
         const float *wp = what + p * E;
         for (int i = 0; i < nin; i++) {
@@ -450,9 +459,7 @@ VoxArgs make_args(const VoxOp &op)
     a.atten_src = op.atten_src;
     a.nv = op.nv;
     a.E = op.P.e_hi - op.P.e_lo + 1;
-    const double NWT = (double)op.P.nwt;
-    a.qpar_b = (float)op.P.dq0;
-    a.qpar_a = (float)((op.P.q_hi - op.P.q_lo - op.P.dq0 * NWT) / (NWT * NWT));
+    a.c = make_f32_consts(op.P);
     return a;
 }
 
@@ -469,15 +476,26 @@ cudaError_t launch_pair_table(const DevProblem &P, const SrcGeom *sg, PairRec *o
     return cudaGetLastError();
 }
 
+template <class F>
+cudaError_t allow_dynamic_smem(F *kernel, int max_smem)
+{
+    // the limit covers static and dynamic shared memory together
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, kernel);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem - (int)fa.sharedSizeBytes);
+}
+
 cudaError_t vox_set_attributes(int max_smem)
 {
     // the launches stay free of attribute calls, so they can be captured
-    cudaError_t e = cudaFuncSetAttribute(k_vox_fwd<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_vox_fwd<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_vox_adj, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem);
+    cudaError_t e = allow_dynamic_smem(k_vox_fwd<true>, max_smem);
+    if (e == cudaSuccess) e = allow_dynamic_smem(k_vox_fwd<false>, max_smem);
+    if (e == cudaSuccess) e = allow_dynamic_smem(k_vox_adj, max_smem);
     return e;
 }
+
+size_t vox_fwd_static_smem() { return sizeof(PairRec); }
 
 size_t vox_fwd_smem(const DevProblem &P) { return vox_fwd_layout(P, P.e_hi - P.e_lo + 1).total; }
 
@@ -492,7 +510,7 @@ size_t vox_adj_smem(const DevProblem &P, int warps)
 {
     const int E = P.e_hi - P.e_lo + 1, K = P.nwt;
     return al16(sizeof(float) * 6 * E) + sizeof(float4) * K + sizeof(float4) * (size_t)warps * E +
-           sizeof(float2) * (size_t)warps * 32 * K;
+           sizeof(float2) * (size_t)warps * 32 * K + sizeof(PairRec) * warps;
 }
 
 int vox_adj_groups(const VoxOp &op, int sm_count)

@@ -276,7 +276,8 @@ int32_t xrdt_op_create(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectr
         return bail(rc);
     int optin = 0;
     e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
-    if (e == cudaSuccess && ((int64_t)vox_fwd_smem(P) > optin || (int64_t)vox_adj_smem(P, vox_adj_warps(K)) > optin)) {
+    if (e == cudaSuccess && ((int64_t)(vox_fwd_smem(P) + vox_fwd_static_smem()) > optin ||
+                           (int64_t)vox_adj_smem(P, vox_adj_warps(K)) > optin)) {
         fail(ctx, XRDT_ERR_UNSUPPORTED, "the problem's tables exceed the shared memory of one block");
         return bail(XRDT_ERR_UNSUPPORTED);
     }

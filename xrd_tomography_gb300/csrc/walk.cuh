@@ -54,10 +54,10 @@ __device__ inline void walk_setup(const DevProblem &P, double ex, double ey, dou
 // the latter exactly) -- and the caller then decides in FP64 with
 // walk_setup.  Endpoint rounding (|e| ~ 300 voxels -> 1.5e-5) dominates the
 // FP32 error; the guards are several times that.
-__device__ __forceinline__ bool walk_setup_f32(const DevProblem &P, float ex, float ey, float vx, float vy,
-                                               float DQ, float inv_DQ, WalkSetup *w)
+__device__ __forceinline__ bool walk_setup_f32(const DevProblem &P, const F32Consts &C, float ex, float ey,
+                                               float vx, float vy, WalkSetup *w)
 {
-    const float NX = (float)P.nx, NY = (float)P.ny;
+    const float NX = C.nxf, NY = C.nyf, DQ = C.DQ, inv_DQ = C.inv_DQ;
     const float eps = 0.00001f;
     const float G = 2e-4f;
     const float dx = vx - ex, dy = vy - ey;

@@ -30,6 +30,22 @@ struct DevProblem {
     double q_min, q_max, a_min, a_max, dq_tab, da_tab;
 };
 
+// FP32 copies of the problem constants that the FP32 kernels use inside
+// their loops, converted once on the host.  A float kernel argument is read
+// from the constant bank by the instruction that uses it; a conversion of a
+// double argument that the compiler re-derives inside a loop (instead of
+// holding it in a register) runs on the FP64 pipe, which on this GPU issues
+// at 1/64 of the FP32 rate.
+struct F32Consts {
+    float vox, DQ, inv_DQ, nxf, nyf, rsqrt2pi;
+    float dqf_hi, dqf_lo, inv_dqf, q_lo, q_hi;
+    float kn0, kn1, kn2;
+    float edmin, inv_dEd, dEd, dEs;
+    float qmin_t, inv_dqt;
+    float qpar_a, qpar_b;   // coarse bin edges: edge(n) = q_lo + qpar_b n + qpar_a n^2
+};
+F32Consts make_f32_consts(const DevProblem &P);
+
 // Per-source geometry (integrate_diffraction.cu:93-121), host-computed in double.
 struct SrcGeom {
     double sphi, cphi;
@@ -146,6 +162,7 @@ cudaError_t launch_pair_table(const DevProblem &P, const SrcGeom *sg, PairRec *o
                               int64_t *launches);
 // Opts the operator kernels in to max_smem bytes of dynamic shared memory.
 cudaError_t vox_set_attributes(int max_smem);
+size_t vox_fwd_static_smem();
 size_t vox_fwd_smem(const DevProblem &P);
 int vox_adj_warps(int K);
 size_t vox_adj_smem(const DevProblem &P, int warps);
