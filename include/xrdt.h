@@ -248,6 +248,18 @@ int32_t xrdt_op_adjoint(xrdt_op *op, const float *w, float *g, uint32_t flags);
  * graph launch of three kernels: forward with the ratios, adjoint, update. */
 int32_t xrdt_op_mlem(xrdt_op *op, const float *y, const float *c, float *x,
                      int32_t iters, uint32_t flags);
+/* The same model for a host list of rays, computed by the FP64 kernel at the
+ * reference's launch shape (one block per ray, NWT threads, every voxel and
+ * both line integrals recomputed per block, as integrate_diffraction.cu:33-409
+ * is launched by Forward_XRD.cu:244-259): the plain FP64 GPU path the fast
+ * operator is measured against.  flags must be XRDT_OP_PLAIN_FP64; NWT must
+ * be a multiple of 32, at most 1024.  forward: y[i] = (Av x)[rays[i]];
+ * adjoint: g = sum_i w[i] Av[rays[i], :, :] (w and y have n_rays entries). */
+#define XRDT_OP_PLAIN_FP64 0x1u
+int32_t xrdt_op_forward_rays(xrdt_op *op, const float *x, const int64_t *rays,
+                             int64_t n_rays, float *y, uint32_t flags);
+int32_t xrdt_op_adjoint_rays(xrdt_op *op, const float *w, const int64_t *rays,
+                             int64_t n_rays, float *g, uint32_t flags);
 
 /* The same MLEM for callers that cannot allocate device memory (a host
  * framework that owns the device pool, a real-time loop that must not risk

@@ -6,7 +6,7 @@ import pytest
 
 import xrd_tomography_gb300 as xt
 from xrd_tomography_gb300 import synth
-from tests.tolerances import FAST_RTOL, max_rel_err
+from tests.tolerances import FAST_RTOL, PLAIN_RTOL, max_rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -206,6 +206,29 @@ def test_full_size_mlem_graph_equals_composed_calls(ctx, torch_cuda):
         return float((y.double() * torch.log(m) - m).sum())
     assert loglik(x) > loglik(x0)
     op.close()
+
+
+def test_plain_fp64_rays_match_oracle(ctx, oracle_lib):
+    """The FP64 kernel at the reference's launch shape on ray lists: forward
+    rows and the adjoint of a weighted ray set against the oracle, and the
+    fast operator against it on the same rays."""
+    for inp in (synth.make_inputs(synth.tiny_problem(), 12), synth.sub_phantom_inputs()):
+        p = inp.problem
+        op = make_op(inp, ctx)
+        rng = np.random.default_rng(8)
+        rays = np.sort(rng.choice(p.rays, 24, replace=False))
+        x = rand_x(inp, 9)
+        w = rng.uniform(0.5, 1.5, rays.size).astype(np.float32)
+        y_ref, g_ref = oracle_lib.vox_rays(inp, rays, x=x, w=w)
+        y = op.forward_rays_fp64(x, rays)
+        g = op.adjoint_rays_fp64(w, rays)
+        assert max_rel_err(y, y_ref) < PLAIN_RTOL
+        assert max_rel_err(g, g_ref.reshape(-1)) < PLAIN_RTOL
+        assert max_rel_err(op.forward(x)[rays], y) < FAST_RTOL
+        # the ray-list entry points run only the FP64 kernel
+        rc = xt.api.lib().xrdt_op_forward_rays(op.h, x.ctypes.data, rays.ctypes.data, rays.size, y.ctypes.data, 0)
+        assert rc == 7
+        op.close()
 
 
 def test_operator_errors(ctx):

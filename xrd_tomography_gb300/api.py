@@ -14,6 +14,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import weakref
 
 import numpy as np
 
@@ -24,6 +25,7 @@ LIB_PATH = os.path.join(HERE, "libxrdt.so")
 
 FWD_PLAIN_FP64 = 0x1
 FWD_NO_SYNC = 0x2
+OP_PLAIN_FP64 = 0x1
 (KERNEL_PREP_MAP, KERNEL_PREP_VOXELS, KERNEL_SRC_ATTEN, KERNEL_FORWARD, KERNEL_PLAIN, KERNEL_GATHER,
  KERNEL_MLEM, KERNEL_VOX_FORWARD, KERNEL_VOX_ADJOINT, KERNEL_VOX_UPDATE) = range(10)
 
@@ -58,6 +60,8 @@ SIGNATURES = {
     "xrdt_op_forward": (ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_uint32]),
     "xrdt_op_adjoint": (ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_uint32]),
     "xrdt_op_mlem": (ctypes.c_int32, [_vp, _vp, _vp, _vp, ctypes.c_int32, ctypes.c_uint32]),
+    "xrdt_op_forward_rays": (ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_int64, _vp, ctypes.c_uint32]),
+    "xrdt_op_adjoint_rays": (ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_int64, _vp, ctypes.c_uint32]),
     "xrdt_forward_rays": (ctypes.c_int32, [_vp, _P, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_float,
                                            ctypes.c_float, ctypes.c_float, ctypes.c_float, _vp, ctypes.c_int64,
                                            _vp, _vp, _vp, ctypes.c_uint32]),
@@ -116,9 +120,12 @@ class Context:
         h = _vp()
         _check(lib().xrdt_ctx_create(ctypes.byref(h), device, _vp(stream) if stream else None))
         self.h = h
+        self._operators = weakref.WeakSet()   # destroyed before the context
 
     def close(self):
         if self.h:
+            for op in list(self._operators):
+                op.close()
             lib().xrdt_ctx_destroy(self.h)
             self.h = None
 
@@ -276,6 +283,7 @@ class Operator:
         _check(lib().xrdt_op_create(self.ctx.h, ctypes.byref(p), *[k[0] for k in keep], ctypes.byref(h)),
                self.ctx.h)
         self.h = h
+        self.ctx._operators.add(self)
 
     @property
     def voxels(self) -> int:
@@ -286,9 +294,10 @@ class Operator:
         return self.p.nx * self.p.ny * self.p.nwt
 
     def close(self):
-        if getattr(self, "h", None):
+        # an operator must not outlive its context (xrdt_op_destroy reads it)
+        if getattr(self, "h", None) and self.ctx.h:
             lib().xrdt_op_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):  # pragma: no cover - interpreter shutdown order
         try:
@@ -313,6 +322,24 @@ class Operator:
         pg, kg = _ptr(g, np.float32)
         _check(lib().xrdt_op_adjoint(self.h, pw, pg, 0), self.ctx.h)
         return kg
+
+    def forward_rays_fp64(self, x, rays):
+        """(Av x)[rays] by the FP64 kernel at the reference's launch shape."""
+        rays = np.ascontiguousarray(rays, np.int64)
+        px, kx = _ptr(x, np.float32)
+        y = np.empty(rays.size, np.float32)
+        _check(lib().xrdt_op_forward_rays(self.h, px, rays.ctypes.data, rays.size, y.ctypes.data, OP_PLAIN_FP64),
+               self.ctx.h)
+        return y
+
+    def adjoint_rays_fp64(self, w, rays):
+        """sum_i w[i] Av[rays[i]] by the FP64 kernel at the reference's launch shape."""
+        rays = np.ascontiguousarray(rays, np.int64)
+        pw, kw = _ptr(w, np.float32)
+        g = np.empty(self.unknowns, np.float32)
+        _check(lib().xrdt_op_adjoint_rays(self.h, pw, rays.ctypes.data, rays.size, g.ctypes.data, OP_PLAIN_FP64),
+               self.ctx.h)
+        return g
 
     def mlem(self, y, c, x0, iters: int):
         """iters MLEM updates from x0 (main.m:162-176 with per-voxel unknowns).

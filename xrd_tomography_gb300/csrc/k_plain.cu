@@ -219,6 +219,96 @@ k_plain_forward(DevProblem P, int same_grid, const SrcGeom *__restrict__ sg,
     }
 }
 
+// The per-voxel model of one ray at the same launch shape, in FP64: thread
+// k = coarse bin, every voxel and both line integrals recomputed per block.
+// Forward (x != NULL): y[out] = sum_{v,k} Av[ray,v,k] x[v,k].  Adjoint
+// (w != NULL): g[v,k] += w[out] Av[ray,v,k], added in FP64 with atomics into
+// the full-grid layout (nx + ny*NX)*NWT + k.
+__global__ void __launch_bounds__(1024)
+k_plain_vox(DevProblem P, int same_grid, const SrcGeom *__restrict__ sg, const float *__restrict__ spectrum,
+            const int32_t *__restrict__ seg, const float *__restrict__ a1, const float *__restrict__ a2,
+            const double *__restrict__ coarse_q, const int64_t *__restrict__ rays, const float *__restrict__ x,
+            float *__restrict__ y, const float *__restrict__ w, double *__restrict__ g)
+{
+    extern __shared__ double smem[];
+    const int NWT = P.nwt;
+    const int nwarps = (int)(blockDim.x >> 5);
+    double *red = smem;                       // [2*nwarps]
+    double *spec = red + 2 * nwarps;          // [2*dnrg+1]
+    const int64_t r = rays[blockIdx.x];
+    const int src = (int)(r % P.n_src);
+    const int det = (int)((r / P.n_src) % P.n_det);
+    const int nrg = (int)(r / ((int64_t)P.n_src * P.n_det));
+    const int k = threadIdx.x;
+    const double qnow = coarse_q[2 * k], dqnow = coarse_q[2 * k + 1];
+    int lo, hi;
+    src_nrg_range(P, same_grid, nrg, &lo, &hi);
+    for (int i = k; i <= 2 * P.dnrg; i += blockDim.x) spec[i] = (double)spectrum[(lo + i) + (int64_t)nrg * P.nrg_src];
+    __syncthreads();
+    const double wr = w ? (double)w[blockIdx.x] : 0.0;
+
+    const SrcGeom gs = sg[src];
+    double Rdet_x, Rdet_y, Rdet_z;
+    det_position(P, gs.sphi, gs.cphi, det, &Rdet_x, &Rdet_y, &Rdet_z);
+    const double ndet_x = gs.sphi, ndet_y = -gs.cphi;
+    const double nsrc_x = -gs.sphi * P.sta, nsrc_y = gs.cphi * P.sta, nsrc_z = -P.cta;
+    const double nsrc_xy = sqrt(nsrc_x * nsrc_x + nsrc_y * nsrc_y);
+    double acc = 0.0;
+    for (int nx = 0; nx < P.nx; nx++) {
+        for (int ny = 0; ny < P.ny; ny++) {
+            if (seg[nx + (int64_t)ny * P.nx] <= 0) continue;
+            const double Rvox_x = ((double)nx + 0.5) * P.vox, Rvox_y = ((double)ny + 0.5) * P.vox;
+            const double ax = Rvox_x - gs.Rsrc_x, ay = Rvox_y - gs.Rsrc_y;
+            const double proj = ax * nsrc_x + ay * nsrc_y;
+            const double az = -proj / nsrc_xy * P.tan_half;
+            const double Hvox = proj / nsrc_xy * P.tan_full;
+            const double bx = Rdet_x - Rvox_x, by = Rdet_y - Rvox_y, bz = Rdet_z - az;
+            const double ab = ax * bx + ay * by + az * bz;
+            const double anorm2 = ax * ax + ay * ay + az * az;
+            const double bnorm2 = bx * bx + by * by + bz * bz;
+            const double costheta = ab * (1.0 / sqrt(anorm2)) * (1.0 / sqrt(bnorm2));
+            const double sth = sqrt(fabs(1.0 - costheta) / 2.0);
+            const double Sx = bx - ab * ax / anorm2, Sy = by - ab * ay / anorm2, Sz = bz - ab * az / anorm2;
+            const double Dx = -ax + ab * bx / bnorm2, Dy = -ay + ab * by / bnorm2, Dz = -az + ab * bz / bnorm2;
+            const double Vx = -(Sx + Dx), Vy = -(Sy + Dy), Vz = -(Sz + Dz);
+            const double Dndet = Dx * ndet_x + Dy * ndet_y;
+            const double Snsrc = Sx * nsrc_x + Sy * nsrc_y + Sz * nsrc_z;
+            const double dD2 = (Dx * Dx + Dy * Dy + Dz * Dz - Dndet * Dndet) * P.geomAdet / 12.0;
+            const double vV2 = (P.vox * P.vox * (Vx * Vx + Vy * Vy) + Hvox * Hvox * Vz * Vz) / 12.0;
+            const double sS2 = (Sx * Sx + Sy * Sy + Sz * Sz - Snsrc * Snsrc) * P.focal * P.focal / 12.0;
+            const double Rdotn = -gs.sphi * ax + gs.cphi * ay;
+            const double cospsi = Rdotn * (1.0 / sqrt(ax * ax + ay * ay));
+            const double gsv = cospsi * (1.0 / sqrt(anorm2)) * P.tan_full;
+            const double gvd = -(ndet_x * bx + ndet_y * by) * (1.0 / sqrt(bnorm2 * bnorm2 * bnorm2));
+            const double Wg = gsv * gvd * (1.0 + costheta * costheta) / 2.0;
+            double Ad_x, Ad_y, As_x, As_y;  // integrate_diffraction.cu:259-260, labels as written
+            attenuate(P, a1, a2, Rdet_x, Rdet_y, Rvox_x, Rvox_y, red, nwarps, &Ad_x, &Ad_y);
+            attenuate(P, a1, a2, gs.Rsrc_x, gs.Rsrc_y, Rvox_x, Rvox_y, red, nwarps, &As_x, &As_y);
+            double t = 0.0;   // sum over the window of this bin's term
+            for (int e = lo; e <= hi; e++) {
+                const double Esrc1 = P.e_src_min + (double)e * P.dEs, Esrc2 = P.e_src_min + (double)(e + 1) * P.dEs;
+                const double Esrc = 0.5 * (Esrc1 + Esrc2);
+                const double ein = Esrc / P.mec2;
+                const double wvt = 2.0 * Esrc / P.hbarc * sth;
+                const double s2 = (2.0 * sth / P.hbarc) * (2.0 * sth / P.hbarc) * P.dEs * P.dEs / 12.0 +
+                                  (Esrc / P.hbarc) * (Esrc / P.hbarc) * (sS2 + vV2 + dD2) /
+                                      (2.0 * sth) / (2.0 * sth) / anorm2 / bnorm2;
+                const double f1 = ein * ein * ein, f2 = P.kn0 + P.kn1 * ein + P.kn2 * ein * ein;
+                const double PP = exp(-(Ad_x / f1 + Ad_y / f2)) * exp(-(As_x / f1 + As_y / f2));
+                t += spec[e - lo] * PP * exp(-(wvt - qnow) * (wvt - qnow) / (2.0 * s2)) * P.rsqrt2pi / sqrt(s2) * dqnow;
+            }
+            const int64_t idx = ((int64_t)nx + (int64_t)ny * P.nx) * NWT + k;
+            if (x) acc += Wg * t * (double)x[idx];
+            if (g) atomicAdd(g + idx, wr * Wg * t);
+        }
+    }
+    if (y) {
+        double dummy = 0.0;
+        block_sum2(acc, dummy, red, nwarps);
+        if (k == 0) y[blockIdx.x] = (float)acc;
+    }
+}
+
 } // namespace
 
 cudaError_t launch_plain_forward(const DevProblem &P, const SrcGeom *d_src,
@@ -245,4 +335,20 @@ cudaError_t launch_plain_forward(const DevProblem &P, const SrcGeom *d_src,
     return cudaGetLastError();
 }
 
+cudaError_t launch_plain_vox(const DevProblem &P, const SrcGeom *d_src, const float *spectrum, const int32_t *seg,
+                             const float *a1, const float *a2, const double *d_coarse_q, const int64_t *d_rays,
+                             int64_t n_rays, const float *x, float *y, const float *w, double *g, cudaStream_t s,
+                             int64_t *launches)
+{
+    if (n_rays == 0) return cudaSuccess;
+    const int same_grid = (P.nrg_src == P.nrg_det && P.e_src_min == P.e_det_min && P.dEs == P.dEd);
+    const int nwarps = P.nwt / 32;
+    const size_t smem = sizeof(double) * (2 * (size_t)nwarps + 2 * P.dnrg + 1);
+    k_plain_vox<<<(unsigned)n_rays, P.nwt, smem, s>>>(P, same_grid, d_src, spectrum, seg, a1, a2, d_coarse_q, d_rays,
+                                                     x, y, w, g);
+    if (launches) (*launches)++;
+    return cudaGetLastError();
+}
+
 } // namespace xrdt
+

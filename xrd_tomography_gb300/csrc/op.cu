@@ -33,6 +33,13 @@ struct xrdt_op {
     double *sens = nullptr;               // [nv][NWT]
     float *xfull = nullptr;               // staging of the full-grid layout
     float *ray_a = nullptr, *ray_b = nullptr;   // staging of ray vectors
+    // inputs of the FP64 kernel at the reference launch shape
+    const SrcGeom *src = nullptr;
+    float *spectrum = nullptr;
+    double *coarse_qd = nullptr;          // [nwt] (centre, width) in double
+    double *gd = nullptr;                 // [NX*NY*NWT] FP64 adjoint accumulator
+    int64_t *rays_d = nullptr;            // staged ray list
+    int64_t rays_cap = 0;
     // MLEM iteration as a graph, keyed by the ray vectors it reads
     cudaGraphExec_t mlem_exec = nullptr;
     const void *mlem_key[2] = {};
@@ -246,6 +253,26 @@ int32_t xrdt_op_create(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectr
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_wn, ht.win_n.data(), sizeof(int) * ht.win_n.size(), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_cq, ht.coarse_q.data(), sizeof(float4) * ht.coarse_q.size(), cudaMemcpyHostToDevice, st);
 
+    op->src = d_src;
+    {
+        std::vector<double> cqd(2 * (size_t)K);
+        for (int k = 0; k < K; k++) {
+            const double NWT = (double)K;
+            const double e1 = p->q_lo + (double)k * p->dq0 +
+                              (p->q_hi - p->q_lo - p->dq0 * NWT) * (double)((int64_t)k * k) / (NWT * NWT);
+            const double e2 = p->q_lo + (double)(k + 1) * p->dq0 +
+                              (p->q_hi - p->q_lo - p->dq0 * NWT) * (double)((int64_t)(k + 1) * (k + 1)) / (NWT * NWT);
+            cqd[2 * k] = 0.5 * (e1 + e2);
+            cqd[2 * k + 1] = e2 - e1;
+        }
+        if ((rc = op_alloc_t(op, cqd.size(), &op->coarse_qd)) || (rc = op_alloc_t(op, hspec.size(), &op->spectrum)))
+            return bail(rc);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(op->coarse_qd, cqd.data(), sizeof(double) * cqd.size(), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(op->spectrum, hspec.data(), sizeof(float) * hspec.size(), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);   // cqd leaves scope
+    }
     op->v.P = P;
     op->v.nv = nv;
     op->v.pairs = d_pairs;
@@ -366,6 +393,102 @@ int32_t xrdt_op_adjoint(xrdt_op *op, const float *w, float *g, uint32_t flags)
     CK(cudaStreamSynchronize(st));
     return XRDT_OK;
 }
+
+} // extern "C"
+
+namespace {
+
+// Stages a host ray list, checking each index.
+int stage_rays(xrdt_op *op, const int64_t *rays, int64_t n_rays)
+{
+    xrdt_ctx *ctx = op->ctx;
+    if (n_rays < 0 || n_rays > 2147483647LL) return fail(ctx, XRDT_ERR_DIMS, "bad ray count");
+    if (n_rays && !rays) return fail(ctx, XRDT_ERR_NULL, "ray list is NULL");
+    if (n_rays && is_device_ptr(rays)) return fail(ctx, XRDT_ERR_UNSUPPORTED, "the ray list must be host memory");
+    for (int64_t i = 0; i < n_rays; i++)
+        if (rays[i] < 0 || rays[i] >= op->rays)
+            return fail(ctx, XRDT_ERR_INPUT, fmt("ray %lld out of range", (long long)rays[i]));
+    if (n_rays > op->rays_cap) {
+        int rc = op_alloc_t(op, (size_t)n_rays, &op->rays_d);
+        if (rc) return rc;
+        op->rays_cap = n_rays;
+    }
+    if (n_rays) CK(cudaMemcpyAsync(op->rays_d, rays, sizeof(int64_t) * n_rays, cudaMemcpyHostToDevice, ctx->stream));
+    return XRDT_OK;
+}
+
+int plain_ok(xrdt_op *op, uint32_t flags)
+{
+    if (flags != XRDT_OP_PLAIN_FP64)
+        return fail(op->ctx, XRDT_ERR_UNSUPPORTED, "ray-list calls run the FP64 kernel: pass XRDT_OP_PLAIN_FP64");
+    if (op->p.nwt % 32 != 0 || op->p.nwt > 1024)
+        return fail(op->ctx, XRDT_ERR_UNSUPPORTED, "the reference launch shape needs NWT a multiple of 32, <= 1024");
+    return XRDT_OK;
+}
+
+__global__ void k_double_to_float(const double *__restrict__ a, float *__restrict__ b, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+
+} // namespace
+
+extern "C" {
+
+int32_t xrdt_op_forward_rays(xrdt_op *op, const float *x, const int64_t *rays, int64_t n_rays, float *y,
+                             uint32_t flags)
+{
+    int rc = begin(op);
+    if (rc) return rc;
+    xrdt_ctx *ctx = op->ctx;
+    if (!x || !y) return fail(ctx, XRDT_ERR_NULL, "x and y are required");
+    if ((rc = plain_ok(op, flags)) || (rc = stage_rays(op, rays, n_rays))) return rc;
+    cudaStream_t st = ctx->stream;
+    const size_t nfull = (size_t)op->p.nx * op->p.ny * op->p.nwt;
+    const float *dx;
+    if ((rc = view_in(op, x, nfull, op->xfull, &dx))) return rc;
+    const bool hostY = !is_device_ptr(y);
+    float *dy = hostY ? op->ray_a : y;   // n_rays <= rays
+    {
+        ProfScope ps(ctx, XRDT_KERNEL_PLAIN);
+        CK(launch_plain_vox(op->v.P, op->src, op->spectrum, op->seg, op->a1, op->a2, op->coarse_qd, op->rays_d,
+                            n_rays, dx, dy, nullptr, nullptr, st, &ctx->launches));
+    }
+    if (hostY && n_rays) CK(cudaMemcpyAsync(y, dy, sizeof(float) * n_rays, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return XRDT_OK;
+}
+
+int32_t xrdt_op_adjoint_rays(xrdt_op *op, const float *w, const int64_t *rays, int64_t n_rays, float *g,
+                             uint32_t flags)
+{
+    int rc = begin(op);
+    if (rc) return rc;
+    xrdt_ctx *ctx = op->ctx;
+    if (!w || !g) return fail(ctx, XRDT_ERR_NULL, "w and g are required");
+    if ((rc = plain_ok(op, flags)) || (rc = stage_rays(op, rays, n_rays))) return rc;
+    cudaStream_t st = ctx->stream;
+    const size_t nfull = (size_t)op->p.nx * op->p.ny * op->p.nwt;
+    if (!op->gd && (rc = op_alloc_t(op, nfull, &op->gd))) return rc;
+    const float *dw;
+    if ((rc = view_in(op, w, (size_t)n_rays, op->ray_a, &dw))) return rc;
+    const bool hostG = !is_device_ptr(g);
+    float *dg = hostG ? op->xfull : g;
+    CK(cudaMemsetAsync(op->gd, 0, sizeof(double) * nfull, st));
+    {
+        ProfScope ps(ctx, XRDT_KERNEL_PLAIN);
+        CK(launch_plain_vox(op->v.P, op->src, op->spectrum, op->seg, op->a1, op->a2, op->coarse_qd, op->rays_d,
+                            n_rays, nullptr, nullptr, dw, op->gd, st, &ctx->launches));
+    }
+    k_double_to_float<<<256, 256, 0, st>>>(op->gd, dg, (int64_t)nfull);
+    CK(cudaGetLastError());
+    ctx->launches++;
+    if (hostG) CK(cudaMemcpyAsync(g, dg, sizeof(float) * nfull, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return XRDT_OK;
+}
+
 
 int32_t xrdt_op_mlem(xrdt_op *op, const float *y, const float *c, float *x, int32_t iters, uint32_t flags)
 {

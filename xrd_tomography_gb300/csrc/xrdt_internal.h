@@ -89,6 +89,14 @@ cudaError_t launch_plain_forward(const DevProblem &P, const SrcGeom *d_src,
                                  const double *d_coarse_q, const int64_t *d_rays, int64_t n_rays,
                                  float *N, float *C, float *A, cudaStream_t s, int64_t *launches);
 
+// The per-voxel model at the same launch shape (NWT threads, NWT % 32 == 0):
+// y[i] = Av[rays[i]] x (x != NULL) and g += sum_i w[i] Av[rays[i]] (w != NULL,
+// g in FP64, full-grid layout).
+cudaError_t launch_plain_vox(const DevProblem &P, const SrcGeom *d_src, const float *spectrum, const int32_t *seg,
+                             const float *a1, const float *a2, const double *d_coarse_q, const int64_t *d_rays,
+                             int64_t n_rays, const float *x, float *y, const float *w, double *g, cudaStream_t s,
+                             int64_t *launches);
+
 // k_prep.cu
 struct PrepBuffers {
     float4 *cells;          // [(ny+1)*(nx+1)*2] bilinear cells
