@@ -261,6 +261,32 @@ int32_t xrdt_op_forward_rays(xrdt_op *op, const float *x, const int64_t *rays,
 int32_t xrdt_op_adjoint_rays(xrdt_op *op, const float *w, const int64_t *rays,
                              int64_t n_rays, float *g, uint32_t flags);
 
+/* ---- batches: many operators in one launch per kernel ------------------
+ * A batch runs the forward, the adjoint and MLEM of several operators
+ * (phantoms and scanners of any sizes) together: the forward and the adjoint
+ * are persistent kernels whose blocks take work from one queue that holds
+ * every problem's (source, pixel) pairs or (voxel chunk, pair group) tiles,
+ * so uneven problems fill the GPU together; each MLEM iteration of the whole
+ * batch is one CUDA graph launch.  The adjoint's tile shape (warps per block
+ * and tiles per block slot) is chosen by timing candidates on the batch on
+ * its first MLEM call or on xrdt_batch_tune.  Arrays are per-problem device
+ * pointers in operator order, with each operator's sizes.  A batch uses its
+ * operators' buffers: an operator takes part in one call at a time. */
+typedef struct xrdt_batch xrdt_batch;
+int32_t xrdt_batch_create(xrdt_ctx *ctx, xrdt_op *const *ops, int32_t n,
+                          xrdt_batch **batch);
+int32_t xrdt_batch_destroy(xrdt_batch *batch);
+int32_t xrdt_batch_forward(xrdt_batch *batch, const float *const *x,
+                           float *const *y, uint32_t flags);
+int32_t xrdt_batch_adjoint(xrdt_batch *batch, const float *const *w,
+                           float *const *g, uint32_t flags);
+int32_t xrdt_batch_mlem(xrdt_batch *batch, const float *const *y,
+                        const float *const *c, float *const *x, int32_t iters,
+                        uint32_t flags);
+/* Runs the tile-shape search now (once per batch) and reports the choice. */
+int32_t xrdt_batch_tune(xrdt_batch *batch, int32_t *adj_warps, int64_t *adj_tiles,
+                        int32_t *fwd_grid, int32_t *adj_grid);
+
 /* The same MLEM for callers that cannot allocate device memory (a host
  * framework that owns the device pool, a real-time loop that must not risk
  * an allocation or its implicit synchronisation, an embedder that only hands

@@ -61,6 +61,13 @@ SIGNATURES = {
     "xrdt_op_adjoint": (ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_uint32]),
     "xrdt_op_mlem": (ctypes.c_int32, [_vp, _vp, _vp, _vp, ctypes.c_int32, ctypes.c_uint32]),
     "xrdt_op_forward_rays": (ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_int64, _vp, ctypes.c_uint32]),
+    "xrdt_batch_create": (ctypes.c_int32, [_vp, _vp, ctypes.c_int32, ctypes.POINTER(_vp)]),
+    "xrdt_batch_destroy": (ctypes.c_int32, [_vp]),
+    "xrdt_batch_forward": (ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_uint32]),
+    "xrdt_batch_adjoint": (ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_uint32]),
+    "xrdt_batch_mlem": (ctypes.c_int32, [_vp, _vp, _vp, _vp, ctypes.c_int32, ctypes.c_uint32]),
+    "xrdt_batch_tune": (ctypes.c_int32, [_vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int64),
+                                         ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
     "xrdt_op_adjoint_rays": (ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_int64, _vp, ctypes.c_uint32]),
     "xrdt_forward_rays": (ctypes.c_int32, [_vp, _P, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_float,
                                            ctypes.c_float, ctypes.c_float, ctypes.c_float, _vp, ctypes.c_int64,
@@ -354,6 +361,58 @@ class Operator:
             px = x.ctypes.data
         _check(lib().xrdt_op_mlem(self.h, py, pc, px, iters, 0), self.ctx.h)
         return x
+
+
+class Batch:
+    """xrdt_batch: several Operators run together, one persistent launch per
+    kernel and one CUDA graph per MLEM iteration.  Every array argument is a
+    list of contiguous torch CUDA tensors, one per operator."""
+
+    def __init__(self, ops, ctx: Context | None = None):
+        self.ctx = ctx or ops[0].ctx
+        self.ops = list(ops)
+        arr = (_vp * len(self.ops))(*[op.h for op in self.ops])
+        h = _vp()
+        _check(lib().xrdt_batch_create(self.ctx.h, arr, len(self.ops), ctypes.byref(h)), self.ctx.h)
+        self.h = h
+        self.ctx._operators.add(self)
+
+    def close(self):
+        if getattr(self, "h", None) and self.ctx.h:
+            lib().xrdt_batch_destroy(self.h)
+        self.h = None
+
+    def __del__(self):  # pragma: no cover - interpreter shutdown order
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _ptrs(ts):
+        for t in ts:
+            if not hasattr(t, "data_ptr") or not t.is_cuda or not t.is_contiguous():
+                raise ValueError("batch arrays must be contiguous CUDA tensors")
+        return (_vp * len(ts))(*[t.data_ptr() for t in ts])
+
+    def forward(self, xs, ys):
+        _check(lib().xrdt_batch_forward(self.h, self._ptrs(xs), self._ptrs(ys), 0), self.ctx.h)
+        return ys
+
+    def adjoint(self, ws, gs):
+        _check(lib().xrdt_batch_adjoint(self.h, self._ptrs(ws), self._ptrs(gs), 0), self.ctx.h)
+        return gs
+
+    def mlem(self, ys, cs, xs, iters: int):
+        _check(lib().xrdt_batch_mlem(self.h, self._ptrs(ys), self._ptrs(cs), self._ptrs(xs), iters, 0), self.ctx.h)
+        return xs
+
+    def tune(self):
+        """(adjoint warps per block, adjoint tiles, forward grid, adjoint grid) chosen by the autotuner."""
+        w, t, fg, ag = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int32(), ctypes.c_int32()
+        _check(lib().xrdt_batch_tune(self.h, ctypes.byref(w), ctypes.byref(t), ctypes.byref(fg), ctypes.byref(ag)),
+               self.ctx.h)
+        return w.value, t.value, fg.value, ag.value
 
 
 def Forward_XRD(spectrum, Ifine, segmentation, a1, a2, S2, q_min, q_max, a_min, a_max,

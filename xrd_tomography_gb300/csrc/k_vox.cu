@@ -1,5 +1,5 @@
 // k_vox.cu -- the model with per-voxel coefficients: forward, adjoint and
-// the MLEM update, matrix-free.
+// the MLEM update, matrix-free, for a batch of independent problems.
 //
 // The reference's model matrix has one unknown per (coarse q bin, material):
 // Amatrix[k, m, ray] = sum over the voxels of material m of the coarse-q
@@ -13,19 +13,27 @@
 // detector-side attenuation of every (pair, voxel) is walked again in each
 // call, the source-side one comes from the per-(source, voxel) table.
 //
-//  * forward (k_vox_fwd): one block per (source, pixel) as in k_fwd.cu; lane =
-//    source energy sums the coarse bins within 7.5 sigma of the wavevector
-//    transfer, weighted by x[v, k] dq_k, into compensated per-energy sums; the
-//    banded spectrum weights give the detector bins.  In MLEM mode the block
-//    goes on to form the ratios y / (Av x + c + 1e-20) of main.m:162 for its
-//    detector bins and folds them back through the same spectrum band into
-//    per-energy weights  what[pair, e] = sum_nrg RF[e,nrg] ratio[nrg].
+// Every kernel takes a batch of problems (phantoms and scanners of any
+// size, VoxJob); a single operator is a batch of one.  The two heavy kernels
+// are persistent: a grid sized to the GPU takes work items from an atomic
+// counter -- the (source, pixel) pairs of all problems for the forward, the
+// (voxel chunk, pair group) tiles of all problems for the adjoint -- so that
+// uneven problems share one launch and the tail stays short.
+//
+//  * forward (k_vox_fwd): one item = one (source, pixel) pair, as in
+//    k_fwd.cu; lane = source energy sums the coarse bins within 7.5 sigma of
+//    the wavevector transfer, weighted by x[v, k] dq_k, into compensated
+//    per-energy sums; the banded spectrum weights give the detector bins.  In
+//    MLEM mode the block goes on to form the ratios y / (Av x + c + 1e-20) of
+//    main.m:162 for its detector bins and folds them back through the same
+//    spectrum band into per-energy weights what[pair, e] = sum_nrg RF[e,nrg]
+//    ratio[nrg].
 //  * adjoint (k_vox_adj): voxel-major, so that g stays on chip.  A warp owns
-//    32 voxels and loops over a range of pairs; per (pair, voxel) lane =
+//    32 voxels and loops over a group of pairs; per (pair, voxel) lane =
 //    energy forms what[pair,e] * (the energy's prefactor), then lane = coarse
 //    bin k adds sum_e of those times G(wvt_e - q_k) to the voxel's compensated
-//    sum.  Ranges of pairs run in parallel blocks and are added in FP64 by
-//    k_vox_reduce, which also applies the MLEM update (main.m:163-176).
+//    sum.  The groups' partial sums are added in FP64 by k_vox_reduce, which
+//    also applies the MLEM update (main.m:163-176).
 #include "scatter.cuh"
 
 namespace xrdt {
@@ -35,25 +43,10 @@ namespace {
 constexpr int kFwdThreads = 256;
 constexpr int kFwdWarps = kFwdThreads / 32;
 
-struct VoxArgs {
-    DevProblem P;
-    const PairRec *pairs;     // [n_src * n_det], index src + det * n_src
-    const EnergyRow *energy;  // [nrg_src]
-    const float *rf_win;      // [nrg_det][2*dnrg+1]
-    const int *win_lo;        // [nrg_det]
-    const int *win_n;         // [nrg_src][2]
-    const float4 *coarse_q;   // [nwt] (q_hi, q_lo, dq, 0)
-    const int *vox_xy;
-    const float4 *cells;
-    const float2 *atten_src;  // [n_src][nv]
-    int nv, E;
-    F32Consts c;
-};
-
-// Per-(voxel, energy) factors shared by the forward and the adjoint:
-// the prefactor RF-less term pref = Pin Pout geom Rayleigh / (sigma sqrt(2 pi)),
-// the wavevector transfer as a pair, the Gaussian exponent scale (log2 units)
-// and the window half-width.
+// Per-(voxel, energy) factors shared by the forward and the adjoint: the
+// prefactor pref = Pin Pout geom Rayleigh / (sigma sqrt(2 pi)) without RF,
+// the wavevector transfer as a pair, the Gaussian exponent scale (log2
+// units) and the window half-width.
 struct EnergyTerm {
     float pref, w_hi, w_lo, cexp, half;
 };
@@ -86,17 +79,38 @@ __device__ __forceinline__ EnergyTerm energy_term(const float *en, int E, int el
 }
 
 // Energy rows in shared memory: 1/f1, 1/f2, wfac_hi, wfac_lo, sig_c1, sig_c2.
-__device__ __forceinline__ void stage_energy_rows(const VoxArgs &a, float *en, int tid, int nthreads)
+__device__ __forceinline__ void stage_energy_rows(const VoxJob &J, float *en, int tid, int nthreads)
 {
-    for (int i = tid; i < a.E; i += nthreads) {
-        const EnergyRow r = a.energy[a.P.e_lo + i];
+    for (int i = tid; i < J.E; i += nthreads) {
+        const EnergyRow r = J.op.energy[J.op.P.e_lo + i];
         en[i] = r.inv_f1;
-        en[a.E + i] = r.inv_f2;
-        en[2 * a.E + i] = r.wfac_hi;
-        en[3 * a.E + i] = r.wfac_lo;
-        en[4 * a.E + i] = r.sig_c1;
-        en[5 * a.E + i] = r.sig_c2;
+        en[J.E + i] = r.inv_f2;
+        en[2 * J.E + i] = r.wfac_hi;
+        en[3 * J.E + i] = r.wfac_lo;
+        en[4 * J.E + i] = r.sig_c1;
+        en[5 * J.E + i] = r.sig_c2;
     }
+}
+
+// The problem that work item t belongs to: the last p with off[p] <= t.
+__device__ __forceinline__ int find_job(const int64_t *__restrict__ off, int n, int64_t t)
+{
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(off + mid) <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Copies a job into shared memory with every thread of the block.
+__device__ __forceinline__ void load_job(const VoxJob *__restrict__ jobs, int p, VoxJob *dst)
+{
+    static_assert(sizeof(VoxJob) % 4 == 0, "job size");
+    const int *src = reinterpret_cast<const int *>(jobs + p);
+    int *d = reinterpret_cast<int *>(dst);
+    for (int i = threadIdx.x; i < (int)(sizeof(VoxJob) / 4); i += blockDim.x) d[i] = __ldg(src + i);
 }
 
 struct FwdLayout {
@@ -122,18 +136,13 @@ __host__ __device__ inline FwdLayout vox_fwd_layout(const DevProblem &P, int E)
     return L;
 }
 
-// y = Av x (MLEM = false), or the per-energy weights of the MLEM ratios
-// (MLEM = true).  xd = x * dq_k in the compact voxel order, [nv][nwt].
+// One (source, pixel) pair of job J, by the whole block.
 template <bool MLEM>
-__global__ void __launch_bounds__(kFwdThreads, 3)
-k_vox_fwd(const VoxArgs a, const float *__restrict__ xd, float *__restrict__ y, const float *__restrict__ ymeas,
-          const float *__restrict__ cbg, float *__restrict__ what)
+__device__ __forceinline__ void vox_fwd_pair(const VoxJob &J, int64_t pidx, unsigned char *sm, PairRec &pair)
 {
-    extern __shared__ __align__(16) unsigned char sm[];
-    __shared__ PairRec pair;
-    const DevProblem &P = a.P;
-    const F32Consts &c = a.c;
-    const int E = a.E, K = P.nwt, W = 2 * P.dnrg + 1;
+    const DevProblem &P = J.op.P;
+    const F32Consts &c = J.c;
+    const int E = J.E, K = P.nwt, W = 2 * P.dnrg + 1;
     const FwdLayout L = vox_fwd_layout(P, E);
     double *TN = (double *)(sm + L.tn);
     float2 *TNs = (float2 *)(sm + L.tns);
@@ -145,38 +154,36 @@ k_vox_fwd(const VoxArgs a, const float *__restrict__ xd, float *__restrict__ y, 
     float *ratio = (float *)(sm + L.ratio);
 
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    const int det = blockIdx.x, src = blockIdx.y;
     const int64_t npairs = (int64_t)P.n_src * P.n_det;
-    const int64_t pidx = (int64_t)src + (int64_t)det * P.n_src;
+    const int src = (int)(pidx % P.n_src);
 
-    stage_energy_rows(a, en, tid, kFwdThreads);
+    stage_energy_rows(J, en, tid, kFwdThreads);
     for (int i = tid; i < kFwdWarps * E; i += kFwdThreads) TNs[i] = make_float2(0.f, 0.f);
-    for (int i = tid; i < 2 * E; i += kFwdThreads) wn[i] = a.win_n[2 * P.e_lo + i];
-    for (int i = tid; i < P.nrg_det * W; i += kFwdThreads) rf[i] = a.rf_win[i];
-    for (int i = tid; i < P.nrg_det; i += kFwdThreads) winlo[i] = a.win_lo[i];
-    for (int i = tid; i < K; i += kFwdThreads) cq[i] = a.coarse_q[i];
-
+    for (int i = tid; i < 2 * E; i += kFwdThreads) wn[i] = J.op.win_n[2 * P.e_lo + i];
+    for (int i = tid; i < P.nrg_det * W; i += kFwdThreads) rf[i] = J.op.rf_win[i];
+    for (int i = tid; i < P.nrg_det; i += kFwdThreads) winlo[i] = J.op.win_lo[i];
+    for (int i = tid; i < K; i += kFwdThreads) cq[i] = J.op.coarse_q[i];
     if (tid < (int)(sizeof(PairRec) / 4))
-        reinterpret_cast<int *>(&pair)[tid] = reinterpret_cast<const int *>(a.pairs + pidx)[tid];
-    const PairRec &pr = pair;
+        reinterpret_cast<int *>(&pair)[tid] = reinterpret_cast<const int *>(J.op.pairs + pidx)[tid];
     const float rsqrt2pi = c.rsqrt2pi;
     const float DQf = c.DQ;
     const float qlo_f = c.q_lo;
+    const float *__restrict__ xd = J.xd;
     __syncthreads();
 
     float2 *TNw = TNs + wid * E;
-    const int nv = a.nv;
+    const int nv = J.op.nv;
     const int nchunks = (nv + 31) >> 5;
     for (int chunk = wid; chunk < nchunks; chunk += kFwdWarps) {
         const int v = min(chunk * 32 + lane, nv - 1);
-        const int xy = a.vox_xy[v];
+        const int xy = J.op.vox_xy[v];
         const float vx = ((float)(xy & 0xffff) + 0.5f) * c.vox;
         const float vy = ((float)(xy >> 16) + 0.5f) * c.vox;
-        const VoxGeom vg = vox_geom(pr.G, vx, vy);
-        const float2 Asv = a.atten_src[(int64_t)src * nv + v];
+        const VoxGeom vg = vox_geom(pair.G, vx, vy);
+        const float2 Asv = J.op.atten_src[(int64_t)src * nv + v];
         WalkSetup ws;
-        if (!walk_setup_f32(P, c, pr.G.Rdx.hi, pr.G.Rdy.hi, vx, vy, &ws))
-            walk_setup_f64(P, pr.Rdx, pr.Rdy, (double)vx, (double)vy, &ws);
+        if (!walk_setup_f32(P, c, pair.G.Rdx.hi, pair.G.Rdy.hi, vx, vy, &ws))
+            walk_setup_f64(P, pair.Rdx, pair.Rdy, (double)vx, (double)vy, &ws);
 
         const int nin = min(32, nv - chunk * 32);
         for (int i = 0; i < nin; i++) {
@@ -187,7 +194,7 @@ k_vox_fwd(const VoxArgs a, const float *__restrict__ xd, float *__restrict__ y, 
             wi.Ly = __shfl_sync(0xffffffffu, ws.Ly, i);
             wi.n = __shfl_sync(0xffffffffu, ws.n, i);
             // the detector-side integral feeds Pin (integrate_diffraction.cu:259-260)
-            const float2 Ad = walk_coop(a.cells, P.nx, P.ny, wi, DQf, lane);
+            const float2 Ad = walk_coop(J.op.cells, P.nx, P.ny, wi, DQf, lane);
             const float sh = __shfl_sync(0xffffffffu, vg.s.hi, i);
             const float sl = __shfl_sync(0xffffffffu, vg.s.lo, i);
             const float sg = __shfl_sync(0xffffffffu, vg.sg, i);
@@ -205,8 +212,8 @@ k_vox_fwd(const VoxArgs a, const float *__restrict__ xd, float *__restrict__ y, 
                 coarse_window(t.w_hi, t.half, qlo_f, c.qpar_a, c.qpar_b, K, &klo, &khi);
                 float acc = 0.f;
                 for (int k = klo; k <= khi; k++) {
-                    const float4 c = cq[k];
-                    const float d = (t.w_hi - c.x) + (t.w_lo - c.y);
+                    const float4 q = cq[k];
+                    const float d = (t.w_hi - q.x) + (t.w_lo - q.y);
                     acc = fmaf(ex2_approx(t.cexp * d * d), __ldg(xrow + k), acc);
                 }
                 float2 s = TNw[el];
@@ -227,8 +234,8 @@ k_vox_fwd(const VoxArgs a, const float *__restrict__ xd, float *__restrict__ y, 
         double acc = 0.0;
         for (int j = 0; j < W; j++) acc += (double)rf[n * W + j] * TN[winlo[n] + j - lo_e];
         const int64_t ray = pidx + (int64_t)n * npairs;
-        if (MLEM) ratio[n] = (float)((double)ymeas[ray] / (acc + (double)cbg[ray] + 1e-20));   // main.m:162
-        else y[ray] = (float)acc;
+        if (MLEM) ratio[n] = (float)((double)J.ymeas[ray] / (acc + (double)J.cbg[ray] + 1e-20));   // main.m:162
+        else J.y[ray] = (float)acc;
     }
     if (MLEM) {
         __syncthreads();
@@ -240,127 +247,181 @@ k_vox_fwd(const VoxArgs a, const float *__restrict__ xd, float *__restrict__ y, 
                 const int j = e - winlo[n];
                 if (j >= 0 && j < W) s += (double)rf[n * W + j] * (double)ratio[n];
             }
-            what[pidx * E + el] = (float)s;
+            J.what[pidx * E + el] = (float)s;
         }
     }
 }
 
-// Adjoint: part[group][v][k] = sum over the group's pairs p of
-// sum_e what[p, e] pref(p,v,e) G(wvt - q_k) dq_k.
-__global__ void __launch_bounds__(128)
-k_vox_adj(const VoxArgs a, const float *__restrict__ what, int pairs_per_group, float *__restrict__ part)
+// Persistent forward over the pairs of every job (offsets off[0 .. n]).
+template <bool MLEM>
+__global__ void __launch_bounds__(kFwdThreads, 3)
+k_vox_fwd(const VoxBatch B)
 {
     extern __shared__ __align__(16) unsigned char sm[];
-    const DevProblem &P = a.P;
-    const F32Consts &c = a.c;
-    const int E = a.E, K = P.nwt;
-    const int nwarps = blockDim.x >> 5;
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    float *en = (float *)sm;                                            // [6][E]
-    float4 *cq = (float4 *)(sm + al16(sizeof(float) * 6 * E));          // [K]
-    float4 *rows = cq + K;                                              // [warps][E]
-    float2 *gacc = (float2 *)(rows + (size_t)nwarps * E);               // [warps][32][K]
-    PairRec *prs = (PairRec *)(gacc + (size_t)nwarps * 32 * K);         // [warps]
-    float4 *rw = rows + (size_t)wid * E;
-    float2 *gw = gacc + (size_t)wid * 32 * K;
-    PairRec &pr = prs[wid];
-
-    stage_energy_rows(a, en, tid, blockDim.x);
-    for (int i = tid; i < K; i += blockDim.x) cq[i] = a.coarse_q[i];
-    for (int i = lane; i < 32 * K; i += 32) gw[i] = make_float2(0.f, 0.f);
-    __syncthreads();
-
-    const int nv = a.nv;
-    const int chunk = blockIdx.x * nwarps + wid;
-    if (chunk * 32 >= nv) return;   // no block-wide barrier follows
-    const int64_t npairs = (int64_t)P.n_src * P.n_det;
-    const int64_t p0 = (int64_t)blockIdx.y * pairs_per_group;
-    const int64_t p1 = min(npairs, p0 + pairs_per_group);
-    const float rsqrt2pi = c.rsqrt2pi;
-    const float DQf = c.DQ;
-    const float q_lo = c.q_lo, q_hi = c.q_hi;
-    const int nin = min(32, nv - chunk * 32);
-    const int v = chunk * 32 + min(lane, nin - 1);
-    const int xy = a.vox_xy[v];
-    const float vx = ((float)(xy & 0xffff) + 0.5f) * c.vox;
-    const float vy = ((float)(xy >> 16) + 0.5f) * c.vox;
-
-    for (int64_t p = p0; p < p1; p++) {
-        __syncwarp();   // the previous pair's constants are no longer read
-        if (lane < (int)(sizeof(PairRec) / 4))
-            reinterpret_cast<int *>(&pr)[lane] = reinterpret_cast<const int *>(a.pairs + p)[lane];
-        __syncwarp();
-        const int src = (int)(p % P.n_src);
-        const VoxGeom vg = vox_geom(pr.G, vx, vy);
-        const float2 Asv = a.atten_src[(int64_t)src * nv + v];
-        WalkSetup ws;
-        if (!walk_setup_f32(P, c, pr.G.Rdx.hi, pr.G.Rdy.hi, vx, vy, &ws))
-            walk_setup_f64(P, pr.Rdx, pr.Rdy, (double)vx, (double)vy, &ws);
-        const float *wp = what + p * E;
-        for (int i = 0; i < nin; i++) {
-            WalkSetup wi;
-            wi.rx = __shfl_sync(0xffffffffu, ws.rx, i);
-            wi.ry = __shfl_sync(0xffffffffu, ws.ry, i);
-            wi.Lx = __shfl_sync(0xffffffffu, ws.Lx, i);
-            wi.Ly = __shfl_sync(0xffffffffu, ws.Ly, i);
-            wi.n = __shfl_sync(0xffffffffu, ws.n, i);
-            const float2 Ad = walk_coop(a.cells, P.nx, P.ny, wi, DQf, lane);
-            const float sh = __shfl_sync(0xffffffffu, vg.s.hi, i);
-            const float sl = __shfl_sync(0xffffffffu, vg.s.lo, i);
-            const float sg = __shfl_sync(0xffffffffu, vg.sg, i);
-            const float Wg = __shfl_sync(0xffffffffu, vg.Wg, i);
-            const float Asx = __shfl_sync(0xffffffffu, Asv.x, i);
-            const float Asy = __shfl_sync(0xffffffffu, Asv.y, i);
-            const float s2f = sh * sh;
-            const float sg_s2 = __fdividef(sg, s2f);
-            for (int el = lane; el < E; el += 32) {
-                const EnergyTerm t = energy_term(en, E, el, Ad.x, Ad.y, Asx, Asy, sh, sl, s2f, sg_s2, Wg, rsqrt2pi);
-                float c = __ldg(wp + el) * t.pref;
-                // a window entirely outside the coarse grid contributes nothing
-                if (t.w_hi + t.half < q_lo || t.w_hi - t.half > q_hi) c = 0.f;
-                rw[el] = make_float4(c, t.w_hi, t.w_lo, t.cexp);
-            }
-            __syncwarp();
-            float2 *gi = gw + i * K;
-            for (int k = lane; k < K; k += 32) {
-                const float4 q = cq[k];
-                float acc = 0.f;
-                for (int e = 0; e < E; e++) {
-                    const float4 r = rw[e];
-                    if (r.x == 0.f) continue;   // uniform across the warp
-                    const float d = (r.y - q.x) + (r.z - q.y);
-                    acc = fmaf(r.x, ex2_approx(r.w * d * d), acc);
-                }
-                float2 s = gi[k];
-                kahan_add(s.x, s.y, acc * q.z);
-                gi[k] = s;
-            }
-            __syncwarp();
+    __shared__ PairRec pair;
+    __shared__ VoxJob job;
+    __shared__ long long item_s;
+    const int64_t *off = B.off + 0 * (B.n + 1);
+    const int64_t total = off[B.n];
+    int cur = -1;
+    for (;;) {
+        __syncthreads();   // the previous item is done with shared memory
+        if (threadIdx.x == 0) item_s = (long long)atomicAdd(B.counters + 0, 1ull);
+        __syncthreads();
+        const int64_t item = item_s;
+        if (item >= total) break;
+        const int p = find_job(off, B.n, item);
+        if (p != cur) {
+            load_job(B.jobs, p, &job);
+            cur = p;
+            __syncthreads();
         }
+        vox_fwd_pair<MLEM>(job, item - off[p], sm, pair);
     }
-    float *out = part + ((int64_t)blockIdx.y * nv + (int64_t)chunk * 32) * K;
-    for (int i = lane; i < nin * K; i += 32) out[i] = gw[i].x - gw[i].y;
 }
 
-// what[p, e] = sum_nrg RF[e, nrg] w[p + nrg * npairs] (w == NULL: all ones).
-__global__ void k_vox_wtab(DevProblem P, int E, const float *__restrict__ rf_win, const int *__restrict__ win_lo,
-                           const int *__restrict__ win_n, const float *__restrict__ w, float *__restrict__ what)
+// Adjoint tile (voxel-chunk block bx, pair group by) of job J.  Shared
+// memory: energy rows and coarse bins, then per warp E rows of (coefficient,
+// wvt pair, exponent scale), 32 x K compensated sums and the current pair's
+// record.
+__global__ void __launch_bounds__(128)
+k_vox_adj(const VoxBatch B)
 {
-    const int W = 2 * P.dnrg + 1;
-    const int64_t npairs = (int64_t)P.n_src * P.n_det;
-    const int64_t total = npairs * E;
+    extern __shared__ __align__(16) unsigned char sm[];
+    __shared__ VoxJob J;
+    __shared__ long long item_s;
+    const int nwarps = blockDim.x >> 5;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int64_t *off = B.off + 1 * (B.n + 1);
+    const int64_t total = off[B.n];
+    int cur = -1;
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) item_s = (long long)atomicAdd(B.counters + 1, 1ull);
+        __syncthreads();
+        const int64_t item = item_s;
+        if (item >= total) break;
+        const int p = find_job(off, B.n, item);
+        if (p != cur) {
+            load_job(B.jobs, p, &J);
+            cur = p;
+            __syncthreads();
+        }
+        const DevProblem &P = J.op.P;
+        const F32Consts &c = J.c;
+        const int E = J.E, K = P.nwt;
+        float *en = (float *)sm;                                            // [6][E]
+        float4 *cq = (float4 *)(sm + al16(sizeof(float) * 6 * E));          // [K]
+        float4 *rows = cq + K;                                              // [warps][E]
+        float2 *gacc = (float2 *)(rows + (size_t)nwarps * E);               // [warps][32][K]
+        PairRec *prs = (PairRec *)(gacc + (size_t)nwarps * 32 * K);         // [warps]
+        float4 *rw = rows + (size_t)wid * E;
+        float2 *gw = gacc + (size_t)wid * 32 * K;
+        PairRec &pr = prs[wid];
+        stage_energy_rows(J, en, tid, blockDim.x);
+        for (int i = tid; i < K; i += blockDim.x) cq[i] = J.op.coarse_q[i];
+        for (int i = lane; i < 32 * K; i += 32) gw[i] = make_float2(0.f, 0.f);
+        __syncthreads();
+
+        const int64_t r = item - off[p];
+        const int bx = (int)(r % J.chunk_blocks), by = (int)(r / J.chunk_blocks);
+        const int nv = J.op.nv;
+        const int chunk = bx * nwarps + wid;
+        if (chunk * 32 >= nv) continue;   // an idle warp; the next item starts with a barrier
+        const int64_t npairs = (int64_t)P.n_src * P.n_det;
+        const int64_t p0 = (int64_t)by * J.ppg;
+        const int64_t p1 = min(npairs, p0 + J.ppg);
+        const float rsqrt2pi = c.rsqrt2pi;
+        const float DQf = c.DQ;
+        const float q_lo = c.q_lo, q_hi = c.q_hi;
+        const int nin = min(32, nv - chunk * 32);
+        const int v = chunk * 32 + min(lane, nin - 1);
+        const int xy = J.op.vox_xy[v];
+        const float vx = ((float)(xy & 0xffff) + 0.5f) * c.vox;
+        const float vy = ((float)(xy >> 16) + 0.5f) * c.vox;
+
+        for (int64_t pp = p0; pp < p1; pp++) {
+            __syncwarp();   // the previous pair's constants are no longer read
+            if (lane < (int)(sizeof(PairRec) / 4))
+                reinterpret_cast<int *>(&pr)[lane] = reinterpret_cast<const int *>(J.op.pairs + pp)[lane];
+            __syncwarp();
+            const int src = (int)(pp % P.n_src);
+            const VoxGeom vg = vox_geom(pr.G, vx, vy);
+            const float2 Asv = J.op.atten_src[(int64_t)src * nv + v];
+            WalkSetup ws;
+            if (!walk_setup_f32(P, c, pr.G.Rdx.hi, pr.G.Rdy.hi, vx, vy, &ws))
+                walk_setup_f64(P, pr.Rdx, pr.Rdy, (double)vx, (double)vy, &ws);
+            const float *wp = J.what + pp * E;
+            for (int i = 0; i < nin; i++) {
+                WalkSetup wi;
+                wi.rx = __shfl_sync(0xffffffffu, ws.rx, i);
+                wi.ry = __shfl_sync(0xffffffffu, ws.ry, i);
+                wi.Lx = __shfl_sync(0xffffffffu, ws.Lx, i);
+                wi.Ly = __shfl_sync(0xffffffffu, ws.Ly, i);
+                wi.n = __shfl_sync(0xffffffffu, ws.n, i);
+                const float2 Ad = walk_coop(J.op.cells, P.nx, P.ny, wi, DQf, lane);
+                const float sh = __shfl_sync(0xffffffffu, vg.s.hi, i);
+                const float sl = __shfl_sync(0xffffffffu, vg.s.lo, i);
+                const float sg = __shfl_sync(0xffffffffu, vg.sg, i);
+                const float Wg = __shfl_sync(0xffffffffu, vg.Wg, i);
+                const float Asx = __shfl_sync(0xffffffffu, Asv.x, i);
+                const float Asy = __shfl_sync(0xffffffffu, Asv.y, i);
+                const float s2f = sh * sh;
+                const float sg_s2 = __fdividef(sg, s2f);
+                for (int el = lane; el < E; el += 32) {
+                    const EnergyTerm t =
+                        energy_term(en, E, el, Ad.x, Ad.y, Asx, Asy, sh, sl, s2f, sg_s2, Wg, rsqrt2pi);
+                    float cf = __ldg(wp + el) * t.pref;
+                    // a window entirely outside the coarse grid contributes nothing
+                    if (t.w_hi + t.half < q_lo || t.w_hi - t.half > q_hi) cf = 0.f;
+                    rw[el] = make_float4(cf, t.w_hi, t.w_lo, t.cexp);
+                }
+                __syncwarp();
+                float2 *gi = gw + i * K;
+                for (int k = lane; k < K; k += 32) {
+                    const float4 q = cq[k];
+                    float acc = 0.f;
+                    for (int e = 0; e < E; e++) {
+                        const float4 rr = rw[e];
+                        if (rr.x == 0.f) continue;   // uniform across the warp
+                        const float d = (rr.y - q.x) + (rr.z - q.y);
+                        acc = fmaf(rr.x, ex2_approx(rr.w * d * d), acc);
+                    }
+                    float2 s = gi[k];
+                    kahan_add(s.x, s.y, acc * q.z);
+                    gi[k] = s;
+                }
+                __syncwarp();
+            }
+        }
+        float *out = J.part + ((int64_t)by * nv + (int64_t)chunk * 32) * K;
+        for (int i = lane; i < nin * K; i += 32) out[i] = gw[i].x - gw[i].y;
+    }
+}
+
+// what[p, e] = sum_nrg RF[e, nrg] w[p + nrg * npairs] (ones: every w = 1).
+__global__ void k_vox_wtab(const VoxBatch B, int ones)
+{
+    const int64_t *off = B.off + 4 * (B.n + 1);
+    const int64_t total = off[B.n];
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
          t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t p = t / E;
-        const int el = (int)(t - p * E), e = P.e_lo + el;
+        const int pj = find_job(off, B.n, t);
+        const VoxJob &J = B.jobs[pj];
+        const DevProblem &P = J.op.P;
+        const int W = 2 * P.dnrg + 1, E = J.E;
+        const int64_t npairs = (int64_t)P.n_src * P.n_det;
+        const int64_t loc = t - off[pj];
+        const int64_t p = loc / E;
+        const int el = (int)(loc - p * E), e = P.e_lo + el;
         double s = 0.0;
-        for (int n = win_n[2 * e]; n <= win_n[2 * e + 1]; n++) {
-            const int j = e - win_lo[n];
+        for (int n = J.op.win_n[2 * e]; n <= J.op.win_n[2 * e + 1]; n++) {
+            const int j = e - J.op.win_lo[n];
             if (j < 0 || j >= W) continue;
-            const double wv = w ? (double)w[p + (int64_t)n * npairs] : 1.0;
-            s += (double)rf_win[n * W + j] * wv;
+            const double wv = ones ? 1.0 : (double)J.w[p + (int64_t)n * npairs];
+            s += (double)J.op.rf_win[n * W + j] * wv;
         }
-        what[t] = (float)s;
+        J.what[loc] = (float)s;
     }
 }
 
@@ -369,58 +430,69 @@ __global__ void k_vox_wtab(DevProblem P, int E, const float *__restrict__ rf_win
 //   mode 1: the MLEM update x <- x * sum / (sens + 1e-7), non-finite -> 0,
 //           negative -> 0 (main.m:162-176), and xd = x dq
 //   mode 2: g[voxel] = sum in the full-grid layout (nx + ny*NX)*nwt + k
-__global__ void k_vox_reduce(const float *__restrict__ part, int groups, int nv, int K, int mode,
-                             double *__restrict__ sens, float *__restrict__ xc, float *__restrict__ xd,
-                             const float4 *__restrict__ coarse_q, const int *__restrict__ vox_xy, int nx,
-                             float *__restrict__ g)
+__global__ void k_vox_reduce(const VoxBatch B, int mode)
 {
-    const int64_t total = (int64_t)nv * K;
+    const int64_t *off = B.off + 2 * (B.n + 1);
+    const int64_t total = off[B.n];
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
          t += (int64_t)gridDim.x * blockDim.x) {
+        const int pj = find_job(off, B.n, t);
+        const VoxJob &J = B.jobs[pj];
+        const int K = J.op.P.nwt;
+        const int64_t loc = t - off[pj];
+        const int64_t n = (int64_t)J.op.nv * K;
         double s = 0.0;
-        for (int gi = 0; gi < groups; gi++) s += (double)part[(int64_t)gi * total + t];
+        for (int gi = 0; gi < J.groups; gi++) s += (double)J.part[(int64_t)gi * n + loc];
         if (mode == 0) {
-            sens[t] = s;
+            J.sens[loc] = s;
         } else if (mode == 1) {
-            float v = (float)((double)xc[t] * s / (sens[t] + 1e-7));
+            float v = (float)((double)J.xc[loc] * s / (J.sens[loc] + 1e-7));
             if (!isfinite(v)) v = 0.f;
             if (v < 0.f) v = 0.f;
-            xc[t] = v;
-            xd[t] = v * coarse_q[t % K].z;
+            J.xc[loc] = v;
+            J.xd[loc] = v * J.op.coarse_q[loc % K].z;
         } else {
-            const int64_t vi = t / K;
-            const int xy = vox_xy[vi];
-            g[((int64_t)(xy & 0xffff) + (int64_t)(xy >> 16) * nx) * K + (t - vi * K)] = (float)s;
+            const int64_t vi = loc / K;
+            const int xy = J.op.vox_xy[vi];
+            J.g[((int64_t)(xy & 0xffff) + (int64_t)(xy >> 16) * J.op.P.nx) * K + (loc - vi * K)] = (float)s;
         }
     }
 }
 
-// Full grid [ny][nx][K] -> compact voxel order: xc = x, xd = x dq.
-__global__ void k_vox_gather(const float *__restrict__ x, const int *__restrict__ vox_xy, int nv, int K, int nx,
-                             const float4 *__restrict__ coarse_q, float *__restrict__ xc, float *__restrict__ xd)
+// Full grid -> compact voxel order: xd = x dq (and xc = x when with_xc).
+__global__ void k_vox_gather(const VoxBatch B, int with_xc)
 {
-    const int64_t total = (int64_t)nv * K;
+    const int64_t *off = B.off + 2 * (B.n + 1);
+    const int64_t total = off[B.n];
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
          t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t vi = t / K;
-        const int k = (int)(t - vi * K);
-        const int xy = vox_xy[vi];
-        const float v = x[((int64_t)(xy & 0xffff) + (int64_t)(xy >> 16) * nx) * K + k];
-        if (xc) xc[t] = v;
-        xd[t] = v * coarse_q[k].z;
+        const int pj = find_job(off, B.n, t);
+        const VoxJob &J = B.jobs[pj];
+        const int K = J.op.P.nwt;
+        const int64_t loc = t - off[pj];
+        const int64_t vi = loc / K;
+        const int k = (int)(loc - vi * K);
+        const int xy = J.op.vox_xy[vi];
+        const float v = J.xfull[((int64_t)(xy & 0xffff) + (int64_t)(xy >> 16) * J.op.P.nx) * K + k];
+        if (with_xc) J.xc[loc] = v;
+        J.xd[loc] = v * J.op.coarse_q[k].z;
     }
 }
 
 // Compact -> full grid (the other voxels are left as they are).
-__global__ void k_vox_scatter(const float *__restrict__ xc, const int *__restrict__ vox_xy, int nv, int K, int nx,
-                              float *__restrict__ x)
+__global__ void k_vox_scatter(const VoxBatch B)
 {
-    const int64_t total = (int64_t)nv * K;
+    const int64_t *off = B.off + 2 * (B.n + 1);
+    const int64_t total = off[B.n];
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
          t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t vi = t / K;
-        const int xy = vox_xy[vi];
-        x[((int64_t)(xy & 0xffff) + (int64_t)(xy >> 16) * nx) * K + (t - vi * K)] = xc[t];
+        const int pj = find_job(off, B.n, t);
+        const VoxJob &J = B.jobs[pj];
+        const int K = J.op.P.nwt;
+        const int64_t loc = t - off[pj];
+        const int64_t vi = loc / K;
+        const int xy = J.op.vox_xy[vi];
+        J.xout[((int64_t)(xy & 0xffff) + (int64_t)(xy >> 16) * J.op.P.nx) * K + (loc - vi * K)] = J.xc[loc];
     }
 }
 
@@ -444,23 +516,25 @@ int grid_for(int64_t n, int threads)
     return (int)(b < 1 ? 1 : b);
 }
 
-VoxArgs make_args(const VoxOp &op)
+template <class F>
+cudaError_t allow_dynamic_smem(F *kernel, int max_smem)
 {
-    VoxArgs a;
-    a.P = op.P;
-    a.pairs = op.pairs;
-    a.energy = op.energy;
-    a.rf_win = op.rf_win;
-    a.win_lo = op.win_lo;
-    a.win_n = op.win_n;
-    a.coarse_q = op.coarse_q;
-    a.vox_xy = op.vox_xy;
-    a.cells = op.cells;
-    a.atten_src = op.atten_src;
-    a.nv = op.nv;
-    a.E = op.P.e_hi - op.P.e_lo + 1;
-    a.c = make_f32_consts(op.P);
-    return a;
+    // the limit covers static and dynamic shared memory together
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, kernel);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem - (int)fa.sharedSizeBytes);
+}
+
+template <class F>
+size_t static_smem(F *kernel)
+{
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return fa.sharedSizeBytes;
 }
 
 } // namespace
@@ -476,16 +550,6 @@ cudaError_t launch_pair_table(const DevProblem &P, const SrcGeom *sg, PairRec *o
     return cudaGetLastError();
 }
 
-template <class F>
-cudaError_t allow_dynamic_smem(F *kernel, int max_smem)
-{
-    // the limit covers static and dynamic shared memory together
-    cudaFuncAttributes fa;
-    cudaError_t e = cudaFuncGetAttributes(&fa, kernel);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem - (int)fa.sharedSizeBytes);
-}
-
 cudaError_t vox_set_attributes(int max_smem)
 {
     // the launches stay free of attribute calls, so they can be captured
@@ -495,16 +559,10 @@ cudaError_t vox_set_attributes(int max_smem)
     return e;
 }
 
-size_t vox_fwd_static_smem() { return sizeof(PairRec); }
+size_t vox_fwd_static_smem() { return static_smem(k_vox_fwd<true>); }
+size_t vox_adj_static_smem() { return static_smem(k_vox_adj); }
 
 size_t vox_fwd_smem(const DevProblem &P) { return vox_fwd_layout(P, P.e_hi - P.e_lo + 1).total; }
-
-int vox_adj_warps(int K)
-{
-    // per warp: 32 voxels x K compensated sums, plus the energy rows
-    int w = (int)((96 * 1024) / ((size_t)32 * K * sizeof(float2)));
-    return w < 1 ? 1 : (w > 4 ? 4 : w);
-}
 
 size_t vox_adj_smem(const DevProblem &P, int warps)
 {
@@ -513,76 +571,70 @@ size_t vox_adj_smem(const DevProblem &P, int warps)
            sizeof(float2) * (size_t)warps * 32 * K + sizeof(PairRec) * warps;
 }
 
-int vox_adj_groups(const VoxOp &op, int sm_count)
+int vox_fwd_blocks_per_sm(size_t smem)
 {
-    const int chunks = (op.nv + 31) / 32;
-    const int64_t npairs = (int64_t)op.P.n_src * op.P.n_det;
-    int64_t g = ((int64_t)sm_count * 32 + chunks - 1) / chunks;   // about 32 warps per SM in all
-    if (g < 1) g = 1;
-    if (g > npairs) g = npairs;
-    if (g > 1024) g = 1024;
-    return (int)g;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_vox_fwd<true>, kFwdThreads, smem) != cudaSuccess) {
+        cudaGetLastError();
+        n = 1;
+    }
+    return n < 1 ? 1 : n;
 }
 
-cudaError_t launch_vox_forward(const VoxOp &op, const float *xd, float *y, const float *ymeas, const float *cbg,
-                               float *what, cudaStream_t s, int64_t *launches)
+int vox_adj_blocks_per_sm(int warps, size_t smem)
 {
-    const VoxArgs a = make_args(op);
-    const size_t smem = vox_fwd_smem(op.P);
-    dim3 grid(op.P.n_det, op.P.n_src);
-    if (what) k_vox_fwd<true><<<grid, kFwdThreads, smem, s>>>(a, xd, nullptr, ymeas, cbg, what);
-    else k_vox_fwd<false><<<grid, kFwdThreads, smem, s>>>(a, xd, y, nullptr, nullptr, nullptr);
-    if (launches) (*launches)++;
-    return cudaGetLastError();
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_vox_adj, 32 * warps, smem) != cudaSuccess) {
+        cudaGetLastError();
+        n = 1;
+    }
+    return n < 1 ? 1 : n;
 }
 
-cudaError_t launch_vox_wtab(const VoxOp &op, const float *w, float *what, cudaStream_t s, int64_t *launches)
-{
-    const int E = op.P.e_hi - op.P.e_lo + 1;
-    const int64_t n = (int64_t)op.P.n_src * op.P.n_det * E;
-    k_vox_wtab<<<grid_for(n, 256), 256, 0, s>>>(op.P, E, op.rf_win, op.win_lo, op.win_n, w, what);
-    if (launches) (*launches)++;
-    return cudaGetLastError();
-}
-
-cudaError_t launch_vox_adjoint(const VoxOp &op, const float *what, float *part, int groups, cudaStream_t s,
+cudaError_t launch_vox_forward(const VoxBatch &B, bool mlem, int grid, size_t smem, cudaStream_t s,
                                int64_t *launches)
 {
-    const VoxArgs a = make_args(op);
-    const int warps = vox_adj_warps(op.P.nwt);
-    const size_t smem = vox_adj_smem(op.P, warps);
-    const int64_t npairs = (int64_t)op.P.n_src * op.P.n_det;
-    const int ppg = (int)((npairs + groups - 1) / groups);
-    const int chunks = (op.nv + 31) / 32;
-    dim3 grid((chunks + warps - 1) / warps, groups);
-    k_vox_adj<<<grid, 32 * warps, smem, s>>>(a, what, ppg, part);
+    cudaError_t e = cudaMemsetAsync(B.counters + 0, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    if (mlem) k_vox_fwd<true><<<grid, kFwdThreads, smem, s>>>(B);
+    else k_vox_fwd<false><<<grid, kFwdThreads, smem, s>>>(B);
     if (launches) (*launches)++;
     return cudaGetLastError();
 }
 
-cudaError_t launch_vox_reduce(const VoxOp &op, const float *part, int groups, int mode, double *sens, float *xc,
-                              float *xd, float *g, cudaStream_t s, int64_t *launches)
+cudaError_t launch_vox_adjoint(const VoxBatch &B, int grid, size_t smem, cudaStream_t s, int64_t *launches)
 {
-    const int64_t n = (int64_t)op.nv * op.P.nwt;
-    k_vox_reduce<<<grid_for(n, 256), 256, 0, s>>>(part, groups, op.nv, op.P.nwt, mode, sens, xc, xd, op.coarse_q,
-                                                  op.vox_xy, op.P.nx, g);
+    cudaError_t e = cudaMemsetAsync(B.counters + 1, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    k_vox_adj<<<grid, 32 * B.adj_warps, smem, s>>>(B);
     if (launches) (*launches)++;
     return cudaGetLastError();
 }
 
-cudaError_t launch_vox_gather(const VoxOp &op, const float *x, float *xc, float *xd, cudaStream_t s,
-                              int64_t *launches)
+cudaError_t launch_vox_wtab(const VoxBatch &B, int64_t total, bool ones, cudaStream_t s, int64_t *launches)
 {
-    const int64_t n = (int64_t)op.nv * op.P.nwt;
-    k_vox_gather<<<grid_for(n, 256), 256, 0, s>>>(x, op.vox_xy, op.nv, op.P.nwt, op.P.nx, op.coarse_q, xc, xd);
+    k_vox_wtab<<<grid_for(total, 256), 256, 0, s>>>(B, ones ? 1 : 0);
     if (launches) (*launches)++;
     return cudaGetLastError();
 }
 
-cudaError_t launch_vox_scatter(const VoxOp &op, const float *xc, float *x, cudaStream_t s, int64_t *launches)
+cudaError_t launch_vox_reduce(const VoxBatch &B, int64_t total, int mode, cudaStream_t s, int64_t *launches)
 {
-    const int64_t n = (int64_t)op.nv * op.P.nwt;
-    k_vox_scatter<<<grid_for(n, 256), 256, 0, s>>>(xc, op.vox_xy, op.nv, op.P.nwt, op.P.nx, x);
+    k_vox_reduce<<<grid_for(total, 256), 256, 0, s>>>(B, mode);
+    if (launches) (*launches)++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_vox_gather(const VoxBatch &B, int64_t total, bool with_xc, cudaStream_t s, int64_t *launches)
+{
+    k_vox_gather<<<grid_for(total, 256), 256, 0, s>>>(B, with_xc ? 1 : 0);
+    if (launches) (*launches)++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_vox_scatter(const VoxBatch &B, int64_t total, cudaStream_t s, int64_t *launches)
+{
+    k_vox_scatter<<<grid_for(total, 256), 256, 0, s>>>(B);
     if (launches) (*launches)++;
     return cudaGetLastError();
 }

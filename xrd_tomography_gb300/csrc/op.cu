@@ -21,7 +21,7 @@ struct xrdt_op {
     xrdt_problem p;
     VoxOp v;
     std::vector<void *> allocs;
-    int groups = 1;
+    int groups_cap = 1;                   // rows of part: the most adjoint pair groups
     int64_t rays = 0;
     bool sens_ready = false;              // sens holds Av^T 1
     // device buffers
@@ -40,9 +40,28 @@ struct xrdt_op {
     double *gd = nullptr;                 // [NX*NY*NWT] FP64 adjoint accumulator
     int64_t *rays_d = nullptr;            // staged ray list
     int64_t rays_cap = 0;
-    // MLEM iteration as a graph, keyed by the ray vectors it reads
+    struct Plan *plan = nullptr;          // the operator as a batch of one (created on first use)
+};
+
+// A batch of operators as the kernels see it: the job descriptors (a pinned
+// host mirror and its device copy), the work offsets, the adjoint split and
+// the persistent grids, and the MLEM iteration captured as a graph.
+struct Plan {
+    xrdt_ctx *ctx = nullptr;
+    std::vector<xrdt_op *> ops;
+    VoxJob *jobs_h = nullptr;
+    VoxJob *jobs_d = nullptr;
+    int64_t *off_d = nullptr;
+    unsigned long long *counters_d = nullptr;
+    std::vector<int64_t> off;          // 5 x (n + 1)
+    int sms = 0;
+    int adj_warps = 1;
+    int64_t adj_tiles = 0;             // target number of adjoint tiles
+    int fwd_grid = 1, adj_grid = 1;
+    size_t fwd_smem = 0, adj_smem = 0;
+    bool tuned = false;
     cudaGraphExec_t mlem_exec = nullptr;
-    const void *mlem_key[2] = {};
+    int64_t mlem_cfg[3] = {};          // adj_warps, adj_tiles, fwd_grid of the captured graph
 };
 
 namespace {
@@ -83,9 +102,21 @@ int op_alloc_t(xrdt_op *op, size_t count, T **out)
     return rc;
 }
 
+void plan_free(Plan *pl)
+{
+    if (!pl) return;
+    if (pl->mlem_exec) cudaGraphExecDestroy(pl->mlem_exec);
+    if (pl->jobs_h) cudaFreeHost(pl->jobs_h);
+    if (pl->jobs_d) cudaFree(pl->jobs_d);
+    if (pl->off_d) cudaFree(pl->off_d);
+    if (pl->counters_d) cudaFree(pl->counters_d);
+    delete pl;
+}
+
 void op_free(xrdt_op *op)
 {
-    if (op->mlem_exec) cudaGraphExecDestroy(op->mlem_exec);
+    plan_free(op->plan);
+    op->plan = nullptr;
     for (void *p : op->allocs) cudaFree(p);
     op->allocs.clear();
 }
@@ -122,26 +153,331 @@ int begin(xrdt_op *op)
     return XRDT_OK;
 }
 
-// Sensitivity Av^T 1, once per operator.
-int ensure_sens(xrdt_op *op)
+// ---- plans ------------------------------------------------------------------
+
+int64_t pairs_of(const xrdt_op *op) { return (int64_t)op->p.n_src * op->v.P.n_det; }
+int chunks_of(const xrdt_op *op) { return (op->v.nv + 31) / 32; }
+
+// Adjoint split for a warps-per-block count and a target tile count: one
+// pairs-per-group for the whole batch, so that tiles carry similar work.
+void plan_split(Plan *pl, int warps, int64_t tiles)
 {
-    xrdt_ctx *ctx = op->ctx;
-    if (op->sens_ready) return XRDT_OK;
+    const int n = (int)pl->ops.size();
+    double work = 0.0;   // sum of chunk blocks x pairs
+    for (int i = 0; i < n; i++) {
+        const int cb = (chunks_of(pl->ops[i]) + warps - 1) / warps;
+        work += (double)cb * (double)pairs_of(pl->ops[i]);
+    }
+    int64_t ppg = (int64_t)std::ceil(work / (double)std::max<int64_t>(tiles, 1));
+    if (ppg < 1) ppg = 1;
+    pl->off.assign(5 * (size_t)(n + 1), 0);
+    size_t smem = 0;
+    for (int i = 0; i < n; i++) {
+        const xrdt_op *op = pl->ops[i];
+        VoxJob &J = pl->jobs_h[i];
+        const int64_t np = pairs_of(op);
+        J.chunk_blocks = std::max(1, (chunks_of(op) + warps - 1) / warps);
+        int64_t g = (np + ppg - 1) / ppg;
+        if (g > op->groups_cap) g = op->groups_cap;
+        if (g < 1) g = 1;
+        J.groups = (int)g;
+        J.ppg = (int)((np + g - 1) / g);
+        int64_t *o = pl->off.data();
+        const int N1 = n + 1;
+        o[0 * N1 + i + 1] = o[0 * N1 + i] + np;
+        o[1 * N1 + i + 1] = o[1 * N1 + i] + (op->v.nv > 0 ? (int64_t)J.chunk_blocks * J.groups : 0);
+        o[2 * N1 + i + 1] = o[2 * N1 + i] + (int64_t)op->v.nv * op->p.nwt;
+        o[3 * N1 + i + 1] = o[3 * N1 + i] + (int64_t)op->p.nx * op->p.ny * op->p.nwt;
+        o[4 * N1 + i + 1] = o[4 * N1 + i] + np * J.E;
+        smem = std::max(smem, vox_adj_smem(op->v.P, warps));
+    }
+    pl->adj_warps = warps;
+    pl->adj_tiles = tiles;
+    pl->adj_smem = smem;
+    const int bps = vox_adj_blocks_per_sm(warps, smem);
+    const int64_t items = pl->off[1 * (size_t)(n + 1) + n];
+    pl->adj_grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)pl->sms * bps, items));
+}
+
+int plan_upload(Plan *pl)
+{
+    xrdt_ctx *ctx = pl->ctx;
+    const size_t n = pl->ops.size();
+    CK(cudaMemcpyAsync(pl->jobs_d, pl->jobs_h, sizeof(VoxJob) * n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(pl->off_d, pl->off.data(), sizeof(int64_t) * pl->off.size(), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    return XRDT_OK;
+}
+
+VoxBatch plan_batch(const Plan *pl)
+{
+    VoxBatch B;
+    B.jobs = pl->jobs_d;
+    B.off = pl->off_d;
+    B.counters = pl->counters_d;
+    B.n = (int)pl->ops.size();
+    B.adj_warps = pl->adj_warps;
+    return B;
+}
+
+int64_t plan_total(const Plan *pl, int row) { return pl->off[(size_t)row * (pl->ops.size() + 1) + pl->ops.size()]; }
+
+int plan_create(xrdt_ctx *ctx, xrdt_op *const *ops, int n, Plan **out)
+{
+    Plan *pl = new Plan();
+    pl->ctx = ctx;
+    pl->ops.assign(ops, ops + n);
+    cudaError_t e = cudaMallocHost((void **)&pl->jobs_h, sizeof(VoxJob) * n);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&pl->jobs_d, sizeof(VoxJob) * n);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&pl->off_d, sizeof(int64_t) * 5 * (n + 1));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&pl->counters_d, sizeof(unsigned long long) * 2);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&pl->sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        plan_free(pl);
+        return fail(ctx, XRDT_ERR_ALLOC, fmt("batch set-up: %s", cudaGetErrorString(e)));
+    }
+    memset(pl->jobs_h, 0, sizeof(VoxJob) * n);
+    size_t fsmem = 0;
+    for (int i = 0; i < n; i++) {
+        xrdt_op *op = ops[i];
+        VoxJob &J = pl->jobs_h[i];
+        J.op = op->v;
+        J.c = make_f32_consts(op->v.P);
+        J.E = op->v.P.e_hi - op->v.P.e_lo + 1;
+        J.xd = op->xd;
+        J.xc = op->xc;
+        J.what = op->what;
+        J.part = op->part;
+        J.sens = op->sens;
+        fsmem = std::max(fsmem, vox_fwd_smem(op->v.P));
+    }
+    pl->fwd_smem = fsmem;
+    // the widest adjoint block the shared memory allows
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
+    int warps = 4;
+    for (; warps > 1; warps /= 2) {
+        size_t sm = 0;
+        for (int i = 0; i < n; i++) sm = std::max(sm, vox_adj_smem(ops[i]->v.P, warps));
+        if ((int64_t)(sm + vox_adj_static_smem()) <= optin) break;
+    }
+    plan_split(pl, warps, (int64_t)pl->sms * 4 * vox_adj_blocks_per_sm(warps, 0));
+    const int64_t items = plan_total(pl, 0);
+    pl->fwd_grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)pl->sms * vox_fwd_blocks_per_sm(fsmem), items));
+    *out = pl;
+    return XRDT_OK;
+}
+
+// Sensitivity Av^T 1 of every operator of the plan that has none yet.
+int plan_sens(Plan *pl)
+{
+    xrdt_ctx *ctx = pl->ctx;
+    bool all = true;
+    for (xrdt_op *op : pl->ops) all = all && op->sens_ready;
+    if (all) return XRDT_OK;
+    int rc = plan_upload(pl);
+    if (rc) return rc;
+    const VoxBatch B = plan_batch(pl);
     cudaStream_t st = ctx->stream;
     {
         ProfScope ps(ctx, XRDT_KERNEL_VOX_UPDATE);
-        CK(launch_vox_wtab(op->v, nullptr, op->what, st, &ctx->launches));
+        CK(launch_vox_wtab(B, plan_total(pl, 4), true, st, &ctx->launches));
     }
     {
         ProfScope ps(ctx, XRDT_KERNEL_VOX_ADJOINT);
-        CK(launch_vox_adjoint(op->v, op->what, op->part, op->groups, st, &ctx->launches));
+        CK(launch_vox_adjoint(B, pl->adj_grid, pl->adj_smem, st, &ctx->launches));
     }
     {
         ProfScope ps(ctx, XRDT_KERNEL_VOX_UPDATE);
-        CK(launch_vox_reduce(op->v, op->part, op->groups, 0, op->sens, nullptr, nullptr, nullptr, st,
-                             &ctx->launches));
+        CK(launch_vox_reduce(B, plan_total(pl, 2), 0, st, &ctx->launches));
     }
-    op->sens_ready = true;
+    for (xrdt_op *op : pl->ops) op->sens_ready = true;
+    return XRDT_OK;
+}
+
+// Autotuner of the adjoint split: times one adjoint launch per candidate
+// (warps per block x tiles per SM slot) and keeps the fastest.  Reads the
+// per-energy weights of all ones and writes only the partial sums.
+int plan_tune(Plan *pl)
+{
+    xrdt_ctx *ctx = pl->ctx;
+    if (pl->tuned) return XRDT_OK;
+    cudaStream_t st = ctx->stream;
+    int optin = 0;
+    CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
+    int rc = plan_upload(pl);
+    if (rc) return rc;
+    CK(launch_vox_wtab(plan_batch(pl), plan_total(pl, 4), true, st, &ctx->launches));
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    float best = 1e30f;
+    int best_w = pl->adj_warps;
+    int64_t best_t = pl->adj_tiles;
+    const int warps_c[3] = {1, 2, 4};
+    const int per_slot[3] = {2, 4, 8};
+    for (int wi = 0; wi < 3; wi++) {
+        const int w = warps_c[wi];
+        size_t sm = 0;
+        for (xrdt_op *op : pl->ops) sm = std::max(sm, vox_adj_smem(op->v.P, w));
+        if ((int64_t)(sm + vox_adj_static_smem()) > optin) continue;
+        const int64_t slots = (int64_t)pl->sms * vox_adj_blocks_per_sm(w, sm);
+        for (int ti = 0; ti < 3; ti++) {
+            plan_split(pl, w, slots * per_slot[ti]);
+            if ((rc = plan_upload(pl))) break;
+            cudaError_t e = cudaEventRecord(a, st);
+            if (e == cudaSuccess) e = launch_vox_adjoint(plan_batch(pl), pl->adj_grid, pl->adj_smem, st, &ctx->launches);
+            if (e == cudaSuccess) e = cudaEventRecord(b, st);
+            if (e == cudaSuccess) e = cudaEventSynchronize(b);
+            float ms = 0.f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                rc = fail(ctx, XRDT_ERR_CUDA, fmt("adjoint autotuning: %s", cudaGetErrorString(e)));
+                break;
+            }
+            if (ms < best) {
+                best = ms;
+                best_w = w;
+                best_t = slots * per_slot[ti];
+            }
+        }
+        if (rc) break;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (rc) return rc;
+    plan_split(pl, best_w, best_t);
+    pl->tuned = true;
+    return plan_upload(pl);
+}
+
+int op_plan(xrdt_op *op, Plan **pl)
+{
+    if (!op->plan) {
+        int rc = plan_create(op->ctx, &op, 1, &op->plan);
+        if (rc) return rc;
+    }
+    *pl = op->plan;
+    return XRDT_OK;
+}
+
+// y[i] = Av_i x[i] for every problem (device arrays, full-grid x).
+int plan_forward(Plan *pl, const float *const *x, float *const *y)
+{
+    xrdt_ctx *ctx = pl->ctx;
+    cudaStream_t st = ctx->stream;
+    const int n = (int)pl->ops.size();
+    for (int i = 0; i < n; i++) {
+        pl->jobs_h[i].xfull = x[i];
+        pl->jobs_h[i].y = y[i];
+    }
+    int rc = plan_upload(pl);
+    if (rc) return rc;
+    const VoxBatch B = plan_batch(pl);
+    if (plan_total(pl, 2) > 0) {
+        ProfScope ps(ctx, XRDT_KERNEL_VOX_UPDATE);
+        CK(launch_vox_gather(B, plan_total(pl, 2), false, st, &ctx->launches));
+    }
+    // a problem without voxels gets zeros: its pairs sum nothing
+    ProfScope ps(ctx, XRDT_KERNEL_VOX_FORWARD);
+    CK(launch_vox_forward(B, false, pl->fwd_grid, pl->fwd_smem, st, &ctx->launches));
+    return XRDT_OK;
+}
+
+// g[i] = Av_i^T w[i] for every problem (device arrays, full-grid g).
+int plan_adjoint(Plan *pl, const float *const *w, float *const *g)
+{
+    xrdt_ctx *ctx = pl->ctx;
+    cudaStream_t st = ctx->stream;
+    const int n = (int)pl->ops.size();
+    for (int i = 0; i < n; i++) {
+        const xrdt_op *op = pl->ops[i];
+        pl->jobs_h[i].w = w[i];
+        pl->jobs_h[i].g = g[i];
+        CK(cudaMemsetAsync(g[i], 0, sizeof(float) * (size_t)op->p.nx * op->p.ny * op->p.nwt, st));
+    }
+    if (plan_total(pl, 2) == 0) return XRDT_OK;
+    int rc = plan_upload(pl);
+    if (rc) return rc;
+    const VoxBatch B = plan_batch(pl);
+    {
+        ProfScope ps(ctx, XRDT_KERNEL_VOX_UPDATE);
+        CK(launch_vox_wtab(B, plan_total(pl, 4), false, st, &ctx->launches));
+    }
+    {
+        ProfScope ps(ctx, XRDT_KERNEL_VOX_ADJOINT);
+        CK(launch_vox_adjoint(B, pl->adj_grid, pl->adj_smem, st, &ctx->launches));
+    }
+    ProfScope ps(ctx, XRDT_KERNEL_VOX_UPDATE);
+    CK(launch_vox_reduce(B, plan_total(pl, 2), 2, st, &ctx->launches));
+    return XRDT_OK;
+}
+
+// iters MLEM updates of every problem; x[i] full grid, in and out (device).
+int plan_mlem(Plan *pl, const float *const *y, const float *const *c, float *const *x, int iters)
+{
+    xrdt_ctx *ctx = pl->ctx;
+    cudaStream_t st = ctx->stream;
+    const int n = (int)pl->ops.size();
+    if (iters == 0) return XRDT_OK;
+    int rc;
+    if (plan_total(pl, 2) > 0) {
+        if ((rc = plan_tune(pl)) || (rc = plan_sens(pl))) return rc;
+        for (int i = 0; i < n; i++) {
+            pl->jobs_h[i].ymeas = y[i];
+            pl->jobs_h[i].cbg = c[i];
+            pl->jobs_h[i].xfull = x[i];
+            pl->jobs_h[i].xout = x[i];
+        }
+        if ((rc = plan_upload(pl))) return rc;
+        const VoxBatch B = plan_batch(pl);
+        {
+            ProfScope ps(ctx, XRDT_KERNEL_VOX_UPDATE);
+            CK(launch_vox_gather(B, plan_total(pl, 2), true, st, &ctx->launches));
+        }
+        const int64_t cfg[3] = {pl->adj_warps, pl->adj_tiles, pl->fwd_grid};
+        if (!pl->mlem_exec || memcmp(cfg, pl->mlem_cfg, sizeof cfg) != 0) {
+            if (pl->mlem_exec) {
+                cudaGraphExecDestroy(pl->mlem_exec);
+                pl->mlem_exec = nullptr;
+            }
+            // the graph reads the job descriptors at run time: new arrays
+            // only need a new upload, not a new capture
+            cudaGraph_t graph;
+            CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            int64_t dummy = 0;
+            cudaError_t le = launch_vox_forward(B, true, pl->fwd_grid, pl->fwd_smem, st, &dummy);
+            if (le == cudaSuccess) le = launch_vox_adjoint(B, pl->adj_grid, pl->adj_smem, st, &dummy);
+            if (le == cudaSuccess) le = launch_vox_reduce(B, plan_total(pl, 2), 1, st, &dummy);
+            cudaError_t ce = cudaStreamEndCapture(st, &graph);
+            if (le != cudaSuccess) {
+                if (ce == cudaSuccess) cudaGraphDestroy(graph);
+                cudaGetLastError();
+                return fail(ctx, XRDT_ERR_CUDA, fmt("MLEM capture: %s", cudaGetErrorString(le)));
+            }
+            CK(ce);
+            cudaError_t ie = cudaGraphInstantiate(&pl->mlem_exec, graph, 0);
+            cudaGraphDestroy(graph);
+            CK(ie);
+            memcpy(pl->mlem_cfg, cfg, sizeof cfg);
+        }
+        {
+            ProfScope ps(ctx, XRDT_KERNEL_VOX_FORWARD);   // the whole iteration (three kernels)
+            for (int it = 0; it < iters; it++) CK(cudaGraphLaunch(pl->mlem_exec, st));
+        }
+        ctx->launches += 3 * (int64_t)iters;
+    }
+    // empty voxels have no sensitivity: the update sets them to 0
+    for (int i = 0; i < n; i++) {
+        const xrdt_op *op = pl->ops[i];
+        CK(cudaMemsetAsync(x[i], 0, sizeof(float) * (size_t)op->p.nx * op->p.ny * op->p.nwt, st));
+    }
+    if (plan_total(pl, 2) > 0) {
+        ProfScope ps(ctx, XRDT_KERNEL_VOX_UPDATE);
+        CK(launch_vox_scatter(plan_batch(pl), plan_total(pl, 2), st, &ctx->launches));
+    }
     return XRDT_OK;
 }
 
@@ -293,18 +629,23 @@ int32_t xrdt_op_create(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectr
         fail(ctx, XRDT_ERR_CUDA, fmt("operator tables: %s", cudaGetErrorString(e)));
         return bail(XRDT_ERR_CUDA);
     }
-    op->groups = vox_adj_groups(op->v, sms);
+    // partial-sum rows for up to the adjoint pair groups that fill the GPU
+    // with the narrowest tiles this problem can get on its own
+    {
+        const int64_t cb = std::max(1, (nv + 63) / 64);
+        op->groups_cap = (int)std::max<int64_t>(1, std::min<int64_t>(npairs, ((int64_t)sms * 64 + cb - 1) / cb));
+    }
     const size_t nx_k = (size_t)std::max(nv, 1) * K;
     if ((rc = op_alloc_t(op, nx_k, &op->xc)) || (rc = op_alloc_t(op, nx_k, &op->xd)) ||
         (rc = op_alloc_t(op, (size_t)npairs * E, &op->what)) ||
-        (rc = op_alloc_t(op, (size_t)op->groups * nx_k, &op->part)) || (rc = op_alloc_t(op, nx_k, &op->sens)) ||
+        (rc = op_alloc_t(op, (size_t)op->groups_cap * nx_k, &op->part)) || (rc = op_alloc_t(op, nx_k, &op->sens)) ||
         (rc = op_alloc_t(op, (size_t)nvox * K, &op->xfull)) || (rc = op_alloc_t(op, (size_t)op->rays, &op->ray_a)) ||
         (rc = op_alloc_t(op, (size_t)op->rays, &op->ray_b)))
         return bail(rc);
     int optin = 0;
     e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
     if (e == cudaSuccess && ((int64_t)(vox_fwd_smem(P) + vox_fwd_static_smem()) > optin ||
-                           (int64_t)vox_adj_smem(P, vox_adj_warps(K)) > optin)) {
+                           (int64_t)(vox_adj_smem(P, 1) + vox_adj_static_smem()) > optin)) {
         fail(ctx, XRDT_ERR_UNSUPPORTED, "the problem's tables exceed the shared memory of one block");
         return bail(XRDT_ERR_UNSUPPORTED);
     }
@@ -341,22 +682,13 @@ int32_t xrdt_op_forward(xrdt_op *op, const float *x, float *y, uint32_t flags)
     if (!x || !y) return fail(ctx, XRDT_ERR_NULL, "x and y are required");
     if (flags) return fail(ctx, XRDT_ERR_UNSUPPORTED, "unknown flag bits");
     cudaStream_t st = ctx->stream;
-    const int K = op->p.nwt;
-    const size_t nfull = (size_t)op->p.nx * op->p.ny * K;
+    const size_t nfull = (size_t)op->p.nx * op->p.ny * op->p.nwt;
     const bool hostY = !is_device_ptr(y);
     float *dy = hostY ? op->ray_a : y;
-    if (op->v.nv == 0) {
-        CK(cudaMemsetAsync(dy, 0, sizeof(float) * op->rays, st));
-    } else {
-        const float *dx;
-        if ((rc = view_in(op, x, nfull, op->xfull, &dx))) return rc;
-        {
-            ProfScope ps(ctx, XRDT_KERNEL_VOX_UPDATE);
-            CK(launch_vox_gather(op->v, dx, nullptr, op->xd, st, &ctx->launches));
-        }
-        ProfScope ps(ctx, XRDT_KERNEL_VOX_FORWARD);
-        CK(launch_vox_forward(op->v, op->xd, dy, nullptr, nullptr, nullptr, st, &ctx->launches));
-    }
+    const float *dx;
+    Plan *pl;
+    if ((rc = view_in(op, x, nfull, op->xfull, &dx)) || (rc = op_plan(op, &pl))) return rc;
+    if ((rc = plan_forward(pl, &dx, &dy))) return rc;
     if (hostY) CK(cudaMemcpyAsync(y, dy, sizeof(float) * op->rays, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     return XRDT_OK;
@@ -370,25 +702,13 @@ int32_t xrdt_op_adjoint(xrdt_op *op, const float *w, float *g, uint32_t flags)
     if (!w || !g) return fail(ctx, XRDT_ERR_NULL, "w and g are required");
     if (flags) return fail(ctx, XRDT_ERR_UNSUPPORTED, "unknown flag bits");
     cudaStream_t st = ctx->stream;
-    const int K = op->p.nwt;
-    const size_t nfull = (size_t)op->p.nx * op->p.ny * K;
+    const size_t nfull = (size_t)op->p.nx * op->p.ny * op->p.nwt;
     const bool hostG = !is_device_ptr(g);
     float *dg = hostG ? op->xfull : g;
-    CK(cudaMemsetAsync(dg, 0, sizeof(float) * nfull, st));
-    if (op->v.nv > 0) {
-        const float *dw;
-        if ((rc = view_in(op, w, op->rays, op->ray_a, &dw))) return rc;
-        {
-            ProfScope ps(ctx, XRDT_KERNEL_VOX_UPDATE);
-            CK(launch_vox_wtab(op->v, dw, op->what, st, &ctx->launches));
-        }
-        {
-            ProfScope ps(ctx, XRDT_KERNEL_VOX_ADJOINT);
-            CK(launch_vox_adjoint(op->v, op->what, op->part, op->groups, st, &ctx->launches));
-        }
-        ProfScope ps(ctx, XRDT_KERNEL_VOX_UPDATE);
-        CK(launch_vox_reduce(op->v, op->part, op->groups, 2, nullptr, nullptr, nullptr, dg, st, &ctx->launches));
-    }
+    const float *dw;
+    Plan *pl;
+    if ((rc = view_in(op, w, op->rays, op->ray_a, &dw)) || (rc = op_plan(op, &pl))) return rc;
+    if ((rc = plan_adjoint(pl, &dw, &dg))) return rc;
     if (hostG) CK(cudaMemcpyAsync(g, dg, sizeof(float) * nfull, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     return XRDT_OK;
@@ -498,62 +818,148 @@ int32_t xrdt_op_mlem(xrdt_op *op, const float *y, const float *c, float *x, int3
     if (!y || !c || !x) return fail(ctx, XRDT_ERR_NULL, "y, c and x are required");
     if (iters < 0) return fail(ctx, XRDT_ERR_DIMS, "iters must be >= 0");
     if (flags) return fail(ctx, XRDT_ERR_UNSUPPORTED, "unknown flag bits");
-    cudaStream_t st = ctx->stream;
-    const int K = op->p.nwt;
-    const size_t nfull = (size_t)op->p.nx * op->p.ny * K;
     if (iters == 0) return XRDT_OK;
+    cudaStream_t st = ctx->stream;
+    const size_t nfull = (size_t)op->p.nx * op->p.ny * op->p.nwt;
     const bool hostX = !is_device_ptr(x);
     float *dx = hostX ? op->xfull : x;
     if (hostX) CK(cudaMemcpyAsync(dx, x, sizeof(float) * nfull, cudaMemcpyHostToDevice, st));
-    if (op->v.nv > 0) {
-        const float *dy, *dc;
-        if ((rc = view_in(op, y, op->rays, op->ray_a, &dy))) return rc;
-        if ((rc = view_in(op, c, op->rays, op->ray_b, &dc))) return rc;
-        if ((rc = ensure_sens(op))) return rc;
-        {
-            ProfScope ps(ctx, XRDT_KERNEL_VOX_UPDATE);
-            CK(launch_vox_gather(op->v, dx, op->xc, op->xd, st, &ctx->launches));
-        }
-        const void *key[2] = {dy, dc};
-        if (!op->mlem_exec || op->mlem_key[0] != key[0] || op->mlem_key[1] != key[1]) {
-            if (op->mlem_exec) {
-                cudaGraphExecDestroy(op->mlem_exec);
-                op->mlem_exec = nullptr;
-            }
-            cudaGraph_t graph;
-            CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-            int64_t dummy = 0;
-            cudaError_t le = launch_vox_forward(op->v, op->xd, nullptr, dy, dc, op->what, st, &dummy);
-            if (le == cudaSuccess) le = launch_vox_adjoint(op->v, op->what, op->part, op->groups, st, &dummy);
-            if (le == cudaSuccess)
-                le = launch_vox_reduce(op->v, op->part, op->groups, 1, op->sens, op->xc, op->xd, nullptr, st, &dummy);
-            cudaError_t ce = cudaStreamEndCapture(st, &graph);
-            if (le != cudaSuccess) {
-                if (ce == cudaSuccess) cudaGraphDestroy(graph);
-                cudaGetLastError();
-                return fail(ctx, XRDT_ERR_CUDA, fmt("MLEM capture: %s", cudaGetErrorString(le)));
-            }
-            CK(ce);
-            cudaError_t ie = cudaGraphInstantiate(&op->mlem_exec, graph, 0);
-            cudaGraphDestroy(graph);
-            CK(ie);
-            op->mlem_key[0] = key[0];
-            op->mlem_key[1] = key[1];
-        }
-        {
-            ProfScope ps(ctx, XRDT_KERNEL_VOX_FORWARD);   // the whole iteration (three kernels)
-            for (int it = 0; it < iters; it++) CK(cudaGraphLaunch(op->mlem_exec, st));
-        }
-        ctx->launches += 3 * (int64_t)iters;
-        // empty voxels have no sensitivity: the update sets them to 0
-        CK(cudaMemsetAsync(dx, 0, sizeof(float) * nfull, st));
-        ProfScope ps(ctx, XRDT_KERNEL_VOX_UPDATE);
-        CK(launch_vox_scatter(op->v, op->xc, dx, st, &ctx->launches));
-    } else {
-        CK(cudaMemsetAsync(dx, 0, sizeof(float) * nfull, st));
-    }
+    const float *dy, *dc;
+    Plan *pl;
+    if ((rc = view_in(op, y, op->rays, op->ray_a, &dy)) || (rc = view_in(op, c, op->rays, op->ray_b, &dc)) ||
+        (rc = op_plan(op, &pl)))
+        return rc;
+    if ((rc = plan_mlem(pl, &dy, &dc, &dx, iters))) return rc;
     if (hostX) CK(cudaMemcpyAsync(x, dx, sizeof(float) * nfull, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    return XRDT_OK;
+}
+
+} // extern "C"
+
+// ---- batches of operators ---------------------------------------------------
+
+struct xrdt_batch {
+    xrdt_ctx *ctx = nullptr;
+    Plan *plan = nullptr;
+};
+
+namespace {
+
+int batch_arrays(xrdt_batch *b, const void *const *a, const char *what)
+{
+    xrdt_ctx *ctx = b->ctx;
+    if (!a) return fail(ctx, XRDT_ERR_NULL, fmt("the %s array is NULL", what));
+    for (size_t i = 0; i < b->plan->ops.size(); i++) {
+        if (!a[i]) return fail(ctx, XRDT_ERR_NULL, fmt("%s[%zu] is NULL", what, i));
+        if (!is_device_ptr(a[i]))
+            return fail(ctx, XRDT_ERR_UNSUPPORTED, fmt("%s[%zu] must be device memory", what, i));
+    }
+    return XRDT_OK;
+}
+
+int batch_begin(xrdt_batch *b)
+{
+    if (!b || !b->ctx || !b->plan) return XRDT_ERR_NULL;
+    xrdt_ctx *ctx = b->ctx;
+    ctx->err.clear();
+    CK(cudaSetDevice(ctx->device));
+    return XRDT_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int32_t xrdt_batch_create(xrdt_ctx *ctx, xrdt_op *const *ops, int32_t n, xrdt_batch **out)
+{
+    if (!ctx || !out) return XRDT_ERR_NULL;
+    *out = nullptr;
+    ctx->err.clear();
+    if (!ops || n < 1) return fail(ctx, XRDT_ERR_DIMS, "a batch needs at least one operator");
+    for (int i = 0; i < n; i++) {
+        if (!ops[i]) return fail(ctx, XRDT_ERR_NULL, fmt("operator %d is NULL", i));
+        if (ops[i]->ctx != ctx) return fail(ctx, XRDT_ERR_INPUT, fmt("operator %d belongs to another context", i));
+        for (int j = 0; j < i; j++)
+            if (ops[j] == ops[i]) return fail(ctx, XRDT_ERR_INPUT, fmt("operator %d appears twice", i));
+    }
+    CK(cudaSetDevice(ctx->device));
+    xrdt_batch *b = new xrdt_batch();
+    b->ctx = ctx;
+    int rc = plan_create(ctx, ops, n, &b->plan);
+    if (rc) {
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return XRDT_OK;
+}
+
+int32_t xrdt_batch_destroy(xrdt_batch *b)
+{
+    if (!b) return XRDT_ERR_NULL;
+    if (b->ctx) {
+        cudaSetDevice(b->ctx->device);
+        cudaStreamSynchronize(b->ctx->stream);
+    }
+    plan_free(b->plan);
+    delete b;
+    return XRDT_OK;
+}
+
+int32_t xrdt_batch_forward(xrdt_batch *b, const float *const *x, float *const *y, uint32_t flags)
+{
+    int rc = batch_begin(b);
+    if (rc) return rc;
+    xrdt_ctx *ctx = b->ctx;
+    if (flags) return fail(ctx, XRDT_ERR_UNSUPPORTED, "unknown flag bits");
+    if ((rc = batch_arrays(b, (const void *const *)x, "x")) || (rc = batch_arrays(b, (const void *const *)y, "y")))
+        return rc;
+    if ((rc = plan_forward(b->plan, x, y))) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return XRDT_OK;
+}
+
+int32_t xrdt_batch_adjoint(xrdt_batch *b, const float *const *w, float *const *g, uint32_t flags)
+{
+    int rc = batch_begin(b);
+    if (rc) return rc;
+    xrdt_ctx *ctx = b->ctx;
+    if (flags) return fail(ctx, XRDT_ERR_UNSUPPORTED, "unknown flag bits");
+    if ((rc = batch_arrays(b, (const void *const *)w, "w")) || (rc = batch_arrays(b, (const void *const *)g, "g")))
+        return rc;
+    if ((rc = plan_adjoint(b->plan, w, g))) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return XRDT_OK;
+}
+
+int32_t xrdt_batch_mlem(xrdt_batch *b, const float *const *y, const float *const *c, float *const *x, int32_t iters,
+                        uint32_t flags)
+{
+    int rc = batch_begin(b);
+    if (rc) return rc;
+    xrdt_ctx *ctx = b->ctx;
+    if (flags) return fail(ctx, XRDT_ERR_UNSUPPORTED, "unknown flag bits");
+    if (iters < 0) return fail(ctx, XRDT_ERR_DIMS, "iters must be >= 0");
+    if ((rc = batch_arrays(b, (const void *const *)y, "y")) || (rc = batch_arrays(b, (const void *const *)c, "c")) ||
+        (rc = batch_arrays(b, (const void *const *)x, "x")))
+        return rc;
+    if ((rc = plan_mlem(b->plan, y, c, x, iters))) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return XRDT_OK;
+}
+
+int32_t xrdt_batch_tune(xrdt_batch *b, int32_t *adj_warps, int64_t *adj_tiles, int32_t *fwd_grid, int32_t *adj_grid)
+{
+    int rc = batch_begin(b);
+    if (rc) return rc;
+    xrdt_ctx *ctx = b->ctx;
+    if ((rc = plan_tune(b->plan))) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (adj_warps) *adj_warps = b->plan->adj_warps;
+    if (adj_tiles) *adj_tiles = plan_total(b->plan, 1);
+    if (fwd_grid) *fwd_grid = b->plan->fwd_grid;
+    if (adj_grid) *adj_grid = b->plan->adj_grid;
     return XRDT_OK;
 }
 

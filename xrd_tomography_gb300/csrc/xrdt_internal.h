@@ -168,23 +168,55 @@ cudaError_t launch_compact_voxels(const DevProblem &P, const int32_t *seg, PrepB
                                   int64_t *launches);
 cudaError_t launch_pair_table(const DevProblem &P, const SrcGeom *sg, PairRec *out, cudaStream_t s,
                               int64_t *launches);
-// Opts the operator kernels in to max_smem bytes of dynamic shared memory.
+
+// One problem of an operator batch as the kernels read it (device memory):
+// its tables, its adjoint split and its buffers.
+struct VoxJob {
+    VoxOp op;
+    F32Consts c;
+    int E;                     // source bins in the spectrum windows
+    int groups;                // adjoint pair groups (rows of part)
+    int ppg;                   // pairs per group
+    int chunk_blocks;          // adjoint blocks along the voxel chunks
+    float *xd, *xc;            // [nv][nwt] unknowns times dq, unknowns
+    float *y;                  // [rays] forward output
+    const float *ymeas, *cbg;  // [rays] MLEM counts and background
+    float *what;               // [pairs][E] per-energy weights
+    float *part;               // [groups][nv][nwt] adjoint partial sums
+    double *sens;              // [nv][nwt] sensitivity
+    float *g;                  // [nx*ny*nwt] adjoint output
+    const float *w;            // [rays] adjoint weights
+    const float *xfull;        // [nx*ny*nwt] coefficients to gather
+    float *xout;               // [nx*ny*nwt] coefficients to scatter to
+    int pad;
+};
+// Kernel argument of the batched operator kernels.  off holds five prefix
+// sums over the n jobs, each of n + 1 entries: 0 forward items (pairs),
+// 1 adjoint items (chunk blocks x groups), 2 unknowns (nv*nwt), 3 full-grid
+// entries (nx*ny*nwt), 4 per-energy weights (pairs*E).
+struct VoxBatch {
+    const VoxJob *jobs;
+    const int64_t *off;
+    unsigned long long *counters;   // [2] work counters of the two persistent kernels
+    int n;
+    int adj_warps;
+};
+// Opts the operator kernels in to max_smem bytes of shared memory per block.
 cudaError_t vox_set_attributes(int max_smem);
 size_t vox_fwd_static_smem();
+size_t vox_adj_static_smem();
 size_t vox_fwd_smem(const DevProblem &P);
-int vox_adj_warps(int K);
 size_t vox_adj_smem(const DevProblem &P, int warps);
-int vox_adj_groups(const VoxOp &op, int sm_count);
-// y = Av x (what == NULL), or the MLEM per-energy weights of y/(Av x + c).
-cudaError_t launch_vox_forward(const VoxOp &op, const float *xd, float *y, const float *ymeas, const float *cbg,
-                               float *what, cudaStream_t s, int64_t *launches);
-cudaError_t launch_vox_wtab(const VoxOp &op, const float *w, float *what, cudaStream_t s, int64_t *launches);
-cudaError_t launch_vox_adjoint(const VoxOp &op, const float *what, float *part, int groups, cudaStream_t s,
+int vox_fwd_blocks_per_sm(size_t smem);
+int vox_adj_blocks_per_sm(int warps, size_t smem);
+// Persistent kernels: grid blocks take items until the counter passes the total.
+cudaError_t launch_vox_forward(const VoxBatch &B, bool mlem, int grid, size_t smem, cudaStream_t s,
                                int64_t *launches);
-cudaError_t launch_vox_reduce(const VoxOp &op, const float *part, int groups, int mode, double *sens, float *xc,
-                              float *xd, float *g, cudaStream_t s, int64_t *launches);
-cudaError_t launch_vox_gather(const VoxOp &op, const float *x, float *xc, float *xd, cudaStream_t s,
-                              int64_t *launches);
-cudaError_t launch_vox_scatter(const VoxOp &op, const float *xc, float *x, cudaStream_t s, int64_t *launches);
+cudaError_t launch_vox_adjoint(const VoxBatch &B, int grid, size_t smem, cudaStream_t s, int64_t *launches);
+// Element-wise kernels over the concatenated ranges (total = the last offset).
+cudaError_t launch_vox_wtab(const VoxBatch &B, int64_t total, bool ones, cudaStream_t s, int64_t *launches);
+cudaError_t launch_vox_reduce(const VoxBatch &B, int64_t total, int mode, cudaStream_t s, int64_t *launches);
+cudaError_t launch_vox_gather(const VoxBatch &B, int64_t total, bool with_xc, cudaStream_t s, int64_t *launches);
+cudaError_t launch_vox_scatter(const VoxBatch &B, int64_t total, cudaStream_t s, int64_t *launches);
 
 } // namespace xrdt

@@ -251,3 +251,27 @@ def vox_truth(inp: Inputs) -> np.ndarray:
     dens = a2[on] / np.median(a2[on]) if on.any() else a2[on]
     x[on] = coarse[seg[on] - 1] * dens[:, None]
     return x.astype(np.float32).reshape(-1)
+
+
+def batch_inputs(n: int, seed: int = SEED_BASE + 3, side=(64, 384), views=(60, 360), px=(128, 768),
+                 nwt: int = 32, nqf: int = 128, nrg: int = 64, n_mat: int = 4) -> list:
+    """Independent problems of the batched workload: phantom sides, view
+    counts and detector widths drawn uniformly from the given ranges (the
+    batched configuration uses 64-384 voxels, 60-360 views, 128-768 px),
+    a q grid of nqf fine bins, nrg energy bins, 2 mm voxels, and a fan
+    scanner that keeps sources and detectors outside the phantom."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        sd = int(rng.integers(side[0], side[1] + 1))
+        nv = int(rng.integers(views[0], views[1] + 1))
+        npx = int(rng.integers(px[0], px[1] + 1))
+        p = _base(sd, sd, nv, npx, 1, nrg, nrg, (20.0, 80.0), (20.0, 80.0), 5,
+                  nwt, nqf, n_mat, 64, 64, (0.5, 4.0), 0.05)
+        vox_mm = 2.0
+        r_src = 1.5 * sd * vox_mm
+        r_det = 1.1 * sd * vox_mm
+        col = 2.6 * sd * vox_mm / npx
+        p = scanner(p, vox_mm, r_src, r_det, col)
+        out.append(make_inputs(p, seed * 1000 + i, n_ellipses=6))
+    return out
