@@ -226,6 +226,15 @@ def run_reference(args):
 
 # ---- GPU leg -------------------------------------------------------------------
 
+def plain_wave(dev) -> int:
+    """Rays for timing the FP64 kernel at the reference's launch shape: 16
+    one-warp blocks per SM, enough to keep every SM's FP64 pipe busy, so
+    that the sample's rate is the kernel's full-GPU rate (a few blocks would
+    leave most SMs idle and understate it)."""
+    import torch
+    return 16 * torch.cuda.get_device_properties(dev).multi_processor_count
+
+
 def hbm_peak_gbs():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -273,7 +282,7 @@ def mlem_stored_bench(xt, synth, ctx, stream, dev, iters=200):
                          "traffic": None, "algorithmic_bytes_per_iter": traffic, "peak_source": src}}
 
 
-def vox_mlem_bench(xt, synth, ctx, stream, dev, iters=50, plain_rays=16):
+def vox_mlem_bench(xt, synth, ctx, stream, dev, iters=50):
     """Per-voxel-coefficient MLEM (main.m:162-176 with one coarse-q pattern per
     voxel) on the 128x128 workload: counts drawn from a seeded ground truth
     (Poisson, peak 1e3 per pixel-bin, flat 5% incoherent bias), 50 iterations
@@ -317,10 +326,9 @@ def vox_mlem_bench(xt, synth, ctx, stream, dev, iters=50, plain_rays=16):
     ctx.set_profiling(False)
     # plain FP64 path on a ray subset
     rng = np.random.default_rng(3)
-    sub = np.sort(rng.choice(p.rays, plain_rays, replace=False))
+    sub = np.sort(rng.choice(p.rays, min(p.rays, plain_wave(dev)), replace=False))
     xh = x.cpu().numpy()
     wh = w[torch.from_numpy(sub).to(dev)].cpu().numpy()
-    op.forward_rays_fp64(xh, sub[:2])
     t0 = time.perf_counter()
     op.forward_rays_fp64(xh, sub)
     t1 = time.perf_counter()
@@ -337,6 +345,77 @@ def vox_mlem_bench(xt, synth, ctx, stream, dev, iters=50, plain_rays=16):
             "plain_fp64_ms_per_iter": plain_iter_ms,
             "plain_fp64_sample": f"forward and adjoint on {sub.size} of {p.rays} rays, scaled to all rays",
             "speedup_vs_plain_fp64": plain_iter_ms / ms_iter}
+
+
+def batch_mlem_bench(xt, synth, ctx, stream, dev, n=8, iters=10):
+    """Batched MLEM over phantoms of uneven size (the batched configuration's
+    generator with its ranges scaled down so that the section takes seconds:
+    sides 64-160 voxels, 24-64 views, 64-160 px, 64 energy bins, 128 fine q
+    bins, 32 coefficients per voxel): one persistent launch per kernel and
+    one CUDA graph per iteration for the whole batch, against the same
+    operators run one after another and the plain FP64 kernel."""
+    import torch
+    inps = synth.batch_inputs(n, side=(64, 160), views=(24, 64), px=(64, 160))
+    ops = [xt.Operator(i.problem, i.spectrum, i.seg, i.a1, i.a2, ctx=ctx) for i in inps]
+    ys, cs, x0 = [], [], []
+    for k, (inp, op) in enumerate(zip(inps, ops)):
+        xtrue = torch.from_numpy(synth.vox_truth(inp)).to(dev)
+        ybar = op.forward(xtrue, torch.empty(inp.problem.rays, device=dev)).double()
+        scale = 1e3 / max(float(ybar.max()), 1e-30)
+        c = torch.full((inp.problem.rays,), 0.05 * float(ybar.mean()) * scale, dtype=torch.float32, device=dev)
+        gen = torch.Generator(device="cpu").manual_seed(100 + k)
+        ys.append(torch.poisson((ybar * scale + c.double()).cpu(), generator=gen).float().to(dev))
+        cs.append(c)
+        on = torch.from_numpy(np.repeat(np.asarray(inp.seg).reshape(-1) > 0, inp.problem.nwt)).to(dev)
+        x0.append(torch.where(on, 1.0, 0.0).float())
+    batch = xt.Batch(ops, ctx=ctx)
+    warps, tiles, fgrid, agrid = batch.tune()
+    xb = [x.clone() for x in x0]
+    batch.mlem(ys, cs, xb, 1)                          # sensitivity and graph capture
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    torch.cuda.synchronize(dev)
+    ev[0].record(stream)
+    batch.mlem(ys, cs, xb, iters)
+    ev[1].record(stream)
+    torch.cuda.synchronize(dev)
+    ms_batch = ev[0].elapsed_time(ev[1]) / iters
+    # the same operators one after another
+    ms_seq = 0.0
+    for k, op in enumerate(ops):
+        x = x0[k].clone()
+        op.mlem(ys[k], cs[k], x, 1)
+        torch.cuda.synchronize(dev)
+        ev[0].record(stream)
+        op.mlem(ys[k], cs[k], x, iters)
+        ev[1].record(stream)
+        torch.cuda.synchronize(dev)
+        ms_seq += ev[0].elapsed_time(ev[1]) / iters
+    # plain FP64 forward + adjoint on a few rays of every problem
+    plain_ms = 0.0
+    rng = np.random.default_rng(9)
+    for k, (inp, op) in enumerate(zip(inps, ops)):
+        sub = np.sort(rng.choice(inp.problem.rays, min(inp.problem.rays, plain_wave(dev)), replace=False))
+        xh = x0[k].cpu().numpy()
+        wh = np.ones(sub.size, np.float32)
+        t0 = time.perf_counter()
+        op.forward_rays_fp64(xh, sub)
+        op.adjoint_rays_fp64(wh, sub)
+        plain_ms += (time.perf_counter() - t0) * 1e3 * inp.problem.rays / sub.size
+    pv = sum(int((i.seg > 0).sum()) * i.problem.n_src * i.problem.n_col * i.problem.n_row for i in inps)
+    sizes = [f"{i.problem.nx}^2/{i.problem.n_src}v/{i.problem.n_col}px" for i in inps]
+    batch.close()
+    for op in ops:
+        op.close()
+    return {"workload": f"{n} phantoms ({', '.join(sizes)}), 64 energy bins, 32 coefficients per voxel, "
+                        f"{iters} MLEM iterations, one graph per iteration",
+            "ms_per_iter": ms_batch, "iter_per_s": 1e3 / ms_batch,
+            "pair_voxels_per_iter": pv, "g_pair_voxels_per_s": pv / (ms_batch * 1e-3) / 1e9,
+            "sequential_ms_per_iter": ms_seq, "batching_speedup": ms_seq / ms_batch,
+            "plain_fp64_ms_per_iter": plain_ms, "speedup_vs_plain_fp64": plain_ms / ms_batch,
+            "plain_fp64_sample": f"forward and adjoint on {plain_wave(dev)} rays of every problem (16 blocks per SM), "
+                                 f"scaled to all rays",
+            "autotuned": {"adjoint_warps": warps, "adjoint_tiles": tiles, "forward_grid": fgrid,
+                          "adjoint_grid": agrid}}
 
 
 def run_ours(args):
@@ -437,6 +516,7 @@ def run_ours(args):
     if rank == 0 and not args.no_baselines:
         line["mlem"] = mlem_stored_bench(xt, synth, ctx, stream, dev)
         line["vox_mlem"] = vox_mlem_bench(xt, synth, ctx, stream, dev)
+        line["batch_mlem"] = batch_mlem_bench(xt, synth, ctx, stream, dev)
     if rank == 0:
         # roofline of the dominant kernel: the forward kernel's exponentials
         # (Gaussian q terms, attenuation and Compton factors) on the SFU
@@ -460,8 +540,7 @@ def run_ours(args):
         if not args.no_baselines:
             # plain FP64 kernel at the reference launch shape, on a ray subset
             rng = np.random.default_rng(2)
-            sub = rng.choice(p.rays, 32, replace=False)
-            xt.forward_rays(p, sub[:4], *host, *tables, plain=True, ctx=ctx)
+            sub = rng.choice(p.rays, min(p.rays, plain_wave(dev)), replace=False)
             t0 = time.perf_counter()
             xt.forward_rays(p, sub, *host, *tables, plain=True, ctx=ctx)
             dt = time.perf_counter() - t0
