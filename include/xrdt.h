@@ -149,7 +149,8 @@ int64_t xrdt_ctx_launch_count(const xrdt_ctx *ctx);
 #define XRDT_KERNEL_VOX_FORWARD 7  /* per-voxel operator: forward (and MLEM ratios)  */
 #define XRDT_KERNEL_VOX_ADJOINT 8  /* per-voxel operator: adjoint                    */
 #define XRDT_KERNEL_VOX_UPDATE  9  /* per-voxel operator: sums, update, staging      */
-#define XRDT_KERNEL_COUNT       10
+#define XRDT_KERNEL_CT          10 /* transmission sinogram                          */
+#define XRDT_KERNEL_COUNT       11
 /* With profiling on, every launch is bracketed by CUDA events on the
  * context's stream and the forward kernel counts the exponentials it
  * evaluates.  Off by default; turning it on or off clears the statistics. */
@@ -198,6 +199,23 @@ int32_t xrdt_forward_rays(xrdt_ctx *ctx, const xrdt_problem *p,
                           uint32_t flags);
 
 /* ---- MLEM with an explicit model matrix (main.m:154-176) --------------- */
+/* ---- transmission CT sinogram ---------------------------------------
+ * The reference declares a transmitted-photon output and its no-phantom
+ * gain (Tphotons, gain0) and the launches that would fill them,
+ * integrate_src2det and polychromatic_src2det, only in comments
+ * (Forward_XRD.cu:125-140,169-199,263-276).  Here, per (source, pixel,
+ * detector energy bin) in the Nphotons layout [SRC, COL, ROW, NRG]:
+ *   Tphotons = sum_{e in window(nrg)} RF[e,nrg] exp(-(A1/ein^3 + A2/KN(ein)))
+ *   gain0    = sum_{e in window(nrg)} RF[e,nrg]
+ * with (A1, A2) the line integral of the (a1, a2) map along the source ->
+ * pixel chord clipped to [0,NX] x [0,NY], sampled every DQ from the entry
+ * point as attenuator.cu:9-109 samples.  -log(Tphotons / gain0) is the
+ * energy-resolved CT sinogram.  Spectrum, windows and attenuation model as
+ * xrdt_forward. */
+int32_t xrdt_ct_sinogram(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum,
+                         const float *a1, const float *a2, float *Tphotons,
+                         float *gain0, uint32_t flags);
+
 /* Runs `iters` iterations of
  *     x <- x .* (A' * (y ./ (A*x + c + 1e-20))) ./ (sum(A,1)' + 1e-7)
  *     x(~isfinite(x)) = 0;  x(x < 0) = 0

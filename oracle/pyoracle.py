@@ -45,6 +45,7 @@ def lib():
         _lib = ctypes.CDLL(LIB)
         _lib.xrdt_oracle_forward_rays.restype = ctypes.c_int32
         _lib.xrdt_oracle_vox_rays.restype = ctypes.c_int32
+        _lib.xrdt_oracle_ct_rays.restype = ctypes.c_int32
         _lib.xrdt_oracle_attenuator.restype = ctypes.c_int64
         _lib.xrdt_oracle_get_intersection.restype = ctypes.c_int32
     return _lib
@@ -120,6 +121,19 @@ def vox_rays(inp, rays, x=None, w=None, threads=0):
     if rc != 0:
         raise ValueError(f"oracle rejected the input ({rc})")
     return y, (None if g is None else g.reshape(p.ny, p.nx, p.nwt))
+
+
+def ct_rays(inp, rays, threads=0):
+    """(Tphotons, gain0) of the CT sinogram for the listed rays, in FP64."""
+    p = inp.problem
+    rays = np.ascontiguousarray(rays, np.int64)
+    T = np.zeros(rays.size)
+    G = np.zeros(rays.size)
+    keep = [np.ascontiguousarray(a, np.float32) for a in (inp.spectrum, inp.a1, inp.a2)]
+    lib().xrdt_oracle_ct_rays(ctypes.byref(p), keep[0].ctypes.data_as(_f), keep[1].ctypes.data_as(_f),
+                              keep[2].ctypes.data_as(_f), rays.ctypes.data_as(_i64), ctypes.c_int64(rays.size),
+                              T.ctypes.data_as(_d), G.ctypes.data_as(_d), ctypes.c_int32(threads))
+    return T, G
 
 
 def ref_forward_rays(inp, rays, threads=0):

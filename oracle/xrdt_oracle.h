@@ -66,6 +66,11 @@ int32_t xrdt_oracle_vox_rays(const xrdt_problem *p, const float *spectrum, const
                              const int64_t *rays, int64_t n_rays, double *y_out, double *g_out,
                              int32_t n_threads);
 
+/* Transmission through the map per listed ray (Nphotons index) and the
+ * same without the phantom: Tphotons and gain0 of the CT sinogram. */
+int32_t xrdt_oracle_ct_rays(const xrdt_problem *p, const float *spectrum, const float *a1, const float *a2,
+                            const int64_t *rays, int64_t n_rays, double *T_out, double *G_out, int32_t n_threads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -163,3 +163,24 @@ def test_forward_matches_reference_kernel_fresh_inputs(oracle_lib):
     assert max_rel_err(N, Nr, floor=0) < 1e-10
     assert max_rel_err(C, Cr, floor=0) < 1e-10
     assert max_rel_err(A, Ar, floor=1e-12) < 1e-10
+
+
+def test_oracle_ct_limits(oracle_lib):
+    """CT restatement: without a phantom every channel transmits its whole
+    spectrum weight; doubling the attenuation lowers every transmission."""
+    from xrd_tomography_gb300 import synth
+    inp = synth.make_inputs(synth.tiny_problem(), 4)
+    rays = np.arange(inp.problem.rays)
+    T, G = oracle_lib.ct_rays(inp, rays)
+    z = synth.make_inputs(synth.tiny_problem(), 4)
+    z.a1 = np.zeros_like(z.a1)
+    z.a2 = np.zeros_like(z.a2)
+    T0, G0 = oracle_lib.ct_rays(z, rays)
+    np.testing.assert_array_equal(T0, G0)
+    np.testing.assert_array_equal(G, G0)
+    d = synth.make_inputs(synth.tiny_problem(), 4)
+    d.a1 = 2 * d.a1
+    d.a2 = 2 * d.a2
+    T2, _ = oracle_lib.ct_rays(d, rays)
+    hit = T < G
+    assert hit.any() and np.all(T2[hit] < T[hit]) and np.all(T2[~hit] == T[~hit])

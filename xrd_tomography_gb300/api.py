@@ -27,7 +27,7 @@ FWD_PLAIN_FP64 = 0x1
 FWD_NO_SYNC = 0x2
 OP_PLAIN_FP64 = 0x1
 (KERNEL_PREP_MAP, KERNEL_PREP_VOXELS, KERNEL_SRC_ATTEN, KERNEL_FORWARD, KERNEL_PLAIN, KERNEL_GATHER,
- KERNEL_MLEM, KERNEL_VOX_FORWARD, KERNEL_VOX_ADJOINT, KERNEL_VOX_UPDATE) = range(10)
+ KERNEL_MLEM, KERNEL_VOX_FORWARD, KERNEL_VOX_ADJOINT, KERNEL_VOX_UPDATE, KERNEL_CT) = range(11)
 
 _P = ctypes.POINTER(Problem)
 _vp = ctypes.c_void_p
@@ -61,6 +61,7 @@ SIGNATURES = {
     "xrdt_op_adjoint": (ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_uint32]),
     "xrdt_op_mlem": (ctypes.c_int32, [_vp, _vp, _vp, _vp, ctypes.c_int32, ctypes.c_uint32]),
     "xrdt_op_forward_rays": (ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_int64, _vp, ctypes.c_uint32]),
+    "xrdt_ct_sinogram": (ctypes.c_int32, [_vp, _P, _vp, _vp, _vp, _vp, _vp, ctypes.c_uint32]),
     "xrdt_batch_create": (ctypes.c_int32, [_vp, _vp, ctypes.c_int32, ctypes.POINTER(_vp)]),
     "xrdt_batch_destroy": (ctypes.c_int32, [_vp]),
     "xrdt_batch_forward": (ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_uint32]),
@@ -237,6 +238,19 @@ def forward_rays(p: Problem, rays, spectrum, Ifine, seg, a1, a2, S2, q_min, q_ma
                                  A.ctypes.data if A is not None else None, FWD_PLAIN_FP64 if plain else 0)
     _check(rc, ctx.h)
     return N, C, A
+
+
+def ct_sinogram(p: Problem, spectrum, a1, a2, Tphotons=None, gain0=None, ctx: Context | None = None):
+    """xrdt_ct_sinogram: (Tphotons, gain0) per (source, pixel, energy bin) in
+    the Nphotons layout; -log(Tphotons / gain0) is the CT sinogram."""
+    ctx = ctx or default_context()
+    if Tphotons is None:
+        Tphotons = np.empty(p.rays, np.float32)
+    if gain0 is None:
+        gain0 = np.empty(p.rays, np.float32)
+    ptrs = [_ptr(a, np.float32) for a in (spectrum, a1, a2, Tphotons, gain0)]
+    _check(lib().xrdt_ct_sinogram(ctx.h, ctypes.byref(p), *[q[0] for q in ptrs], 0), ctx.h)
+    return ptrs[3][1], ptrs[4][1]
 
 
 def mlem_matrix(A, y, c, x0, iters: int, K: int | None = None, ctx: Context | None = None):

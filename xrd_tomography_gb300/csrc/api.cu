@@ -785,6 +785,68 @@ int32_t xrdt_forward_rays(xrdt_ctx *ctx, const xrdt_problem *p, const float *spe
                         rays ? rays : &none, n_rays, Nphotons, Cphotons, A_rows, flags);
 }
 
+int32_t xrdt_ct_sinogram(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, const float *a1, const float *a2,
+                         float *Tphotons, float *gain0, uint32_t flags)
+{
+    if (!ctx) return XRDT_ERR_NULL;
+    ctx->err.clear();
+    if (!p || !spectrum || !a1 || !a2 || !Tphotons || !gain0)
+        return fail(ctx, XRDT_ERR_NULL, "a required array pointer is NULL");
+    int rc = xrdt_problem_validate(p);
+    if (rc) return fail(ctx, rc, fmt("problem rejected: %s", xrdt_status_string(rc)));
+    if (flags) return fail(ctx, XRDT_ERR_UNSUPPORTED, "unknown flag bits");
+    DevProblem P;
+    std::string err;
+    build_dev_problem(p, 0.f, 1.f, 0.f, 1.f, &P, &err);
+    P.nq = 0;   // no Compton table
+    P.na = 0;
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const int64_t nvox = (int64_t)p->nx * p->ny;
+    const int64_t rays = xrdt_problem_rays(p);
+    const void *d_spec, *d_a1, *d_a2;
+    if ((rc = stage_in(ctx, S_SPEC, spectrum, sizeof(float) * p->nrg_src * p->nrg_det, &d_spec))) return rc;
+    if ((rc = stage_in(ctx, S_A1, a1, sizeof(float) * nvox, &d_a1))) return rc;
+    if ((rc = stage_in(ctx, S_A2, a2, sizeof(float) * nvox, &d_a2))) return rc;
+    const bool hostT = !is_device_ptr(Tphotons), hostG = !is_device_ptr(gain0);
+    float *dT = Tphotons, *dG = gain0;
+    void *tmp;
+    if (hostT) { if ((rc = get_buf(ctx, S_N, sizeof(float) * rays, &tmp))) return rc; dT = (float *)tmp; }
+    if (hostG) { if ((rc = get_buf(ctx, S_C, sizeof(float) * rays, &tmp))) return rc; dG = (float *)tmp; }
+    std::vector<float> hspec((size_t)p->nrg_src * p->nrg_det);
+    CK(cudaMemcpy(hspec.data(), spectrum, sizeof(float) * hspec.size(), cudaMemcpyDefault));
+    HostTables ht;
+    build_host_tables(p, P, hspec.data(), &ht);
+    std::vector<SrcGeom> hsg(p->n_src);
+    for (int s = 0; s < p->n_src; s++) src_geom(p, s, &hsg[s]);
+    void *d_srcg, *d_energy, *d_rf, *d_wlo;
+    if ((rc = get_buf(ctx, S_SRCG, sizeof(SrcGeom) * p->n_src, &d_srcg))) return rc;
+    if ((rc = get_buf(ctx, S_ENERGY, sizeof(EnergyRow) * ht.energy.size(), &d_energy))) return rc;
+    if ((rc = get_buf(ctx, S_RFWIN, sizeof(float) * ht.rf_win.size(), &d_rf))) return rc;
+    if ((rc = get_buf(ctx, S_WINLO, sizeof(int) * ht.win_lo.size(), &d_wlo))) return rc;
+    CK(cudaMemcpyAsync(d_srcg, hsg.data(), sizeof(SrcGeom) * p->n_src, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_energy, ht.energy.data(), sizeof(EnergyRow) * ht.energy.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_rf, ht.rf_win.data(), sizeof(float) * ht.rf_win.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_wlo, ht.win_lo.data(), sizeof(int) * ht.win_lo.size(), cudaMemcpyHostToDevice, st));
+    PrepBuffers B;
+    memset(&B, 0, sizeof B);
+    if ((rc = get_buf(ctx, S_CELLS, sizeof(float4) * 2 * (size_t)(p->nx + 1) * (p->ny + 1), &tmp))) return rc;
+    B.cells = (float4 *)tmp;
+    {
+        ProfScope ps(ctx, XRDT_KERNEL_PREP_MAP);
+        CK(launch_prep_map(P, (const float *)d_a1, (const float *)d_a2, nullptr, B, st, &ctx->launches));
+    }
+    {
+        ProfScope ps(ctx, XRDT_KERNEL_CT);
+        CK(launch_ct_sinogram(P, (const SrcGeom *)d_srcg, B.cells, (const EnergyRow *)d_energy, (const float *)d_rf,
+                              (const int *)d_wlo, dT, dG, st, &ctx->launches));
+    }
+    if (hostT) CK(cudaMemcpyAsync(Tphotons, dT, sizeof(float) * rays, cudaMemcpyDeviceToHost, st));
+    if (hostG) CK(cudaMemcpyAsync(gain0, dG, sizeof(float) * rays, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return XRDT_OK;
+}
+
 int32_t xrdt_mlem_matrix(xrdt_ctx *ctx, const float *A, int64_t rays, int32_t K, const float *y, const float *c,
                          float *x, int32_t iters, uint32_t flags)
 {

@@ -97,6 +97,12 @@ cudaError_t launch_plain_vox(const DevProblem &P, const SrcGeom *d_src, const fl
                              int64_t n_rays, const float *x, float *y, const float *w, double *g, cudaStream_t s,
                              int64_t *launches);
 
+// k_ct.cu: transmission through the map per (source, pixel, energy channel)
+// and the same without the phantom, in the Nphotons layout.
+cudaError_t launch_ct_sinogram(const DevProblem &P, const SrcGeom *sg, const float4 *cells, const EnergyRow *energy,
+                               const float *rf_win, const int *win_lo, float *T, float *G0, cudaStream_t s,
+                               int64_t *launches);
+
 // k_prep.cu
 struct PrepBuffers {
     float4 *cells;          // [(ny+1)*(nx+1)*2] bilinear cells
