@@ -3,9 +3,9 @@
 //  * k_build_cells: the (a1,a2) map as bilinear cells.  Replaces Copy2Vector
 //    (Copy2Vector.cu:9-23) and the cudaArray/texture set-up of
 //    Forward_XRD.cu:209-237: cell (ci,cj) holds the bilinear coefficients of
-//    the four texels (ci-1..ci, cj-1..cj) of a zero-bordered map as two
-//    float4, so one sample is two 16-byte loads and three FMAs per component
-//    with no border tests.  Also
+//    the four texels (ci-1..ci, cj-1..cj) of a zero-bordered map, about the
+//    cell centre, as two float4, so one sample is two 16-byte loads and three
+//    packed FMAs with no border tests.  Also
 //    quantises the Compton table to u8 (integrate_diffraction.cu:66-74).
 //  * k_compact_voxels: non-empty voxels in the reference's loop order
 //    (nx outer, ny inner; integrate_diffraction.cu:173-178) and the material
@@ -40,13 +40,15 @@ __global__ void k_build_cells(int nx, int ny, const float *__restrict__ a1, cons
                 v[dj][di][0] = in ? a1[idx] : 0.f;
                 v[dj][di][1] = in ? a2[idx] : 0.f;
             }
-        // bilinear coefficients per component q: f(u,v) = c00 + c10 u + c01 v + c11 u v
+        // bilinear coefficients per component q about the cell centre:
+        // f(u,v) = c00 + c10 u + c01 v + c11 u v for u, v in [-1/2, 1/2]
         float c00[2], c10[2], c01[2], c11[2];
         for (int q = 0; q < 2; q++) {
-            c00[q] = v[0][0][q];
-            c10[q] = v[0][1][q] - v[0][0][q];
-            c01[q] = v[1][0][q] - v[0][0][q];
-            c11[q] = (v[1][1][q] - v[1][0][q]) - (v[0][1][q] - v[0][0][q]);
+            const double f00 = v[0][0][q], f10 = v[0][1][q], f01 = v[1][0][q], f11 = v[1][1][q];
+            c00[q] = (float)(0.25 * ((f00 + f10) + (f01 + f11)));
+            c10[q] = (float)(0.5 * ((f10 - f00) + (f11 - f01)));
+            c01[q] = (float)(0.5 * ((f01 - f00) + (f11 - f10)));
+            c11[q] = (float)((f11 - f01) - (f10 - f00));
         }
         cells[2 * c] = make_float4(c00[0], c00[1], c10[0], c10[1]);
         cells[2 * c + 1] = make_float4(c01[0], c01[1], c11[0], c11[1]);

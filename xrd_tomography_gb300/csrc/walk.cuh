@@ -106,53 +106,51 @@ __device__ __forceinline__ bool walk_setup_f32(const DevProblem &P, const F32Con
     return true;
 }
 
-// One bilinear sample of the cell map at texture coordinates (X+1, Y+1).
-// Cell (ci, cj) holds the bilinear coefficients of the texels (ci-1..ci,
-// cj-1..cj) of the zero-bordered map: f(u,v) = c00 + c10 u + c01 v + c11 u v.
-// The base texel is round(X) instead of floor(X + 0.5): the interpolant is
-// continuous, so any base with weights u, v in [0, 1] gives the same value,
-// and rounding through the float mantissa (adding 1.5 * 2^23) needs no
-// conversion instruction.  Valid for |X| < 2^22; the cell index is clamped
-// for memory safety.
-__device__ __forceinline__ float2 cell_sample(const float4 *__restrict__ cells, int nx, unsigned ncell_m1,
-                                              float X, float Y)
+// One bilinear sample of the cell map at texture coordinates (X+1, Y+1),
+// P = (X, Y).  Cell (ci, cj) holds the coefficients of the texels
+// (ci-1..ci, cj-1..cj) of the zero-bordered map in the frame of the cell
+// centre: f = d00 + d10 u + d01 v + d11 u v with u = X - round(X) and
+// v = Y - round(Y) in [-0.5, 0.5] (k_prep.cu).  The interpolant is
+// continuous, so any base cell whose square holds the point gives the same
+// value, and rounding through the float mantissa (adding 1.5 * 2^23) needs
+// no conversion instruction.  Valid for |X| < 2^22; the cell index is
+// clamped for memory safety.  Both components are evaluated with packed
+// FP32 instructions (two lanes of one register pair: a1 and a2).
+__device__ __forceinline__ float2 cell_sample(const float4 *__restrict__ cells, int nx, unsigned ncell_m1, float2 P)
 {
-    const float tx = X + 12582912.f, ty = Y + 12582912.f;
-    const int ix = __float_as_int(tx) - 0x4B400000, iy = __float_as_int(ty) - 0x4B400000;
-    const float u = (X - (tx - 12582912.f)) + 0.5f;
-    const float v = (Y - (ty - 12582912.f)) + 0.5f;
+    const float2 t = __fadd2_rn(P, make_float2(12582912.f, 12582912.f));
+    const int ix = __float_as_int(t.x) - 0x4B400000, iy = __float_as_int(t.y) - 0x4B400000;
+    const float2 r = __fadd2_rn(t, make_float2(-12582912.f, -12582912.f));   // round(P), exact
+    const float2 d = __ffma2_rn(r, make_float2(-1.f, -1.f), P);               // P - round(P), exact
     const unsigned c = min((unsigned)(ix + 1 + (iy + 1) * (nx + 1)), ncell_m1);
     const float4 c0 = __ldg(cells + 2 * c), c1 = __ldg(cells + 2 * c + 1);
-    return make_float2(fmaf(u, fmaf(v, c1.z, c0.z), fmaf(v, c1.x, c0.x)),
-                       fmaf(u, fmaf(v, c1.w, c0.w), fmaf(v, c1.y, c0.y)));
+    const float2 lo = __ffma2_rn(make_float2(d.y, d.y), make_float2(c1.x, c1.y), make_float2(c0.x, c0.y));
+    const float2 hi = __ffma2_rn(make_float2(d.y, d.y), make_float2(c1.z, c1.w), make_float2(c0.z, c0.w));
+    return __ffma2_rn(make_float2(d.x, d.x), hi, lo);
 }
 
 // Sum of the n samples times DQ; every lane returns the total.  Lane l takes
 // samples l, l+32, l+64, ... two per iteration; the sample index is carried
-// as a float (no int-to-float conversion per sample).
+// as a float (no int-to-float conversion per sample) and the sample point
+// r + k L is formed for x and y in one packed FMA.
 __device__ __forceinline__ float2 walk_coop(const float4 *__restrict__ cells, int nx, int ny,
                                             const WalkSetup &w, float DQ, int lane)
 {
     const unsigned ncell_m1 = (unsigned)((nx + 1) * (ny + 1) - 1);
-    float s1 = 0.f, s2 = 0.f, t1 = 0.f, t2 = 0.f;
+    const float2 L2 = make_float2(w.Lx, w.Ly), R2 = make_float2(w.rx, w.ry);
+    float2 sa = make_float2(0.f, 0.f), sb = make_float2(0.f, 0.f);
     float kf = __int_as_float(0x4B000000 | lane) - 8388608.f;   // (float)lane
     int k = lane;
     for (; k + 32 < w.n; k += 64, kf += 64.f) {
-        const float2 a = cell_sample(cells, nx, ncell_m1, fmaf(w.Lx, kf, w.rx), fmaf(w.Ly, kf, w.ry));
+        const float2 a = cell_sample(cells, nx, ncell_m1, __ffma2_rn(L2, make_float2(kf, kf), R2));
         const float kg = kf + 32.f;
-        const float2 b = cell_sample(cells, nx, ncell_m1, fmaf(w.Lx, kg, w.rx), fmaf(w.Ly, kg, w.ry));
-        s1 += a.x;
-        s2 += a.y;
-        t1 += b.x;
-        t2 += b.y;
+        const float2 b = cell_sample(cells, nx, ncell_m1, __ffma2_rn(L2, make_float2(kg, kg), R2));
+        sa = __fadd2_rn(sa, a);
+        sb = __fadd2_rn(sb, b);
     }
-    if (k < w.n) {
-        const float2 a = cell_sample(cells, nx, ncell_m1, fmaf(w.Lx, kf, w.rx), fmaf(w.Ly, kf, w.ry));
-        s1 += a.x;
-        s2 += a.y;
-    }
-    s1 = warp_sum(s1 + t1);
-    s2 = warp_sum(s2 + t2);
+    if (k < w.n) sa = __fadd2_rn(sa, cell_sample(cells, nx, ncell_m1, __ffma2_rn(L2, make_float2(kf, kf), R2)));
+    const float s1 = warp_sum(sa.x + sb.x);
+    const float s2 = warp_sum(sa.y + sb.y);
     return make_float2(s1 * DQ, s2 * DQ);
 }
 
