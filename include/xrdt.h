@@ -287,7 +287,10 @@ int32_t xrdt_op_adjoint_rays(xrdt_op *op, const float *w, const int64_t *rays,
  * so uneven problems fill the GPU together; each MLEM iteration of the whole
  * batch is one CUDA graph launch.  The adjoint's tile shape (warps per block
  * and tiles per block slot) is chosen by timing candidates on the batch on
- * its first MLEM call or on xrdt_batch_tune.  Arrays are per-problem device
+ * its first MLEM call or on xrdt_batch_tune, and kept in a cache file (one
+ * line per GPU and set of problem sizes; the file is $XRDT_TUNE_CACHE, by
+ * default $XDG_CACHE_HOME/xrdt/tune.txt or $HOME/.cache/xrdt/tune.txt; an
+ * empty XRDT_TUNE_CACHE turns it off).  Arrays are per-problem device
  * pointers in operator order, with each operator's sizes.  A batch uses its
  * operators' buffers: an operator takes part in one call at a time. */
 typedef struct xrdt_batch xrdt_batch;

@@ -22,7 +22,9 @@ def torch_cuda():
 
 
 @pytest.fixture(scope="module")
-def ctx(torch_cuda):
+def ctx(torch_cuda, tmp_path_factory):
+    import os
+    os.environ["XRDT_TUNE_CACHE"] = str(tmp_path_factory.mktemp("tune") / "tune.txt")
     c = xt.Context(0)
     yield c
     c.close()
@@ -68,6 +70,10 @@ def test_batch_matches_single_operators_and_oracle(ctx, torch_cuda, oracle_lib):
     assert max_rel_err(gs[0].cpu().numpy(), g_ref.reshape(-1)) < FAST_RTOL
     warps, tiles, fgrid, agrid = batch.tune()
     assert warps in (1, 2, 4) and tiles >= 1 and fgrid >= 1 and agrid >= 1
+    # a second batch of the same shapes reads the choice from the cache file
+    again = xt.Batch(ops, ctx=ctx)
+    assert again.tune()[:2] == (warps, tiles)
+    again.close()
     batch.close()
     for op in ops:
         op.close()

@@ -8,8 +8,11 @@
 // device; calls convert from and to the full-grid layout [NX*NY][NWT].
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
+#include <sys/stat.h>
 #include <vector>
 
 #include "ctx.h"
@@ -296,6 +299,77 @@ int plan_sens(Plan *pl)
     return XRDT_OK;
 }
 
+// ---- the autotuner's cache on disk ----------------------------------------
+// One line per tuned batch: "<key> <warps> <tiles>".  The key names the GPU
+// and every problem's sizes, so a cached choice is reused only for the same
+// shapes on the same kind of GPU.  XRDT_TUNE_CACHE names the file ("" turns
+// the cache off); by default it is $XDG_CACHE_HOME/xrdt/tune.txt or
+// $HOME/.cache/xrdt/tune.txt.
+
+std::string tune_cache_path()
+{
+    const char *e = getenv("XRDT_TUNE_CACHE");
+    if (e) return std::string(e);
+    const char *x = getenv("XDG_CACHE_HOME");
+    const char *h = getenv("HOME");
+    std::string dir = x && *x ? std::string(x) : (h && *h ? std::string(h) + "/.cache" : std::string());
+    if (dir.empty()) return std::string();
+    mkdir(dir.c_str(), 0755);
+    dir += "/xrdt";
+    mkdir(dir.c_str(), 0755);
+    return dir + "/tune.txt";
+}
+
+std::string tune_key(const Plan *pl)
+{
+    cudaDeviceProp prop;
+    std::string key;
+    if (cudaGetDeviceProperties(&prop, pl->ctx->device) == cudaSuccess) {
+        for (const char *c = prop.name; *c; c++) key += (*c == ' ') ? '_' : *c;
+        key += fmt("-sm%d", prop.multiProcessorCount);
+    } else {
+        cudaGetLastError();
+        key = "gpu";
+    }
+    for (const xrdt_op *op : pl->ops)
+        key += fmt("|%dx%d,v%d,s%d,d%d,e%d,k%d", op->p.nx, op->p.ny, op->v.nv, op->p.n_src, op->v.P.n_det,
+                   op->v.P.e_hi - op->v.P.e_lo + 1, op->p.nwt);
+    return key;
+}
+
+bool tune_cache_get(const std::string &path, const std::string &key, int *warps, int64_t *tiles)
+{
+    if (path.empty()) return false;
+    FILE *f = fopen(path.c_str(), "r");
+    if (!f) return false;
+    bool found = false;
+    std::string line;
+    char buf[4096];
+    while (fgets(buf, sizeof buf, f)) {
+        line = buf;
+        const size_t sp = line.find(' ');
+        if (sp == std::string::npos || line.compare(0, sp, key) != 0 || sp != key.size()) continue;
+        int w = 0;
+        long long t = 0;
+        if (sscanf(line.c_str() + sp + 1, "%d %lld", &w, &t) == 2 && (w == 1 || w == 2 || w == 4) && t > 0) {
+            *warps = w;
+            *tiles = t;
+            found = true;   // the last entry wins
+        }
+    }
+    fclose(f);
+    return found;
+}
+
+void tune_cache_put(const std::string &path, const std::string &key, int warps, int64_t tiles)
+{
+    if (path.empty()) return;
+    FILE *f = fopen(path.c_str(), "a");
+    if (!f) return;
+    fprintf(f, "%s %d %lld\n", key.c_str(), warps, (long long)tiles);
+    fclose(f);
+}
+
 // Autotuner of the adjoint split: times one adjoint launch per candidate
 // (warps per block x tiles per SM slot) and keeps the fastest.  Reads the
 // per-energy weights of all ones and writes only the partial sums.
@@ -306,6 +380,20 @@ int plan_tune(Plan *pl)
     cudaStream_t st = ctx->stream;
     int optin = 0;
     CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
+    const std::string cache = tune_cache_path(), key = tune_key(pl);
+    {
+        int w = 0;
+        int64_t t = 0;
+        size_t sm = 0;
+        if (tune_cache_get(cache, key, &w, &t)) {
+            for (xrdt_op *op : pl->ops) sm = std::max(sm, vox_adj_smem(op->v.P, w));
+            if ((int64_t)(sm + vox_adj_static_smem()) <= optin) {
+                plan_split(pl, w, t);
+                pl->tuned = true;
+                return plan_upload(pl);
+            }
+        }
+    }
     int rc = plan_upload(pl);
     if (rc) return rc;
     CK(launch_vox_wtab(plan_batch(pl), plan_total(pl, 4), true, st, &ctx->launches));
@@ -350,6 +438,7 @@ int plan_tune(Plan *pl)
     if (rc) return rc;
     plan_split(pl, best_w, best_t);
     pl->tuned = true;
+    tune_cache_put(cache, key, best_w, best_t);
     return plan_upload(pl);
 }
 
