@@ -150,7 +150,8 @@ int64_t xrdt_ctx_launch_count(const xrdt_ctx *ctx);
 #define XRDT_KERNEL_VOX_ADJOINT 8  /* per-voxel operator: adjoint                    */
 #define XRDT_KERNEL_VOX_UPDATE  9  /* per-voxel operator: sums, update, staging      */
 #define XRDT_KERNEL_CT          10 /* transmission sinogram                          */
-#define XRDT_KERNEL_COUNT       11
+#define XRDT_KERNEL_BASIS       11 /* basis expansion on the tensor cores            */
+#define XRDT_KERNEL_COUNT       12
 /* With profiling on, every launch is bracketed by CUDA events on the
  * context's stream and the forward kernel counts the exponentials it
  * evaluates.  Off by default; turning it on or off clears the statistics. */
@@ -199,6 +200,17 @@ int32_t xrdt_forward_rays(xrdt_ctx *ctx, const xrdt_problem *p,
                           uint32_t flags);
 
 /* ---- MLEM with an explicit model matrix (main.m:154-176) --------------- */
+/* ---- basis expansion on the tensor cores -----------------------------
+ * I[M x N] = C[M x K] B[K x N], row-major, FP32 accuracy through 3xTF32 on
+ * tcgen05 (FP32 accumulation in tensor memory).  The reference's coarse q
+ * basis is point-sampled (wvt_value.cu:8-22, integrate_diffraction.cu:311-315),
+ * i.e. diagonal; with a dense basis this expands K coefficients per material
+ * (or per voxel) onto the NQF fine q bins, e.g. the Ifine [MAT x NQF] input
+ * of xrdt_forward.  K a multiple of 8 in [8, 64], N a multiple of 16 in
+ * [16, 256].  XRDT_ERR_TIMEOUT if the accumulator never completed. */
+int32_t xrdt_basis_expand(xrdt_ctx *ctx, const float *C, int64_t M, int32_t K,
+                          const float *B, int32_t N, float *I, uint32_t flags);
+
 /* ---- transmission CT sinogram ---------------------------------------
  * The reference declares a transmitted-photon output and its no-phantom
  * gain (Tphotons, gain0) and the launches that would fill them,

@@ -27,7 +27,7 @@ FWD_PLAIN_FP64 = 0x1
 FWD_NO_SYNC = 0x2
 OP_PLAIN_FP64 = 0x1
 (KERNEL_PREP_MAP, KERNEL_PREP_VOXELS, KERNEL_SRC_ATTEN, KERNEL_FORWARD, KERNEL_PLAIN, KERNEL_GATHER,
- KERNEL_MLEM, KERNEL_VOX_FORWARD, KERNEL_VOX_ADJOINT, KERNEL_VOX_UPDATE, KERNEL_CT) = range(11)
+ KERNEL_MLEM, KERNEL_VOX_FORWARD, KERNEL_VOX_ADJOINT, KERNEL_VOX_UPDATE, KERNEL_CT, KERNEL_BASIS) = range(12)
 
 _P = ctypes.POINTER(Problem)
 _vp = ctypes.c_void_p
@@ -61,6 +61,8 @@ SIGNATURES = {
     "xrdt_op_adjoint": (ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_uint32]),
     "xrdt_op_mlem": (ctypes.c_int32, [_vp, _vp, _vp, _vp, ctypes.c_int32, ctypes.c_uint32]),
     "xrdt_op_forward_rays": (ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_int64, _vp, ctypes.c_uint32]),
+    "xrdt_basis_expand": (ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp, ctypes.c_int32, _vp,
+                                           ctypes.c_uint32]),
     "xrdt_ct_sinogram": (ctypes.c_int32, [_vp, _P, _vp, _vp, _vp, _vp, _vp, ctypes.c_uint32]),
     "xrdt_batch_create": (ctypes.c_int32, [_vp, _vp, ctypes.c_int32, ctypes.POINTER(_vp)]),
     "xrdt_batch_destroy": (ctypes.c_int32, [_vp]),
@@ -238,6 +240,23 @@ def forward_rays(p: Problem, rays, spectrum, Ifine, seg, a1, a2, S2, q_min, q_ma
                                  A.ctypes.data if A is not None else None, FWD_PLAIN_FP64 if plain else 0)
     _check(rc, ctx.h)
     return N, C, A
+
+
+def basis_expand(C, B, I=None, ctx: Context | None = None):
+    """xrdt_basis_expand: I = C @ B in FP32 (3xTF32 on the tensor cores).
+    C [M, K] and B [K, N] row-major; returns I [M, N] (numpy unless I is a
+    torch CUDA tensor)."""
+    ctx = ctx or default_context()
+    pc, kc = _ptr(C, np.float32)
+    pb, kb = _ptr(B, np.float32)
+    shape_c = tuple(kc.shape) if hasattr(kc, "shape") else np.shape(kc)
+    M, K = int(shape_c[0]), int(shape_c[1])
+    N = int(kb.shape[1])
+    if I is None:
+        I = np.empty((M, N), np.float32)
+    pi, ki = _ptr(I, np.float32)
+    _check(lib().xrdt_basis_expand(ctx.h, pc, M, K, pb, N, pi, 0), ctx.h)
+    return ki
 
 
 def ct_sinogram(p: Problem, spectrum, a1, a2, Tphotons=None, gain0=None, ctx: Context | None = None):

@@ -39,7 +39,7 @@ enum Slot {
     S_CELLS, S_VXY, S_VMAT, S_VNA, S_VA2, S_CNT, S_ASRC, S_S2U8,
     S_SRCG, S_ENERGY, S_RFWIN, S_OFFS, S_WINLO, S_WINN, S_FINEQ, S_COARSEQ, S_COARSEQD,
     S_RAYS, S_PAIRS, S_NC, S_CC, S_AC,
-    S_MA, S_MY, S_MC, S_MX, S_MPART, S_MSENS,
+    S_MA, S_MY, S_MC, S_MX, S_MPART, S_MSENS, S_BC, S_BB, S_BI, S_ERR,
     S_COUNT
 };
 
@@ -783,6 +783,45 @@ int32_t xrdt_forward_rays(xrdt_ctx *ctx, const xrdt_problem *p, const float *spe
     static const int64_t none = 0;
     return forward_impl(ctx, p, spectrum, Ifine, seg, a1, a2, S2, q_min, q_max, a_min, a_max,
                         rays ? rays : &none, n_rays, Nphotons, Cphotons, A_rows, flags);
+}
+
+int32_t xrdt_basis_expand(xrdt_ctx *ctx, const float *C, int64_t M, int32_t K, const float *B, int32_t N, float *I,
+                          uint32_t flags)
+{
+    if (!ctx) return XRDT_ERR_NULL;
+    ctx->err.clear();
+    if (!C || !B || !I) return fail(ctx, XRDT_ERR_NULL, "C, B and I are required");
+    if (M < 1 || M > ((int64_t)1 << 40) || K < 8 || K > 64 || (K & 7) || N < 16 || N > 256 || (N & 15))
+        return fail(ctx, XRDT_ERR_DIMS, "need M >= 1, K a multiple of 8 in [8, 64], N a multiple of 16 in [16, 256]");
+    if (flags) return fail(ctx, XRDT_ERR_UNSUPPORTED, "unknown flag bits");
+    CK(cudaSetDevice(ctx->device));
+    int optin = 0;
+    CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
+    if ((int64_t)basis_smem(K, N) > optin) return fail(ctx, XRDT_ERR_UNSUPPORTED, "basis too large for one block");
+    cudaStream_t st = ctx->stream;
+    int rc;
+    const void *dC, *dB;
+    if ((rc = stage_in(ctx, S_BC, C, sizeof(float) * (size_t)M * K, &dC))) return rc;
+    if ((rc = stage_in(ctx, S_BB, B, sizeof(float) * (size_t)K * N, &dB))) return rc;
+    const bool hostI = !is_device_ptr(I);
+    float *dI = I;
+    void *tmp;
+    if (hostI) {
+        if ((rc = get_buf(ctx, S_BI, sizeof(float) * (size_t)M * N, &tmp))) return rc;
+        dI = (float *)tmp;
+    }
+    if ((rc = get_buf(ctx, S_ERR, sizeof(unsigned), &tmp))) return rc;
+    unsigned *derr = (unsigned *)tmp;
+    CK(cudaMemsetAsync(derr, 0, sizeof(unsigned), st));
+    {
+        ProfScope ps(ctx, XRDT_KERNEL_BASIS);
+        CK(launch_basis_expand((const float *)dC, M, K, (const float *)dB, N, dI, derr, st, &ctx->launches));
+    }
+    CK(cudaMemcpyAsync(ctx->h_counters + 2, derr, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    if (hostI) CK(cudaMemcpyAsync(I, dI, sizeof(float) * (size_t)M * N, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (ctx->h_counters[2]) return fail(ctx, XRDT_ERR_TIMEOUT, "the tensor-core accumulator never completed");
+    return XRDT_OK;
 }
 
 int32_t xrdt_ct_sinogram(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, const float *a1, const float *a2,

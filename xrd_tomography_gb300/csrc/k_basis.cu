@@ -1,0 +1,192 @@
+// k_basis.cu -- basis expansion on the 5th-generation tensor cores:
+// I[M x N] = C[M x K] B[K x N] in FP32 through 3xTF32.
+//
+// The reference's coarse q "basis" is point-sampled (wvt_value.cu:8-22,
+// integrate_diffraction.cu:311-315): each coefficient is a Gaussian
+// evaluated at one bin centre, a diagonal basis with no contraction.  A dense
+// basis -- K coefficients per material or voxel expanded onto the NQF fine q
+// bins that xrdt_forward's Ifine uses -- is the one GEMM-shaped operation of
+// the model.  This kernel does it with tcgen05.mma:
+//
+//  * one CTA (4 warps) per 128 rows of C; the whole N x K basis and the
+//    CTA's 128 x K rows are staged in shared memory in the canonical K-major
+//    layout without swizzle (core matrices of 8 rows x 16 bytes);
+//  * FP32 accuracy from TF32 inputs: x = hi + lo with hi, lo rounded to TF32,
+//    and D = A_hi B_hi + A_hi B_lo + A_lo B_hi accumulated in FP32 in tensor
+//    memory (the dropped A_lo B_lo term is below 2^-22 of the product);
+//  * one thread issues the MMAs (K = 8 each) and commits them to an
+//    mbarrier; the four warps read their 32 accumulator lanes back with
+//    tcgen05.ld and store the rows.
+//
+// The wait on the mbarrier is bounded: on time-out the kernel raises an error
+// flag, skips the read-back and still frees its tensor memory.
+#include "xrdt_device.cuh"
+
+namespace xrdt {
+
+namespace {
+
+constexpr int kTileM = 128;
+constexpr int kBasisThreads = 128;
+constexpr unsigned kSpinLimit = 1u << 26;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// TF32 rounding (nearest, ties away from zero): the high part of a split.
+__device__ __forceinline__ float tf32_rna(float x)
+{
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+// Canonical K-major layout without swizzle: element (r, k) of a tile with K
+// columns at byte (r/8)(K/4)128 + (k/4)128 + (r%8)16 + (k%4)4, i.e. core
+// matrices of 8 rows x 16 bytes, adjacent in K 128 bytes apart and adjacent
+// in rows (K/4)128 bytes apart.
+__device__ __forceinline__ int kmajor_offset(int r, int k, int K)
+{
+    return (r >> 3) * (K >> 2) * 128 + (k >> 2) * 128 + (r & 7) * 16 + (k & 3) * 4;
+}
+
+// Shared-memory matrix descriptor: start address, leading byte offset (the
+// K-adjacent core matrix), stride byte offset (the next 8 rows), descriptor
+// version 1, base offset 0, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo)
+{
+    uint64_t d = (uint64_t)((addr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// Instruction descriptor of kind::tf32: FP32 accumulator, TF32 A and B,
+// both K-major, no negation, N/8 and M/16.
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N)
+{
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__global__ void __launch_bounds__(kBasisThreads)
+k_basis_expand(const float *__restrict__ C, long long M, int K, const float *__restrict__ B, int N,
+               float *__restrict__ I, unsigned *__restrict__ err)
+{
+    extern __shared__ __align__(1024) unsigned char sm[];
+    const int a_bytes = kTileM * K * 4, b_bytes = N * K * 4;
+    unsigned char *a_hi = sm, *a_lo = sm + a_bytes;
+    unsigned char *b_hi = sm + 2 * a_bytes, *b_lo = b_hi + b_bytes;
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(b_lo + b_bytes);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 1);
+    const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
+    const long long m0 = (long long)blockIdx.x * kTileM;
+
+    uint32_t ncols = 32;   // accumulator columns: a power of two >= N
+    while (ncols < (uint32_t)N) ncols <<= 1;
+    if (wid == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(ncols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    // the CTA's rows of C and the basis, split into TF32 pairs
+    for (int i = tid; i < kTileM * K; i += kBasisThreads) {
+        const int r = i / K, k = i - r * K;
+        const float x = (m0 + r < M) ? __ldg(C + (m0 + r) * K + k) : 0.f;
+        const float hi = tf32_rna(x), lo = tf32_rna(x - hi);
+        const int o = kmajor_offset(r, k, K);
+        *reinterpret_cast<float *>(a_hi + o) = hi;
+        *reinterpret_cast<float *>(a_lo + o) = lo;
+    }
+    for (int i = tid; i < N * K; i += kBasisThreads) {
+        const int k = i / N, n = i - k * N;   // B[k][n], read along n
+        const float x = __ldg(B + i);
+        const float hi = tf32_rna(x), lo = tf32_rna(x - hi);
+        const int o = kmajor_offset(n, k, K);
+        *reinterpret_cast<float *>(b_hi + o) = hi;
+        *reinterpret_cast<float *>(b_lo + o) = lo;
+    }
+    // make the generic-proxy stores visible to the tensor core, publish the
+    // tensor-memory address
+    asm volatile("fence.proxy.async.shared::cta;");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = *tmem_slot;
+
+    if (tid == 0) {
+        const uint32_t idesc = idesc_tf32(kTileM, N);
+        const uint32_t lbo = 128, sbo = (uint32_t)(K >> 2) * 128;
+        uint32_t acc = 0;
+        for (int pass = 0; pass < 3; pass++) {
+            const unsigned char *A = (pass == 2) ? a_lo : a_hi;
+            const unsigned char *Bm = (pass == 1) ? b_lo : b_hi;
+            for (int kk = 0; kk < K; kk += 8) {
+                const uint64_t ad = smem_desc(smem_u32(A + (kk >> 2) * 128), lbo, sbo);
+                const uint64_t bd = smem_desc(smem_u32(Bm + (kk >> 2) * 128), lbo, sbo);
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                    "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+                acc = 1;
+            }
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+            smem_u32(mbar)));
+    }
+    // wait for the accumulator (bounded)
+    uint32_t done = 0;
+    for (unsigned it = 0; !done; it++) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(smem_u32(mbar)), "r"(0u));
+        if (!done && it >= kSpinLimit) break;
+    }
+    done = __all_sync(0xffffffffu, done);   // tcgen05.ld below needs the whole warp
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (!done) {
+        if (lane == 0) atomicOr(err, 1u);
+    } else {
+        // warp w holds accumulator lanes 32w .. 32w+31 = rows of the tile
+        const long long row = m0 + wid * 32 + lane;
+        for (int c = 0; c < N; c += 8) {
+            uint32_t v[8];
+            const uint32_t taddr = tmem + ((uint32_t)(wid * 32) << 16) + (uint32_t)c;
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                         : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                           "=r"(v[7])
+                         : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;");
+            if (row < M) {
+                float *o = I + row * N + c;
+                for (int j = 0; j < 8; j++) o[j] = __uint_as_float(v[j]);
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (wid == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
+}
+
+} // namespace
+
+size_t basis_smem(int K, int N) { return 2 * (size_t)kTileM * K * 4 + 2 * (size_t)N * K * 4 + 16; }
+
+cudaError_t launch_basis_expand(const float *C, long long M, int K, const float *B, int N, float *I, unsigned *err,
+                                cudaStream_t s, int64_t *launches)
+{
+    const size_t smem = basis_smem(K, N);
+    cudaError_t e = cudaFuncSetAttribute(k_basis_expand, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const long long tiles = (M + kTileM - 1) / kTileM;
+    k_basis_expand<<<(unsigned)tiles, kBasisThreads, smem, s>>>(C, M, K, B, N, I, err);
+    if (launches) (*launches)++;
+    return cudaGetLastError();
+}
+
+} // namespace xrdt

@@ -103,6 +103,12 @@ cudaError_t launch_ct_sinogram(const DevProblem &P, const SrcGeom *sg, const flo
                                const float *rf_win, const int *win_lo, float *T, float *G0, cudaStream_t s,
                                int64_t *launches);
 
+// k_basis.cu: I[M x N] = C[M x K] B[K x N] on tcgen05 (3xTF32); err is set
+// when the accumulator wait times out.
+size_t basis_smem(int K, int N);
+cudaError_t launch_basis_expand(const float *C, long long M, int K, const float *B, int N, float *I, unsigned *err,
+                                cudaStream_t s, int64_t *launches);
+
 // k_prep.cu
 struct PrepBuffers {
     float4 *cells;          // [(ny+1)*(nx+1)*2] bilinear cells
