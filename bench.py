@@ -44,6 +44,9 @@ sys.path.insert(0, ROOT)
 
 WORKLOAD = 1            # index of the synthetic configuration
 FLUSH_BYTES = 256 << 20
+# DRAM bytes (read + write) of one k_fwd launch, from an ncu capture of
+# this benchmark's command: per workload index
+K_FWD_DRAM_BYTES = {1: 64696320 + 19122176}
 
 
 def parse():
@@ -530,7 +533,10 @@ def run_ours(args):
         achieved = work / (per_launch_ms * 1e-3) / 1e9
         line["roofline"] = {
             "bound": "sfu", "achieved": achieved, "peak": ex2_peak / 1e9, "unit": "G exp2/s",
-            "frac": achieved / (ex2_peak / 1e9) if ex2_peak > 0 else None, "traffic": None,
+            "frac": achieved / (ex2_peak / 1e9) if ex2_peak > 0 else None,
+            "traffic": K_FWD_DRAM_BYTES.get(args.workload),
+            "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one k_fwd launch "
+                              "(profiles/k_fwd_256x256_dram.md)" if args.workload in K_FWD_DRAM_BYTES else None,
             "kernel": "k_fwd (factored forward projector)",
             "work_per_launch": work, "launch_ms": per_launch_ms,
             "peak_source": "measured on this GPU by xrdt_probe_peak (ex2.approx, all SMs)",

@@ -250,3 +250,38 @@ def test_operator_errors(ctx):
     assert not op.forward(np.ones(op.unknowns, np.float32)).any()
     assert not op.adjoint(np.ones(p.rays, np.float32)).any()
     op.close()
+
+
+def test_reference_configuration_operator(ctx, oracle_lib):
+    """The per-voxel operator on the reference's compiled configuration
+    (NWT = 256 coarse bins, 1024 px x 64 energy bins) with the golden
+    16x16 inputs: forward and adjoint on sampled rays against the oracle,
+    and the voxel sums against the golden model-matrix rows."""
+    import os
+    from xrd_tomography_gb300.problem import reference_problem
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_forward_16.npz"))
+    p = reference_problem(int(g["nx"]), int(g["ny"]))
+    t = g["tables"]
+    inp = synth.Inputs(p, g["spectrum"], g["Ifine"], g["seg"], g["a1"], g["a2"], g["S2"],
+                       float(t[0]), float(t[1]), float(t[2]), float(t[3]))
+    op = make_op(inp, ctx)
+    rng = np.random.default_rng(6)
+    rays = np.sort(rng.choice(p.rays, 64, replace=False))
+    x = rand_x(inp, 7)
+    y = op.forward(x)
+    y_ref, _ = oracle_lib.vox_rays(inp, rays, x=x)
+    assert max_rel_err(y[rays], y_ref) < FAST_RTOL
+    w = np.zeros(p.rays, np.float32)
+    w[rays] = rng.uniform(0.5, 1.5, rays.size)
+    _, g_ref = oracle_lib.vox_rays(inp, rays, w=w[rays])
+    assert max_rel_err(op.adjoint(w), g_ref.reshape(-1)) < FAST_RTOL
+    # per-material sums of the per-voxel rows are the reference's Amatrix rows
+    seg = np.asarray(inp.seg).reshape(-1)
+    xm = rng.uniform(0.0, 1.0, (p.n_mat, p.nwt))
+    xv = np.zeros((seg.size, p.nwt), np.float32)
+    xv[seg > 0] = xm[seg[seg > 0] - 1]
+    gold_rays = np.asarray(g["A_rays"])
+    A_gold = np.asarray(g["A"], np.float64).reshape(gold_rays.size, p.n_mat, p.nwt)
+    yv = op.forward(xv.reshape(-1))
+    assert max_rel_err(yv[gold_rays], np.einsum("rmk,mk->r", A_gold, xm)) < FAST_RTOL
+    op.close()
