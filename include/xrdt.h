@@ -151,7 +151,8 @@ int64_t xrdt_ctx_launch_count(const xrdt_ctx *ctx);
 #define XRDT_KERNEL_VOX_UPDATE  9  /* per-voxel operator: sums, update, staging      */
 #define XRDT_KERNEL_CT          10 /* transmission sinogram                          */
 #define XRDT_KERNEL_BASIS       11 /* basis expansion on the tensor cores            */
-#define XRDT_KERNEL_COUNT       12
+#define XRDT_KERNEL_WALK        12 /* detector-side line integrals of the forward    */
+#define XRDT_KERNEL_COUNT       13
 /* With profiling on, every launch is bracketed by CUDA events on the
  * context's stream and the forward kernel counts the exponentials it
  * evaluates.  Off by default; turning it on or off clears the statistics. */

@@ -27,7 +27,7 @@ FWD_PLAIN_FP64 = 0x1
 FWD_NO_SYNC = 0x2
 OP_PLAIN_FP64 = 0x1
 (KERNEL_PREP_MAP, KERNEL_PREP_VOXELS, KERNEL_SRC_ATTEN, KERNEL_FORWARD, KERNEL_PLAIN, KERNEL_GATHER,
- KERNEL_MLEM, KERNEL_VOX_FORWARD, KERNEL_VOX_ADJOINT, KERNEL_VOX_UPDATE, KERNEL_CT, KERNEL_BASIS) = range(12)
+ KERNEL_MLEM, KERNEL_VOX_FORWARD, KERNEL_VOX_ADJOINT, KERNEL_VOX_UPDATE, KERNEL_CT, KERNEL_BASIS, KERNEL_WALK) = range(13)
 
 _P = ctypes.POINTER(Problem)
 _vp = ctypes.c_void_p

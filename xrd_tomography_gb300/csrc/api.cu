@@ -39,7 +39,7 @@ enum Slot {
     S_CELLS, S_VXY, S_VMAT, S_VNA, S_VA2, S_CNT, S_ASRC, S_S2U8,
     S_SRCG, S_ENERGY, S_RFWIN, S_OFFS, S_WINLO, S_WINN, S_FINEQ, S_COARSEQ, S_COARSEQD,
     S_RAYS, S_PAIRS, S_NC, S_CC, S_AC,
-    S_MA, S_MY, S_MC, S_MX, S_MPART, S_MSENS, S_BC, S_BB, S_BI, S_ERR,
+    S_MA, S_MY, S_MC, S_MX, S_MPART, S_MSENS, S_BC, S_BB, S_BI, S_ERR, S_WALK,
     S_COUNT
 };
 
@@ -542,6 +542,9 @@ int64_t xrdt_ctx_launch_count(const xrdt_ctx *ctx) { return ctx ? ctx->launches 
 
 namespace {
 
+// Bound on the staged detector-side integrals of one tile of pairs.
+constexpr int64_t kWalkTableBytes = (int64_t)4 << 30;
+
 // Shared body of xrdt_forward (rays == NULL: every ray, the Forward_XRD
 // layout) and xrdt_forward_rays (outputs per listed ray).
 int forward_impl(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, const float *Ifine,
@@ -712,10 +715,32 @@ int forward_impl(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, co
         { ProfScope ps(ctx, XRDT_KERNEL_SRC_ATTEN);
           CK(launch_src_atten(P, (const SrcGeom *)d_srcg, nv, B, st, &ctx->launches)); }
         T.work = ctx->profiling ? ctx->d_work : nullptr;
+        // pairs go through in tiles: the detector-side integrals of a tile
+        // (k_walk.cu), then the projector over the same pairs
+        auto project = [&](const int2 *list, int64_t n_total, float *oN, float *oC, float *oA) -> int {
+            // whole groups of 8 pixels of every view (8 entries of a list)
+            const int64_t unit = list ? 8 : 8 * (int64_t)p->n_src;
+            const int64_t fit = std::min<int64_t>(kWalkTableBytes / ((int64_t)nv * (int64_t)sizeof(float2)),
+                                                  (int64_t)1 << 30);
+            const int64_t tile = std::min<int64_t>(n_total, std::max<int64_t>(unit, fit / unit * unit));
+            void *dtab;
+            int r = get_buf(ctx, S_WALK, sizeof(float2) * (size_t)tile * nv, &dtab);
+            if (r) return r;
+            for (int64_t p0 = 0; p0 < n_total; p0 += tile) {
+                const int64_t n = std::min(tile, n_total - p0);
+                {
+                    ProfScope ps(ctx, XRDT_KERNEL_WALK);
+                    CK(launch_det_walk(P, (const SrcGeom *)d_srcg, list ? list + p0 : nullptr, p0, n, B.vox_xy, nv,
+                                       B.cells, (float2 *)dtab, st, &ctx->launches));
+                }
+                ProfScope ps(ctx, XRDT_KERNEL_FORWARD);
+                CK(launch_fast_forward(P, (const SrcGeom *)d_srcg, T, B, nv, (const float *)d_ifine, list, n_total,
+                                       p0, (int)n, (const float2 *)dtab, oN, oC, oA, st, &ctx->launches));
+            }
+            return XRDT_OK;
+        };
         if (!ray_list) {
-            ProfScope ps(ctx, XRDT_KERNEL_FORWARD);
-            CK(launch_fast_forward(P, (const SrcGeom *)d_srcg, T, B, nv, (const float *)d_ifine, nullptr, 0, dN,
-                                   dC, dA, st, &ctx->launches));
+            if ((rc = project(nullptr, (int64_t)p->n_src * P.n_det, dN, dC, dA))) return rc;
         } else if (n_list > 0) {
             // the (src, det) pairs the listed rays need, then a gather
             std::vector<int64_t> cols(n_list);
@@ -741,10 +766,7 @@ int forward_impl(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, co
             if (dA && (rc = get_buf(ctx, S_AC, sizeof(float) * ncomp * MW, &dAc))) return rc;
             CK(cudaMemcpyAsync(dpairs, pairs.data(), sizeof(int2) * np, cudaMemcpyHostToDevice, st));
             CK(cudaMemcpyAsync(didx, idx.data(), sizeof(int64_t) * n_list, cudaMemcpyHostToDevice, st));
-            { ProfScope ps(ctx, XRDT_KERNEL_FORWARD);
-              CK(launch_fast_forward(P, (const SrcGeom *)d_srcg, T, B, nv, (const float *)d_ifine,
-                                     (const int2 *)dpairs, np, (float *)dNc, (float *)dCc, (float *)dAc, st,
-                                     &ctx->launches)); }
+            if ((rc = project((const int2 *)dpairs, np, (float *)dNc, (float *)dCc, (float *)dAc))) return rc;
             ProfScope ps(ctx, XRDT_KERNEL_GATHER);
             CK(launch_gather_rays((const int64_t *)didx, n_list, (const float *)dNc, (const float *)dCc,
                                   (const float *)dAc, (int)MW, dN, dC, dA, st, &ctx->launches));

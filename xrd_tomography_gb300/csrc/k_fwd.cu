@@ -92,8 +92,11 @@ struct FwdArgs {
     const unsigned char *s2u8;
     const float *Ifine;
     float *N, *C, *A;
-    const int2 *pairs;
-    int n_pairs;
+    const int2 *pairs;         // a list of pairs, or NULL: the linear pairs src + det*SRC
+    long long p0;              // block b takes pair p0 + b (of the list or of the linear index)
+    int n_pairs;               // blocks of this launch
+    long long n_cols;          // output columns: the list's length, or SRC*DET
+    const float2 *walk;        // [block][nv] detector-side line integrals (k_walk.cu)
     int nv, E, e_pass, sl;
     F32Consts c;
 };
@@ -132,17 +135,18 @@ k_fwd(const FwdArgs args)
     int det, src;
     int64_t colidx, ncols;   // output column of this block and the number of columns
     if (args.pairs) {
-        const int2 pr = args.pairs[blockIdx.x];
+        colidx = args.p0 + blockIdx.x;
+        const int2 pr = args.pairs[colidx];
         src = pr.x;
         det = pr.y;
-        colidx = blockIdx.x;
-        ncols = args.n_pairs;
+        ncols = args.n_cols;
     } else {
-        det = blockIdx.x;
-        src = blockIdx.y;
-        colidx = (int64_t)src + (int64_t)det * P.n_src;
+        colidx = args.p0 + blockIdx.x;
+        src = (int)(colidx % P.n_src);
+        det = (int)(colidx / P.n_src);
         ncols = (int64_t)P.n_src * P.n_det;
     }
+    const float2 *walk = args.walk + (int64_t)blockIdx.x * args.nv;
 
     // ---- stage the tables ----
     for (int i = tid; i < E; i += kThreads) {
@@ -214,21 +218,13 @@ k_fwd(const FwdArgs args)
             const int nav = args.vox_na[v];
             const float a2v = args.vox_a2[v];
             const float2 Asv = args.atten_src[(int64_t)src * nv + v];
-            WalkSetup ws;
-            if (!walk_setup_f32(P, c, G.Rdx.hi, G.Rdy.hi, vx, vy, &ws))
-                walk_setup_f64(P, pair.Rdx, pair.Rdy, (double)vx, (double)vy, &ws);
+            const float2 Adv = walk[v];
 
             const int nin = min(32, nv - chunk * 32);
             for (int i = 0; i < nin; i++) {
-                WalkSetup wi;
-                wi.rx = __shfl_sync(0xffffffffu, ws.rx, i);
-                wi.ry = __shfl_sync(0xffffffffu, ws.ry, i);
-                wi.Lx = __shfl_sync(0xffffffffu, ws.Lx, i);
-                wi.Ly = __shfl_sync(0xffffffffu, ws.Ly, i);
-                wi.n = __shfl_sync(0xffffffffu, ws.n, i);
                 // labels as at integrate_diffraction.cu:259-260: the detector-side
                 // integral feeds Pin, the source-side one Pout.
-                const float2 Ad = walk_coop(args.cells, P.nx, P.ny, wi, DQf, lane);
+                const float2 Ad = make_float2(__shfl_sync(0xffffffffu, Adv.x, i), __shfl_sync(0xffffffffu, Adv.y, i));
                 const float sh = __shfl_sync(0xffffffffu, vg.s.hi, i);
                 const float sl = __shfl_sync(0xffffffffu, vg.s.lo, i);
                 const float oh = __shfl_sync(0xffffffffu, vg.omc.hi, i);
@@ -447,9 +443,7 @@ cudaError_t launch_variant(const FwdArgs &a, size_t smem, cudaStream_t s)
 {
     cudaError_t e = cudaFuncSetAttribute(k_fwd<WN, WA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    dim3 grid(a.P.n_det, a.P.n_src);
-    if (a.pairs) grid = dim3((unsigned)a.n_pairs, 1);
-    k_fwd<WN, WA><<<grid, kThreads, smem, s>>>(a);
+    k_fwd<WN, WA><<<(unsigned)a.n_pairs, kThreads, smem, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -487,12 +481,15 @@ size_t fast_forward_smem(const DevProblem &P, int sl, int e_pass, bool with_n, b
 
 cudaError_t launch_fast_forward(const DevProblem &P, const SrcGeom *d_src, const FwdTables &T,
                                 const PrepBuffers &B, int nv, const float *Ifine, const int2 *pairs,
-                                int n_pairs, float *N, float *C, float *A, cudaStream_t s,
-                                int64_t *launches)
+                                long long n_list, long long p0, int n_pairs, const float2 *walk, float *N,
+                                float *C, float *A, cudaStream_t s, int64_t *launches)
 {
     FwdArgs a;
     a.pairs = pairs;
+    a.p0 = p0;
     a.n_pairs = n_pairs;
+    a.n_cols = pairs ? n_list : (long long)P.n_src * P.n_det;
+    a.walk = walk;
     a.P = P;
     a.sg = d_src;
     a.T = T;

@@ -141,12 +141,22 @@ struct FwdTables {
     unsigned long long *work;  // nullable: counts the exp2 evaluations
 };
 size_t fast_forward_smem(const DevProblem &P, int sl, int e_pass, bool with_n, bool with_a);
-// pairs (nullable): (src, det) of each block; outputs then go to the compact
-// layout [nrg_det][n_pairs] (and [nrg_det][n_pairs][n_mat*nwt] for A).
+// n_pairs blocks, block b on pair p0 + b: of the list pairs[0 .. n_list)
+// when it is given (outputs then go to the compact layout [nrg_det][n_list],
+// and [nrg_det][n_list][n_mat*nwt] for A), else of the linear index
+// src + det*SRC of the full layout.  walk holds the blocks' detector-side
+// integrals, [n_pairs][nv] (launch_det_walk).
 cudaError_t launch_fast_forward(const DevProblem &P, const SrcGeom *d_src, const FwdTables &T,
                                 const PrepBuffers &B, int nv, const float *Ifine,
-                                const int2 *pairs, int n_pairs,
-                                float *N, float *C, float *A, cudaStream_t s, int64_t *launches);
+                                const int2 *pairs, long long n_list, long long p0, int n_pairs,
+                                const float2 *walk, float *N, float *C, float *A, cudaStream_t s,
+                                int64_t *launches);
+// k_walk.cu: tab[item][v] = detector-side line integral of voxel v for the
+// pair pairs[item] (or the linear pair p0 + item), item < n_items.  Linear
+// pairs come in whole pixels: p0 and n_items multiples of SRC.
+cudaError_t launch_det_walk(const DevProblem &P, const SrcGeom *sg, const int2 *pairs, long long p0,
+                            long long n_items, const int *vox_xy, int nv, const float4 *cells, float2 *tab,
+                            cudaStream_t s, int64_t *launches);
 // out[i] = compact[idx[i]] for N, C and the rows of A (row length mw).
 cudaError_t launch_gather_rays(const int64_t *idx, int64_t n, const float *Nc, const float *Cc,
                                const float *Ac, int mw, float *N, float *C, float *A, cudaStream_t s,
