@@ -612,7 +612,7 @@ int forward_impl(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, co
     void *d_srcg;
     if ((rc = get_buf(ctx, S_SRCG, sizeof(SrcGeom) * p->n_src, &d_srcg))) return rc;
     CK(cudaMemcpyAsync(d_srcg, hsg.data(), sizeof(SrcGeom) * p->n_src, cudaMemcpyHostToDevice, st));
-    if ((rc = get_buf(ctx, S_CELLS, sizeof(float4) * 2 * (size_t)(p->nx + 1) * (p->ny + 1), &tmp))) return rc;
+    if ((rc = get_buf(ctx, S_CELLS, sizeof(float4) * 4 * (size_t)(p->nx + 1) * (p->ny + 1), &tmp))) return rc;
     B.cells = (float4 *)tmp;
     if ((rc = get_buf(ctx, S_VXY, sizeof(int) * nvox, &tmp))) return rc;
     B.vox_xy = (int *)tmp;
@@ -718,8 +718,8 @@ int forward_impl(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, co
         // pairs go through in tiles: the detector-side integrals of a tile
         // (k_walk.cu), then the projector over the same pairs
         auto project = [&](const int2 *list, int64_t n_total, float *oN, float *oC, float *oA) -> int {
-            // whole groups of 8 pixels of every view (8 entries of a list)
-            const int64_t unit = list ? 8 : 8 * (int64_t)p->n_src;
+            // whole groups of 32 pixels of every view (32 entries of a list)
+            const int64_t unit = list ? 32 : 32 * (int64_t)p->n_src;
             const int64_t fit = std::min<int64_t>(kWalkTableBytes / ((int64_t)nv * (int64_t)sizeof(float2)),
                                                   (int64_t)1 << 30);
             const int64_t tile = std::min<int64_t>(n_total, std::max<int64_t>(unit, fit / unit * unit));
@@ -891,7 +891,7 @@ int32_t xrdt_ct_sinogram(xrdt_ctx *ctx, const xrdt_problem *p, const float *spec
     CK(cudaMemcpyAsync(d_wlo, ht.win_lo.data(), sizeof(int) * ht.win_lo.size(), cudaMemcpyHostToDevice, st));
     PrepBuffers B;
     memset(&B, 0, sizeof B);
-    if ((rc = get_buf(ctx, S_CELLS, sizeof(float4) * 2 * (size_t)(p->nx + 1) * (p->ny + 1), &tmp))) return rc;
+    if ((rc = get_buf(ctx, S_CELLS, sizeof(float4) * 4 * (size_t)(p->nx + 1) * (p->ny + 1), &tmp))) return rc;
     B.cells = (float4 *)tmp;
     {
         ProfScope ps(ctx, XRDT_KERNEL_PREP_MAP);

@@ -5,7 +5,10 @@
 //    Forward_XRD.cu:209-237: cell (ci,cj) holds the bilinear coefficients of
 //    the four texels (ci-1..ci, cj-1..cj) of a zero-bordered map, about the
 //    cell centre, as two float4, so one sample is two 16-byte loads and three
-//    packed FMAs with no border tests.  Also
+//    packed FMAs with no border tests.  The map is stored twice: row-major
+//    (ci + cj (NX+1)) and behind it column-major (cj + ci (NY+1)), so that a
+//    warp whose rays lie side by side along y reads neighbouring cells from
+//    one cache line as well as one whose rays lie side by side along x.  Also
 //    quantises the Compton table to u8 (integrate_diffraction.cu:66-74).
 //  * k_compact_voxels: non-empty voxels in the reference's loop order
 //    (nx outer, ny inner; integrate_diffraction.cu:173-178) and the material
@@ -50,8 +53,13 @@ __global__ void k_build_cells(int nx, int ny, const float *__restrict__ a1, cons
             c01[q] = (float)(0.5 * ((f01 - f00) + (f11 - f10)));
             c11[q] = (float)((f11 - f01) - (f10 - f00));
         }
-        cells[2 * c] = make_float4(c00[0], c00[1], c10[0], c10[1]);
-        cells[2 * c + 1] = make_float4(c01[0], c01[1], c11[0], c11[1]);
+        const float4 lo = make_float4(c00[0], c00[1], c10[0], c10[1]);
+        const float4 hi = make_float4(c01[0], c01[1], c11[0], c11[1]);
+        const int64_t ct = ncell + (int64_t)cj + (int64_t)ci * (ny + 1);
+        cells[2 * c] = lo;
+        cells[2 * c + 1] = hi;
+        cells[2 * ct] = lo;
+        cells[2 * ct + 1] = hi;
     }
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ns2; i += stride) {
         const int q = floor_to_int((double)S2[i]);

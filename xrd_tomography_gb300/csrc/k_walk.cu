@@ -8,19 +8,17 @@
 // here a separate kernel walks them and the projector reads the results as
 // one coalesced float2 per voxel.
 //
-// The walk is bound by L1 wavefronts (one per distinct 128-byte line that a
-// warp-wide load touches), so the lanes of a load are kept close together in
-// the plane.  A warp takes a group of 8 rays that end on 8 neighbouring
-// pixels of one view and a strip of voxels.  For each voxel the 8 rays leave
-// from the same point and stay within a few voxels of each other, so lane
-// (r, j) = (lane / 4, lane % 4) takes samples j, j+4, j+8, ... of ray r and
-// each warp-wide load covers about one voxel of path of 8 adjacent rays --
-// a few cells -- instead of 8 voxels of one ray.
-//
-// Per chunk of 32 voxels: lane = voxel sets up the walks of the 8 rays (FP32
-// with the exact FP64 fallback, walk.cuh) into shared memory; then the warp
-// walks voxel by voxel, sums the 4 lanes of each ray, and finally stores the
-// 8 rays' results of the chunk as 8 coalesced rows.
+// Sampled one point per lane, the walk is bound by L1 wavefronts: a
+// warp-wide 16-byte load costs at least four, and every sample needs a
+// 32-byte cell.  Here each lane walks a whole ray cell by cell (walk_cells,
+// walk.cuh), one cell load per run of 3-4 samples.  A warp takes 32 rays
+// that end on 32 neighbouring pixels of one view and leave from the same
+// voxel, so its lanes take about the same number of steps and stay within a
+// few voxels of each other, side by side across the rays.  The warp reads
+// the copy of the cell map (row- or column-major) whose rows run across its
+// rays, so that neighbouring lanes mostly share cache lines.  Per voxel each
+// lane sets up its own ray (FP32 with the exact FP64 fallback) and stores its
+// float2; the stores of consecutive voxels of a row merge in L2.
 #include "scatter.cuh"
 
 namespace xrdt {
@@ -29,22 +27,13 @@ namespace {
 
 constexpr int kWalkThreads = 128;
 constexpr int kWalkWarps = kWalkThreads / 32;
-constexpr int kRays = 8;            // rays per group: neighbouring pixels of one view
-constexpr int kChunksPerStrip = 4;  // chunks of 32 voxels per warp item
-constexpr int kPad = 33;            // row pitch of the per-ray tables (no bank conflicts)
-
-struct WarpTables {
-    float rx[kRays][kPad], ry[kRays][kPad], Lx[kRays][kPad], Ly[kRays][kPad];
-    int n[kRays][kPad];
-    float2 res[kRays][kPad];
-    double ex[kRays], ey[kRays];
-    long long row[kRays];   // output row of each ray, -1 for none
-};
+constexpr int kRays = 32;          // rays per group: neighbouring pixels of one view
+constexpr int kVoxPerStrip = 64;   // voxels per warp item
 
 // Ray r of group g.  Linear pairs (pairs == NULL): the tile holds the pixels
 // d0 .. d0+nd-1 of every view, row (det - d0) * SRC + src; group g is view
-// g % SRC and pixels d0 + 8 (g / SRC) + r.  A list: entries 8g + r.
-__device__ __forceinline__ bool group_ray(const DevProblem &P, const int2 *pairs, long long n_items, int d0, int nd,
+// g % SRC and pixels d0 + 32 (g / SRC) + r.  A list: entries 32g + r.
+__device__ __forceinline__ bool group_ray(const DevProblem &P, const int2 *pairs, long long n_items, int nd,
                                           long long g, int r, int *src, int *det, long long *row)
 {
     if (pairs) {
@@ -60,101 +49,55 @@ __device__ __forceinline__ bool group_ray(const DevProblem &P, const int2 *pairs
     const int dl = (int)(g / P.n_src) * kRays + r;
     if (dl >= nd) return false;
     *src = s;
-    *det = d0 + dl;
+    *det = dl;   // relative to d0
     *row = (long long)dl * P.n_src + s;
     return true;
 }
 
-__global__ void __launch_bounds__(kWalkThreads)
+__global__ void __launch_bounds__(kWalkThreads, 6)
 k_det_walk(DevProblem P, F32Consts c, const SrcGeom *__restrict__ sg, const int2 *__restrict__ pairs,
            long long n_items, int d0, int nd, long long n_groups, const int *__restrict__ vox_xy, int nv,
            const float4 *__restrict__ cells, float2 *__restrict__ tab)
 {
-    __shared__ WarpTables wt_all[kWalkWarps];
-    WarpTables &W = wt_all[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
-    const int r = lane >> 2, j = lane & 3;
-    const unsigned ncell_m1 = (unsigned)((P.nx + 1) * (P.ny + 1) - 1);
-    const int nchunks = (nv + 31) >> 5;
-    const int nstrips = (nchunks + kChunksPerStrip - 1) / kChunksPerStrip;
+    const int64_t ncell = (int64_t)(P.nx + 1) * (P.ny + 1);
+    const unsigned ncell_m1 = (unsigned)(ncell - 1);
+    const float4 *cells_t = cells + 2 * ncell;   // column-major copy
+    const int nstrips = (nv + kVoxPerStrip - 1) / kVoxPerStrip;
     const long long nwork = n_groups * nstrips;
     const long long wstride = (long long)gridDim.x * kWalkWarps;
     for (long long wk = (long long)blockIdx.x * kWalkWarps + (threadIdx.x >> 5); wk < nwork; wk += wstride) {
         const long long g = wk / nstrips;
         const int strip = (int)(wk - g * nstrips);
-        __syncwarp();
-        if (lane < kRays) {
-            int src, det;
-            long long row;
-            if (group_ray(P, pairs, n_items, d0, nd, g, lane, &src, &det, &row)) {
-                const SrcGeom gs = sg[src];
-                double Rdx, Rdy, Rdz;
-                det_position(P, gs.sphi, gs.cphi, det, &Rdx, &Rdy, &Rdz);
-                W.ex[lane] = Rdx;
-                W.ey[lane] = Rdy;
-                W.row[lane] = row;
-            } else {
-                W.row[lane] = -1;
-            }
+        int src = 0, det = 0;
+        long long row = -1;
+        const bool valid = group_ray(P, pairs, n_items, nd, g, lane, &src, &det, &row);
+        double ex = 0.0, ey = 0.0;
+        if (valid) {
+            if (!pairs) det += d0;
+            const SrcGeom gs = sg[src];
+            double ez;
+            det_position(P, gs.sphi, gs.cphi, det, &ex, &ey, &ez);
         }
-        __syncwarp();
-        const int c1 = min(nchunks, (strip + 1) * kChunksPerStrip);
-        for (int chunk = strip * kChunksPerStrip; chunk < c1; chunk++) {
-            const int nin = min(32, nv - chunk * 32);
-            // set-up: lane = voxel, all rays of the group
-            {
-                const int v = min(chunk * 32 + lane, nv - 1);
-                const int xy = vox_xy[v];
-                const float vx = ((float)(xy & 0xffff) + 0.5f) * c.vox;
-                const float vy = ((float)(xy >> 16) + 0.5f) * c.vox;
-                for (int q = 0; q < kRays; q++) {
-                    WalkSetup ws;
-                    if (W.row[q] < 0) {
-                        ws.rx = ws.ry = ws.Lx = ws.Ly = 0.f;
-                        ws.n = 0;
-                    } else {
-                        const double ex = W.ex[q], ey = W.ey[q];
-                        if (!walk_setup_f32(P, c, (float)ex, (float)ey, vx, vy, &ws))
-                            walk_setup_f64(P, ex, ey, (double)vx, (double)vy, &ws);
-                    }
-                    W.rx[q][lane] = ws.rx;
-                    W.ry[q][lane] = ws.ry;
-                    W.Lx[q][lane] = ws.Lx;
-                    W.Ly[q][lane] = ws.Ly;
-                    W.n[q][lane] = ws.n;
-                }
-            }
-            __syncwarp();
-            // walks: lane (r, j) takes samples j, j+4, ... of ray r
-            for (int i = 0; i < nin; i++) {
-                const float2 L2 = make_float2(W.Lx[r][i], W.Ly[r][i]);
-                const float2 R2 = make_float2(W.rx[r][i], W.ry[r][i]);
-                const int n = W.n[r][i];
-                float2 sa = make_float2(0.f, 0.f), sb = make_float2(0.f, 0.f);
-                float kf = (float)j;
-                int k = j;
-                for (; k + 4 < n; k += 8, kf += 8.f) {
-                    const float kg = kf + 4.f;
-                    const float2 a = cell_sample(cells, P.nx, ncell_m1, __ffma2_rn(L2, make_float2(kf, kf), R2));
-                    const float2 b = cell_sample(cells, P.nx, ncell_m1, __ffma2_rn(L2, make_float2(kg, kg), R2));
-                    sa = __fadd2_rn(sa, a);
-                    sb = __fadd2_rn(sb, b);
-                }
-                if (k < n)
-                    sa = __fadd2_rn(sa, cell_sample(cells, P.nx, ncell_m1, __ffma2_rn(L2, make_float2(kf, kf), R2)));
-                float2 s = __fadd2_rn(sa, sb);
-                s.x += __shfl_xor_sync(0xffffffffu, s.x, 1);
-                s.y += __shfl_xor_sync(0xffffffffu, s.y, 1);
-                s.x += __shfl_xor_sync(0xffffffffu, s.x, 2);
-                s.y += __shfl_xor_sync(0xffffffffu, s.y, 2);
-                if (j == 0) W.res[r][i] = make_float2(s.x * c.DQ, s.y * c.DQ);
-            }
-            __syncwarp();
-            for (int q = 0; q < kRays; q++) {
-                const long long row = W.row[q];
-                if (row >= 0 && lane < nin) tab[row * nv + chunk * 32 + lane] = W.res[q][lane];
-            }
-            __syncwarp();
+        const float exf = (float)ex, eyf = (float)ey;
+        float2 *out = tab + (valid ? row : 0) * nv;
+        const int v1 = min(nv, (strip + 1) * kVoxPerStrip);
+        for (int v = strip * kVoxPerStrip; v < v1; v++) {
+            const int xy = vox_xy[v];
+            const float vx = ((float)(xy & 0xffff) + 0.5f) * c.vox;
+            const float vy = ((float)(xy >> 16) + 0.5f) * c.vox;
+            WalkSetup ws;
+            ws.Lx = ws.Ly = 0.f;
+            ws.n = 0;
+            if (valid && !walk_setup_f32(P, c, exf, eyf, vx, vy, &ws))
+                walk_setup_f64(P, ex, ey, (double)vx, (double)vy, &ws);
+            // rays mostly along x lie side by side along y: column-major copy
+            const unsigned along_x = __ballot_sync(0xffffffffu, valid && fabsf(ws.Lx) > fabsf(ws.Ly));
+            const unsigned any = __ballot_sync(0xffffffffu, valid);
+            const bool colmajor = 2 * __popc(along_x) > __popc(any);
+            const float2 A = colmajor ? walk_cells(cells_t, P.ny + 1, 1, ncell_m1, ws, c.DQ)
+                                      : walk_cells(cells, 1, P.nx + 1, ncell_m1, ws, c.DQ);
+            if (valid) out[v] = A;
         }
     }
 }
@@ -177,8 +120,7 @@ cudaError_t launch_det_walk(const DevProblem &P, const SrcGeom *sg, const int2 *
         nd = (int)(n_items / P.n_src);
         n_groups = (long long)P.n_src * ((nd + kRays - 1) / kRays);
     }
-    const int nchunks = (nv + 31) / 32;
-    const long long nwork = n_groups * ((nchunks + kChunksPerStrip - 1) / kChunksPerStrip);
+    const long long nwork = n_groups * ((nv + kVoxPerStrip - 1) / kVoxPerStrip);
     long long blocks = (nwork + kWalkWarps - 1) / kWalkWarps;
     if (blocks > 152LL * 64) blocks = 152LL * 64;
     k_det_walk<<<(unsigned)blocks, kWalkThreads, 0, s>>>(P, make_f32_consts(P), sg, pairs, n_items, d0, nd, n_groups,

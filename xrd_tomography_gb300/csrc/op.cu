@@ -629,7 +629,7 @@ int32_t xrdt_op_create(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectr
     memset(&B, 0, sizeof B);
     SrcGeom *d_src;
     PairRec *d_pairs;
-    if ((rc = op_alloc_t(op, 2 * (size_t)(p->nx + 1) * (p->ny + 1), &B.cells)) ||
+    if ((rc = op_alloc_t(op, 4 * (size_t)(p->nx + 1) * (p->ny + 1), &B.cells)) ||
         (rc = op_alloc_t(op, nvox, &B.vox_xy)) || (rc = op_alloc_t(op, nvox, &B.vox_mat)) ||
         (rc = op_alloc_t(op, 4, &B.counters)) || (rc = op_alloc_t(op, p->n_src, &d_src)))
         return bail(rc);

@@ -154,4 +154,70 @@ __device__ __forceinline__ float2 walk_coop(const float4 *__restrict__ cells, in
     return make_float2(s1 * DQ, s2 * DQ);
 }
 
+// The same sum walked cell by cell by one lane.  The bilinear patch of a
+// cell is a polynomial in the sample index, so the samples j = 0 .. m-1 of
+// a run inside one cell add up in closed form: with (u0, v0) the first
+// sample's offset from the cell centre, S1 = m(m-1)/2 and
+// S2 = (m-1)m(2m-1)/6,
+//     sum u = m u0 + Lx S1,   sum v = m v0 + Ly S1,
+//     sum uv = m u0 v0 + (u0 Ly + v0 Lx) S1 + Lx Ly S2,
+//     sum f = m c00 + c10 sum u + c01 sum v + c11 sum uv.
+// Each step takes the cell of its first sample (as cell_sample does) and
+// the run up to the first sample beyond the cell's exit edge, at least one
+// sample.  A sample within rounding of an edge may fall on either side; the
+// interpolant is continuous there, so the sum changes only by rounding.  The
+// runs are added with Kahan compensation.  One cell load serves the 3-4
+// samples of a run (DQ = 1/4 voxel), where the cooperative walk loads a cell
+// per sample.  The samples are taken from the last (next to the voxel) to
+// the first: rays that end on one voxel then start together and part slowly,
+// so the lanes of a warp walking such rays read neighbouring cells.
+// Cell (ci, cj) is cells[2 (ci sx + cj sy)]: sx = 1, sy = NX+1 for the
+// row-major map, sx = NY+1, sy = 1 for the column-major copy.
+__device__ __forceinline__ float2 walk_cells(const float4 *__restrict__ cells, int sx, int sy, unsigned ncell_m1,
+                                             const WalkSetup &w, float DQ)
+{
+    const float magic = 12582912.f;
+    const float nf = (float)w.n;
+    // reversed ray: sample j at R + (n-1-j) L
+    const float2 L = make_float2(-w.Lx, -w.Ly);
+    const float2 R = __ffma2_rn(make_float2(w.Lx, w.Ly), make_float2(nf - 1.f, nf - 1.f), make_float2(w.rx, w.ry));
+    // minus the inverse steps, clamped so that a run is never overestimated
+    const float ilx = fabsf(L.x) > 1e-4f ? -1.f / L.x : (L.x < 0.f ? 1e4f : -1e4f);
+    const float ily = fabsf(L.y) > 1e-4f ? -1.f / L.y : (L.y < 0.f ? 1e4f : -1e4f);
+    const float2 ninv = make_float2(ilx, ily);
+    // exit edge offset h = +-0.5 (towards the step) times the inverse step
+    const float2 hinv = make_float2(L.x < 0.f ? 0.5f * ilx : -0.5f * ilx, L.y < 0.f ? 0.5f * ily : -0.5f * ily);
+    const float lxly = L.x * L.y;
+    float2 acc = make_float2(0.f, 0.f), comp = make_float2(0.f, 0.f);
+    for (float k0 = 0.f; k0 < nf;) {
+        const float2 P0 = __ffma2_rn(L, make_float2(k0, k0), R);
+        const float2 t = __fadd2_rn(P0, make_float2(magic, magic));
+        const int ix = __float_as_int(t.x) - 0x4B400000, iy = __float_as_int(t.y) - 0x4B400000;
+        const unsigned c = min((unsigned)((ix + 1) * sx + (iy + 1) * sy), ncell_m1);
+        const float4 c0 = __ldg(cells + 2 * c), c1 = __ldg(cells + 2 * c + 1);
+        const float2 r = __fadd2_rn(t, make_float2(-magic, -magic));
+        const float2 d = __fadd2_rn(P0, make_float2(-r.x, -r.y));                // (u0, v0), exact
+        const float2 s = __ffma2_rn(d, ninv, hinv);                                // steps to each exit edge
+        // ceil(s) as round(s + 1/2) through the float mantissa (either way at a tie)
+        float m = __fadd_rn(__fadd_rn(__fadd_rn(fminf(s.x, s.y), 0.5f), magic), -magic);
+        m = fminf(fmaxf(m, 1.f), nf - k0);
+        const float S1 = 0.5f * __fmaf_rn(m, m, -m);
+        const float S2 = S1 * __fmaf_rn(m, 2.f / 3.f, -1.f / 3.f);
+        const float2 su = __ffma2_rn(d, make_float2(m, m), __fmul2_rn(L, make_float2(S1, S1)));
+        float suv = __fmul_rn(__fmul_rn(d.x, d.y), m);
+        suv = __fmaf_rn(__fmaf_rn(d.x, L.y, __fmul_rn(d.y, L.x)), S1, suv);
+        suv = __fmaf_rn(lxly, S2, suv);
+        float2 part = __fmul2_rn(make_float2(suv, suv), make_float2(c1.z, c1.w));
+        part = __ffma2_rn(make_float2(su.y, su.y), make_float2(c1.x, c1.y), part);
+        part = __ffma2_rn(make_float2(su.x, su.x), make_float2(c0.z, c0.w), part);
+        part = __ffma2_rn(make_float2(m, m), make_float2(c0.x, c0.y), part);
+        const float2 y = __fadd2_rn(part, make_float2(-comp.x, -comp.y));
+        const float2 tt = __fadd2_rn(acc, y);
+        comp = __fadd2_rn(__fadd2_rn(tt, make_float2(-acc.x, -acc.y)), make_float2(-y.x, -y.y));
+        acc = tt;
+        k0 += m;
+    }
+    return make_float2((acc.x - comp.x) * DQ, (acc.y - comp.y) * DQ);
+}
+
 } // namespace xrdt

@@ -111,7 +111,7 @@ cudaError_t launch_basis_expand(const float *C, long long M, int K, const float 
 
 // k_prep.cu
 struct PrepBuffers {
-    float4 *cells;          // [(ny+1)*(nx+1)*2] bilinear cells
+    float4 *cells;          // [2][(ny+1)*(nx+1)*2] bilinear cells, row- then column-major
     int *vox_xy;            // [nx*ny] packed x | y << 16 of non-empty voxels
     int *vox_mat;           // [nx*ny]
     int *vox_na;            // [nx*ny] Compton table column per voxel
