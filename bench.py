@@ -45,8 +45,13 @@ sys.path.insert(0, ROOT)
 WORKLOAD = 1            # index of the synthetic configuration
 FLUSH_BYTES = 256 << 20
 # DRAM bytes (read + write) of one k_fwd launch, from an ncu capture of
-# this benchmark's command: per workload index
-K_FWD_DRAM_BYTES = {1: 64696320 + 19122176}
+# this benchmark's command: per workload index, the mean over the launches of
+# one step (the projection goes through in tiles of pairs: on the 256x256
+# workload five tiles of 17280 pairs and one of 5760)
+K_FWD_DRAM_BYTES = {1: (5 * (5491107354 + 16549105) + (1862461133 + 5733811)) // 6}
+# issue slots busy in k_fwd (ncu SpeedOfLight, 128x128 workload): the kernel
+# is bound by instruction issue, not by the SFU rate of the roofline below
+K_FWD_ISSUE_BUSY = 0.8255
 
 
 def parse():
@@ -475,7 +480,8 @@ def run_ours(args):
     fwd_n, fwd_ms, fwd_work = ctx.kernel_stats(xt.api.KERNEL_FORWARD)
     kstats = {name: ctx.kernel_stats(k)[:2] for name, k in
               (("prep_map", xt.api.KERNEL_PREP_MAP), ("prep_voxels", xt.api.KERNEL_PREP_VOXELS),
-               ("src_atten", xt.api.KERNEL_SRC_ATTEN), ("forward", xt.api.KERNEL_FORWARD))}
+               ("src_atten", xt.api.KERNEL_SRC_ATTEN), ("walk", xt.api.KERNEL_WALK),
+               ("forward", xt.api.KERNEL_FORWARD))}
     ctx.set_profiling(False)
     clocks = clk.summary()
 
@@ -535,8 +541,12 @@ def run_ours(args):
             "bound": "sfu", "achieved": achieved, "peak": ex2_peak / 1e9, "unit": "G exp2/s",
             "frac": achieved / (ex2_peak / 1e9) if ex2_peak > 0 else None,
             "traffic": K_FWD_DRAM_BYTES.get(args.workload),
-            "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one k_fwd launch "
-                              "(profiles/k_fwd_256x256_dram.md)" if args.workload in K_FWD_DRAM_BYTES else None,
+            "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum per k_fwd launch, mean over "
+                              "the tiles of a step (profiles/k_fwd_256x256_dram.md)"
+                              if args.workload in K_FWD_DRAM_BYTES else None,
+            "issue_slots_busy": K_FWD_ISSUE_BUSY,
+            "issue_source": "ncu sm__instruction_throughput / Issue Slots Busy of k_fwd "
+                            "(profiles/k_fwd_128x128_sections.md)",
             "kernel": "k_fwd (factored forward projector)",
             "work_per_launch": work, "launch_ms": per_launch_ms,
             "peak_source": "measured on this GPU by xrdt_probe_peak (ex2.approx, all SMs)",

@@ -255,10 +255,13 @@ int32_t xrdt_mlem_matrix(xrdt_ctx *ctx, const float *A, int64_t rays, int32_t K,
  * material gives Amatrix.  Rays are ordered as Nphotons, src + det*SRC +
  * nrg*SRC*DET.  The operator is the forward/backward context: creating it
  * stages the attenuation maps, the voxel list, the (source, pixel) pairs and
- * the source-side line integrals once; every forward or adjoint walks the
- * detector-side attenuation of each (pair, voxel) again instead of storing
- * it.  Arrays may be host or device memory; calls synchronise the context's
- * stream before they return.  The context must outlive the operator. */
+ * the source-side line integrals once.  The detector-side attenuation of
+ * each (pair, voxel) is also walked once and kept ([pairs][voxels] float2)
+ * when that table fits in a quarter of the device memory free at creation
+ * and the environment variable XRDT_WALK_CACHE is not "0"; otherwise every
+ * forward or adjoint walks it again.  Arrays may be host or device memory;
+ * calls synchronise the context's stream before they return.  The context
+ * must outlive the operator. */
 typedef struct xrdt_op xrdt_op;
 /* Requires NWT <= 1024 and at most 128 source bins in the spectrum windows. */
 int32_t xrdt_op_create(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum,
@@ -267,6 +270,9 @@ int32_t xrdt_op_create(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectr
 int32_t xrdt_op_destroy(xrdt_op *op);
 /* Number of non-empty voxels (the voxels that carry unknowns), or -1. */
 int64_t xrdt_op_voxels(const xrdt_op *op);
+/* Bytes of the kept detector-side integrals (0: walked in every call), or
+ * -1. */
+int64_t xrdt_op_walk_bytes(const xrdt_op *op);
 /* y [rays] = Av x; x [NX*NY*NWT] (entries of empty voxels are ignored). */
 int32_t xrdt_op_forward(xrdt_op *op, const float *x, float *y, uint32_t flags);
 /* g [NX*NY*NWT] = Av^T w; w [rays]; g is 0 at empty voxels. */

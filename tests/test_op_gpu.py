@@ -41,11 +41,18 @@ def rand_x(inp, seed):
     return x.reshape(-1)
 
 
-def test_tiny_forward_adjoint_match_oracle(ctx, oracle_lib):
+@pytest.mark.parametrize("cached", [True, False])
+def test_tiny_forward_adjoint_match_oracle(ctx, oracle_lib, monkeypatch, cached):
+    """Both ways of getting the detector-side integrals: the operator's table
+    (walked once, cell by cell) and the walk in every call."""
     inp = synth.make_inputs(synth.tiny_problem(), 7)
     p = inp.problem
+    if not cached:
+        monkeypatch.setenv("XRDT_WALK_CACHE", "0")
     op = make_op(inp, ctx)
-    assert op.voxels == int((np.asarray(inp.seg) > 0).sum())
+    nv = int((np.asarray(inp.seg) > 0).sum())
+    assert op.voxels == nv
+    assert op.walk_bytes == (8 * p.n_src * p.n_col * p.n_row * nv if cached else 0)
     x = rand_x(inp, 1)
     rays = np.arange(p.rays)
     w = np.random.default_rng(2).uniform(0.0, 2.0, p.rays).astype(np.float32)

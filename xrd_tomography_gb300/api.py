@@ -57,6 +57,7 @@ SIGNATURES = {
     "xrdt_op_create": (ctypes.c_int32, [_vp, _P, _vp, _vp, _vp, _vp, ctypes.POINTER(_vp)]),
     "xrdt_op_destroy": (ctypes.c_int32, [_vp]),
     "xrdt_op_voxels": (ctypes.c_int64, [_vp]),
+    "xrdt_op_walk_bytes": (ctypes.c_int64, [_vp]),
     "xrdt_op_forward": (ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_uint32]),
     "xrdt_op_adjoint": (ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_uint32]),
     "xrdt_op_mlem": (ctypes.c_int32, [_vp, _vp, _vp, _vp, ctypes.c_int32, ctypes.c_uint32]),
@@ -332,6 +333,11 @@ class Operator:
     @property
     def unknowns(self) -> int:
         return self.p.nx * self.p.ny * self.p.nwt
+
+    @property
+    def walk_bytes(self) -> int:
+        """Bytes of the kept detector-side integrals (0: walked in every call)."""
+        return int(lib().xrdt_op_walk_bytes(self.h))
 
     def close(self):
         # an operator must not outlive its context (xrdt_op_destroy reads it)

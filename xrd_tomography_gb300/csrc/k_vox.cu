@@ -9,9 +9,8 @@
 //                   * G(wvt(v,e) - q_k; sigma(v,e)) * dq_k .
 //
 // With one unknown per (voxel, coarse bin), x[v, k], the forward model is
-// y = Av x and its adjoint g = Av^T w.  Both are computed on the fly: the
-// detector-side attenuation of every (pair, voxel) is walked again in each
-// call, the source-side one comes from the per-(source, voxel) table.
+// y = Av x and its adjoint g = Av^T w.  Both are computed on the fly; the
+// source-side attenuation comes from the per-(source, voxel) table.
 //
 // Every kernel takes a batch of problems (phantoms and scanners of any
 // size, VoxJob); a single operator is a batch of one.  The two heavy kernels
@@ -19,6 +18,10 @@
 // counter -- the (source, pixel) pairs of all problems for the forward, the
 // (voxel chunk, pair group) tiles of all problems for the adjoint -- so that
 // uneven problems share one launch and the tail stays short.
+//
+// When the operator keeps the detector-side integrals of every (pair, voxel)
+// (VoxOp::walk, walked once by k_walk.cu when the operator is created), the
+// kernels read them instead of walking.
 //
 //  * forward (k_vox_fwd): one item = one (source, pixel) pair, as in
 //    k_fwd.cu; lane = source energy sums the coarse bins within 7.5 sigma of
@@ -181,20 +184,32 @@ __device__ __forceinline__ void vox_fwd_pair(const VoxJob &J, int64_t pidx, unsi
         const float vy = ((float)(xy >> 16) + 0.5f) * c.vox;
         const VoxGeom vg = vox_geom(pair.G, vx, vy);
         const float2 Asv = J.op.atten_src[(int64_t)src * nv + v];
+        // the detector-side integral feeds Pin (integrate_diffraction.cu:259-260):
+        // read from the operator's table, or walked here
+        const float2 *wt = J.op.walk;
+        float2 Adv = make_float2(0.f, 0.f);
         WalkSetup ws;
-        if (!walk_setup_f32(P, c, pair.G.Rdx.hi, pair.G.Rdy.hi, vx, vy, &ws))
+        ws.rx = ws.ry = ws.Lx = ws.Ly = 0.f;
+        ws.n = 0;
+        if (wt)
+            Adv = wt[pidx * nv + v];
+        else if (!walk_setup_f32(P, c, pair.G.Rdx.hi, pair.G.Rdy.hi, vx, vy, &ws))
             walk_setup_f64(P, pair.Rdx, pair.Rdy, (double)vx, (double)vy, &ws);
 
         const int nin = min(32, nv - chunk * 32);
         for (int i = 0; i < nin; i++) {
-            WalkSetup wi;
-            wi.rx = __shfl_sync(0xffffffffu, ws.rx, i);
-            wi.ry = __shfl_sync(0xffffffffu, ws.ry, i);
-            wi.Lx = __shfl_sync(0xffffffffu, ws.Lx, i);
-            wi.Ly = __shfl_sync(0xffffffffu, ws.Ly, i);
-            wi.n = __shfl_sync(0xffffffffu, ws.n, i);
-            // the detector-side integral feeds Pin (integrate_diffraction.cu:259-260)
-            const float2 Ad = walk_coop(J.op.cells, P.nx, P.ny, wi, DQf, lane);
+            float2 Ad;
+            if (wt) {
+                Ad = make_float2(__shfl_sync(0xffffffffu, Adv.x, i), __shfl_sync(0xffffffffu, Adv.y, i));
+            } else {
+                WalkSetup wi;
+                wi.rx = __shfl_sync(0xffffffffu, ws.rx, i);
+                wi.ry = __shfl_sync(0xffffffffu, ws.ry, i);
+                wi.Lx = __shfl_sync(0xffffffffu, ws.Lx, i);
+                wi.Ly = __shfl_sync(0xffffffffu, ws.Ly, i);
+                wi.n = __shfl_sync(0xffffffffu, ws.n, i);
+                Ad = walk_coop(J.op.cells, P.nx, P.ny, wi, DQf, lane);
+            }
             const float sh = __shfl_sync(0xffffffffu, vg.s.hi, i);
             const float sl = __shfl_sync(0xffffffffu, vg.s.lo, i);
             const float sg = __shfl_sync(0xffffffffu, vg.sg, i);
@@ -348,18 +363,29 @@ k_vox_adj(const VoxBatch B)
             const int src = (int)(pp % P.n_src);
             const VoxGeom vg = vox_geom(pr.G, vx, vy);
             const float2 Asv = J.op.atten_src[(int64_t)src * nv + v];
+            const float2 *wt = J.op.walk;
+            float2 Adv = make_float2(0.f, 0.f);
             WalkSetup ws;
-            if (!walk_setup_f32(P, c, pr.G.Rdx.hi, pr.G.Rdy.hi, vx, vy, &ws))
+            ws.rx = ws.ry = ws.Lx = ws.Ly = 0.f;
+            ws.n = 0;
+            if (wt)
+                Adv = wt[pp * nv + v];
+            else if (!walk_setup_f32(P, c, pr.G.Rdx.hi, pr.G.Rdy.hi, vx, vy, &ws))
                 walk_setup_f64(P, pr.Rdx, pr.Rdy, (double)vx, (double)vy, &ws);
             const float *wp = J.what + pp * E;
             for (int i = 0; i < nin; i++) {
-                WalkSetup wi;
-                wi.rx = __shfl_sync(0xffffffffu, ws.rx, i);
-                wi.ry = __shfl_sync(0xffffffffu, ws.ry, i);
-                wi.Lx = __shfl_sync(0xffffffffu, ws.Lx, i);
-                wi.Ly = __shfl_sync(0xffffffffu, ws.Ly, i);
-                wi.n = __shfl_sync(0xffffffffu, ws.n, i);
-                const float2 Ad = walk_coop(J.op.cells, P.nx, P.ny, wi, DQf, lane);
+                float2 Ad;
+                if (wt) {
+                    Ad = make_float2(__shfl_sync(0xffffffffu, Adv.x, i), __shfl_sync(0xffffffffu, Adv.y, i));
+                } else {
+                    WalkSetup wi;
+                    wi.rx = __shfl_sync(0xffffffffu, ws.rx, i);
+                    wi.ry = __shfl_sync(0xffffffffu, ws.ry, i);
+                    wi.Lx = __shfl_sync(0xffffffffu, ws.Lx, i);
+                    wi.Ly = __shfl_sync(0xffffffffu, ws.Ly, i);
+                    wi.n = __shfl_sync(0xffffffffu, ws.n, i);
+                    Ad = walk_coop(J.op.cells, P.nx, P.ny, wi, DQf, lane);
+                }
                 const float sh = __shfl_sync(0xffffffffu, vg.s.hi, i);
                 const float sl = __shfl_sync(0xffffffffu, vg.s.lo, i);
                 const float sg = __shfl_sync(0xffffffffu, vg.sg, i);

@@ -26,6 +26,7 @@ struct xrdt_op {
     std::vector<void *> allocs;
     int groups_cap = 1;                   // rows of part: the most adjoint pair groups
     int64_t rays = 0;
+    int64_t walk_bytes = 0;               // kept detector-side integrals
     bool sens_ready = false;              // sens holds Av^T 1
     // device buffers
     int32_t *seg = nullptr;
@@ -661,6 +662,31 @@ int32_t xrdt_op_create(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectr
         return bail(XRDT_ERR_CUDA);
     }
 
+    // detector-side integrals of every (pair, voxel), walked once here when
+    // the table fits in a quarter of the free device memory
+    float2 *d_walk = nullptr;
+    const char *wc = getenv("XRDT_WALK_CACHE");
+    if (nv > 0 && !(wc && strcmp(wc, "0") == 0)) {
+        const size_t bytes = sizeof(float2) * (size_t)npairs * nv;
+        size_t fr = 0, tot = 0;
+        if ((e = cudaMemGetInfo(&fr, &tot)) != cudaSuccess) {
+            cudaGetLastError();
+            fr = 0;
+        }
+        if (bytes <= fr / 4) {
+            void *w;
+            if ((rc = op_alloc(op, bytes, &w))) return bail(rc);
+            d_walk = (float2 *)w;
+            if ((e = launch_det_walk(P, d_src, nullptr, 0, npairs, B.vox_xy, nv, B.cells, d_walk, st,
+                                     &ctx->launches)) != cudaSuccess) {
+                cudaGetLastError();
+                fail(ctx, XRDT_ERR_CUDA, fmt("detector-side integrals: %s", cudaGetErrorString(e)));
+                return bail(XRDT_ERR_CUDA);
+            }
+            op->walk_bytes = (int64_t)bytes;
+        }
+    }
+
     // per-energy tables
     HostTables ht;
     build_host_tables(p, P, hspec.data(), &ht);
@@ -709,6 +735,7 @@ int32_t xrdt_op_create(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectr
     op->v.vox_xy = B.vox_xy;
     op->v.cells = B.cells;
     op->v.atten_src = B.atten_src;
+    op->v.walk = d_walk;
 
     // work buffers
     int sms = 0;
@@ -762,6 +789,8 @@ int32_t xrdt_op_destroy(xrdt_op *op)
 }
 
 int64_t xrdt_op_voxels(const xrdt_op *op) { return op ? (int64_t)op->v.nv : -1; }
+
+int64_t xrdt_op_walk_bytes(const xrdt_op *op) { return op ? op->walk_bytes : -1; }
 
 int32_t xrdt_op_forward(xrdt_op *op, const float *x, float *y, uint32_t flags)
 {

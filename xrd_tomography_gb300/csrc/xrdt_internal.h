@@ -185,6 +185,7 @@ struct VoxOp {
     const int *vox_xy;
     const float4 *cells;
     const float2 *atten_src;
+    const float2 *walk;        // [n_src * n_det][nv] detector-side integrals, or NULL
 };
 cudaError_t launch_compact_voxels(const DevProblem &P, const int32_t *seg, PrepBuffers &B, cudaStream_t s,
                                   int64_t *launches);
