@@ -263,8 +263,10 @@ k_fwd(const FwdArgs args)
                     const float half = kSig * sig2 * rs;
                     if (WITH_N) {
                         const float jc = (w_hi - qlo_f) * inv_dqf - 0.5f;
-                        const int jlo = max(ceil_nc(jc - half * inv_dqf), 0);
-                        int jhi = min(floor_nc(jc + half * inv_dqf), P.nqf - 1);
+                        // bounded floors: the indices are clamped to the grid and an
+                        // empty window is skipped
+                        const int jlo = max(ceil_bounded(jc - half * inv_dqf), 0);
+                        int jhi = min(floor_bounded(jc + half * inv_dqf), P.nqf - 1);
                         float acc = 0.f;
                         // pref == 0: the attenuation factor underflowed, every term is 0
                         if (jlo <= jhi && pref != 0.f) {
@@ -319,19 +321,21 @@ k_fwd(const FwdArgs args)
                         // channels overlapped by [E1, E2]/eratio (an FP32 misjudgement at a
                         // channel edge drops an overlap below 1e-6 of the bin width)
                         float fn0;
-                        int n0 = floor_nc((Eo_lo * inv_er - edmin) * inv_dEd, &fn0);
+                        // bounded floors: n0 is raised to the window, n1 lowered to it,
+                        // and an empty range is skipped
+                        int n0 = floor_bounded((Eo_lo * inv_er - edmin) * inv_dEd, &fn0);
                         if (n0 < wn[2 * el]) {
                             n0 = wn[2 * el];
                             fn0 = en_wn0f[el];
                         }
-                        const int n1 = min(wn[2 * el + 1], floor_nc(((Eo_lo + dEsf) * inv_er - edmin) * inv_dEd));
+                        const int n1 = min(wn[2 * el + 1], floor_bounded(((Eo_lo + dEsf) * inv_er - edmin) * inv_dEd));
                         if (n0 <= n1) {
                             const float wC = ein * sh;
                             const float arg = eratio + wC * wC;
                             const float l2 = lg2_approx(wC * arg * rsqrt_approx(arg) * inv_er);
                             const float tq = (l2 - qmin_t) * inv_dqt;
                             float ftq;
-                            int nq = floor_nc(tq, &ftq);
+                            int nq = floor_bounded(tq, &ftq);   // clamped to the table below
                             const float fr = tq - ftq;
                             if (!(fr > 2e-4f && fr < 1.f - 2e-4f))  // near a table edge
                                 nq = compton_bin_f64(P, args.T.energy[eg].ein, oh, ol);
@@ -342,7 +346,7 @@ k_fwd(const FwdArgs args)
                             const float Xc = fmaf(Asx, rcp_approx(f1), Asy * rcp_approx(f2));
                             const float Pc = ex2_approx(-(Xin + Xc) * kLog2e);
                             nexp += 1;
-                            if (Pc == 0.f) continue;   // underflow: no contribution
+                            // an underflowed Pc adds exact zeros below: no branch
                             const float Cf = eratio * eratio * (eratio + inv_er - 1.f + cos2) * 0.5f;
                             const float base = Pc * gp * Cf * a2now * S2[nq + na * P.nq];
                             const float span = dEsf * inv_er;   // Eout2 - Eout1
@@ -355,13 +359,27 @@ k_fwd(const FwdArgs args)
                             const float *oe = offse + (size_t)el * SL - wlo;
                             const float bs = base * inv_span;
                             float Ed1 = fmaf(fn0, dEdf, edmin);
-                            for (int n = n0; n <= n1; n++, Ed1 += dEdf) {
-                                // outgoing range relative to the channel's left edge:
-                                // u1 = Eout1 - Edet1 = ((Esrc1 - Edet1) - Edet1*x)/eratio
-                                const float u1 = fmaf(-Ed1, x, oe[n]) * inv_er;
-                                const float u2 = u1 + span;
-                                const float ov = fminf(u2, dEdf) - fmaxf(u1, 0.f);
-                                if (ov > 0.f) cs[n] += ov * bs;
+                            // outgoing range relative to the channel's left edge:
+                            // u1 = Eout1 - Edet1 = ((Esrc1 - Edet1) - Edet1*x)/eratio.
+                            // The range is one source bin wide over eratio >= 1, so
+                            // with dEs <= dEd it meets at most two channels: those
+                            // two straight-line, any further ones in a loop.
+                            {
+                                const float u1 = fmaf(-Ed1, x, oe[n0]) * inv_er;
+                                const float ov = fminf(u1 + span, dEdf) - fmaxf(u1, 0.f);
+                                if (ov > 0.f) cs[n0] += ov * bs;
+                            }
+                            if (n0 < n1) {
+                                const float Ed2 = Ed1 + dEdf;
+                                const float u1 = fmaf(-Ed2, x, oe[n0 + 1]) * inv_er;
+                                const float ov = fminf(u1 + span, dEdf) - fmaxf(u1, 0.f);
+                                if (ov > 0.f) cs[n0 + 1] += ov * bs;
+                                Ed1 = Ed2 + dEdf;
+                                for (int n = n0 + 2; n <= n1; n++, Ed1 += dEdf) {
+                                    const float u1n = fmaf(-Ed1, x, oe[n]) * inv_er;
+                                    const float ovn = fminf(u1n + span, dEdf) - fmaxf(u1n, 0.f);
+                                    if (ovn > 0.f) cs[n] += ovn * bs;
+                                }
                             }
                         }
                     }

@@ -171,6 +171,28 @@ __device__ __forceinline__ int floor_nc(float x)
 // ceil(x) = -floor(-x), same range
 __device__ __forceinline__ int ceil_nc(float x) { return -floor_nc(-x); }
 
+// floor_nc without the clamp, for arguments bounded well inside |x| < 2^22
+// by construction.  Outside that range (infinite or NaN arguments included)
+// the result is an arbitrary int: every caller clamps it into a table or
+// tests for an empty range before using it as an index.
+__device__ __forceinline__ int floor_bounded(float x, float *fl)
+{
+    const float t = x + 12582912.f;
+    const float r = t - 12582912.f;
+    const int i = __float_as_int(t) - 0x4B400000;
+    const bool up = r > x;
+    *fl = up ? r - 1.f : r;
+    return up ? i - 1 : i;
+}
+
+__device__ __forceinline__ int floor_bounded(float x)
+{
+    float fl;
+    return floor_bounded(x, &fl);
+}
+
+__device__ __forceinline__ int ceil_bounded(float x) { return -floor_bounded(-x); }
+
 __device__ inline double warp_sum(double v)
 {
 #pragma unroll
