@@ -54,7 +54,10 @@ __device__ __forceinline__ bool group_ray(const DevProblem &P, const int2 *pairs
     return true;
 }
 
-__global__ void __launch_bounds__(kWalkThreads, 6)
+// 8 blocks (32 warps) per SM: the walk waits on L1 latency, and at 64
+// registers (8 bytes spilled around the FP64 fallback call) it ran 1016 ms on
+// the 256x256 workload against 1089 ms at 6 blocks and 80 registers.
+__global__ void __launch_bounds__(kWalkThreads, 8)
 k_det_walk(DevProblem P, F32Consts c, const SrcGeom *__restrict__ sg, const int2 *__restrict__ pairs,
            long long n_items, int d0, int nd, long long n_groups, const int *__restrict__ vox_xy, int nv,
            const float4 *__restrict__ cells, float2 *__restrict__ tab)
