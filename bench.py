@@ -48,10 +48,10 @@ FLUSH_BYTES = 256 << 20
 # this benchmark's command: per workload index, the mean over the launches of
 # one step (the projection goes through in tiles of pairs: on the 256x256
 # workload five tiles of 17280 pairs and one of 5760)
-K_FWD_DRAM_BYTES = {1: (5 * (5491107354 + 16549105) + (1862461133 + 5733811)) // 6}
+K_FWD_DRAM_BYTES = {1: (5 * (5486237455 + 16250158) + (1863039180 + 6348800)) // 6}
 # issue slots busy in k_fwd (ncu SpeedOfLight, 128x128 workload): the kernel
 # is bound by instruction issue, not by the SFU rate of the roofline below
-K_FWD_ISSUE_BUSY = 0.8255
+K_FWD_ISSUE_BUSY = 0.8338
 
 
 def parse():

@@ -13,9 +13,10 @@
 //  * Gaussian q-resolution sums (:299-315) run over the bins within 7.5 sigma
 //    of the wavevector transfer only (each dropped term is below 7e-13 of the
 //    peak); the reference sums every fine bin.
-//  * The detector-side line integral is a warp-cooperative walk over the
-//    bilinear cell map; the source-side one comes from a per-(source, voxel)
-//    table (k_prep.cu), since it does not depend on the detector pixel.
+//  * The detector-side line integrals of the block's pair come from the table
+//    that k_det_walk (k_walk.cu) writes for the current tile of pairs, one
+//    float2 per voxel; the source-side ones from a per-(source, voxel) table
+//    (k_prep.cu), since they do not depend on the detector pixel.
 //  * Scattering geometry, ROI entry points and sample counts are FP64; the
 //    wavevector transfer is carried as a float pair (about 48 significant
 //    bits) because the Gaussian at 3 sigma amplifies its relative error by
@@ -23,10 +24,10 @@
 //    voxels.
 //
 // Work split inside a block (8 warps): warp w takes voxel chunks w, w+8, ...
-// of 32 voxels.  For a chunk, lane = voxel computes the FP64 geometry; then
-// for each voxel of the chunk the warp walks its detector-side ray together
-// and lane = source energy evaluates the (voxel, energy) term, so each lane
-// keeps the running sum of its own energies in registers.
+// of 32 voxels.  For a chunk, lane = voxel computes the scattering geometry
+// and reads the voxel's line integrals; then for each voxel of the chunk
+// lane = source energy evaluates the (voxel, energy) term and adds it to the
+// warp's compensated per-energy sums.
 #include "scatter.cuh"
 
 namespace xrdt {
