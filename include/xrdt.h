@@ -152,7 +152,8 @@ int64_t xrdt_ctx_launch_count(const xrdt_ctx *ctx);
 #define XRDT_KERNEL_CT          10 /* transmission sinogram                          */
 #define XRDT_KERNEL_BASIS       11 /* basis expansion on the tensor cores            */
 #define XRDT_KERNEL_WALK        12 /* detector-side line integrals of the forward    */
-#define XRDT_KERNEL_COUNT       13
+#define XRDT_KERNEL_SPECTRUM    13 /* spectrum-response matrix builder               */
+#define XRDT_KERNEL_COUNT       14
 /* With profiling on, every launch is bracketed by CUDA events on the
  * context's stream and the forward kernel counts the exponentials it
  * evaluates.  Off by default; turning it on or off clears the statistics. */
@@ -201,6 +202,22 @@ int32_t xrdt_forward_rays(xrdt_ctx *ctx, const xrdt_problem *p,
                           uint32_t flags);
 
 /* ---- MLEM with an explicit model matrix (main.m:154-176) --------------- */
+/* The spectrum-response matrix of spectrum_builder.m:64-95, the spectrum
+ * input of xrdt_forward (prhs[0]).  A fine source spectrum -- bin edges
+ * e_hd [n_hd+1] in keV, increasing, and photons per keV n_hd [n_hd]
+ * (spectrum_builder.m:22-30) -- is spread over detector energies with a
+ * Gaussian of width sigma(E) = sigma0 + sigma1 E (:65; the reference's
+ * 0.5 (1.61 + 0.025 E) is sigma0 = 0.805, sigma1 = 0.0125) and integrated
+ * over each pair of a coarse source bin (src_edges [ns+1]) and a coarse
+ * detector bin (det_edges [nd+1]) with the bins' overlap lengths as weights
+ * (:75-91).  spectrum [ns, nd] column-major: (s, d) at s + d*ns.  The
+ * reference uses one grid for both axes; separate grids are the same sum.
+ * Requires nd <= 65535 and sigma(E) > 0 at every fine bin centre.  Arrays
+ * may be host or device memory; FP64 arithmetic, output rounded to float. */
+int32_t xrdt_spectrum_build(xrdt_ctx *ctx, const float *e_hd, const float *n_hd, int32_t n_hd_bins,
+                            const float *src_edges, int32_t ns, const float *det_edges, int32_t nd,
+                            double sigma0, double sigma1, float *spectrum, uint32_t flags);
+
 /* ---- basis expansion on the tensor cores -----------------------------
  * I[M x N] = C[M x K] B[K x N], row-major, FP32 accuracy through 3xTF32 on
  * tcgen05 (FP32 accumulation in tensor memory).  The reference's coarse q

@@ -27,7 +27,7 @@ FWD_PLAIN_FP64 = 0x1
 FWD_NO_SYNC = 0x2
 OP_PLAIN_FP64 = 0x1
 (KERNEL_PREP_MAP, KERNEL_PREP_VOXELS, KERNEL_SRC_ATTEN, KERNEL_FORWARD, KERNEL_PLAIN, KERNEL_GATHER,
- KERNEL_MLEM, KERNEL_VOX_FORWARD, KERNEL_VOX_ADJOINT, KERNEL_VOX_UPDATE, KERNEL_CT, KERNEL_BASIS, KERNEL_WALK) = range(13)
+ KERNEL_MLEM, KERNEL_VOX_FORWARD, KERNEL_VOX_ADJOINT, KERNEL_VOX_UPDATE, KERNEL_CT, KERNEL_BASIS, KERNEL_WALK, KERNEL_SPECTRUM) = range(14)
 
 _P = ctypes.POINTER(Problem)
 _vp = ctypes.c_void_p
@@ -65,6 +65,8 @@ SIGNATURES = {
     "xrdt_basis_expand": (ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp, ctypes.c_int32, _vp,
                                            ctypes.c_uint32]),
     "xrdt_ct_sinogram": (ctypes.c_int32, [_vp, _P, _vp, _vp, _vp, _vp, _vp, ctypes.c_uint32]),
+    "xrdt_spectrum_build": (ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_int32, _vp, ctypes.c_int32, _vp, ctypes.c_int32,
+                                             ctypes.c_double, ctypes.c_double, _vp, ctypes.c_uint32]),
     "xrdt_batch_create": (ctypes.c_int32, [_vp, _vp, ctypes.c_int32, ctypes.POINTER(_vp)]),
     "xrdt_batch_destroy": (ctypes.c_int32, [_vp]),
     "xrdt_batch_forward": (ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_uint32]),
@@ -258,6 +260,31 @@ def basis_expand(C, B, I=None, ctx: Context | None = None):
     pi, ki = _ptr(I, np.float32)
     _check(lib().xrdt_basis_expand(ctx.h, pc, M, K, pb, N, pi, 0), ctx.h)
     return ki
+
+
+def spectrum_build(e_hd, n_hd, src_edges, det_edges, sigma0=0.805, sigma1=0.0125, out=None,
+                   ctx: Context | None = None):
+    """xrdt_spectrum_build: the spectrum-response matrix of
+    spectrum_builder.m:64-95 from a fine source spectrum (bin edges e_hd
+    [H+1] in keV, photons per keV n_hd [H]) on coarse source and detector
+    bins.  Returns the column-major flat [NS, ND] vector that forward()
+    takes as its spectrum (numpy unless out is a torch CUDA tensor)."""
+    ctx = ctx or default_context()
+
+    def numel(a):
+        return int(a.numel()) if hasattr(a, "numel") else int(np.size(a))
+
+    ns = numel(src_edges) - 1
+    nd = numel(det_edges) - 1
+    nh = numel(n_hd)
+    if numel(e_hd) != nh + 1:
+        raise ValueError("e_hd must hold one more edge than n_hd has bins")
+    if out is None:
+        out = np.empty(ns * nd, np.float32)
+    ptrs = [_ptr(a, np.float32) for a in (e_hd, n_hd, src_edges, det_edges, out)]
+    _check(lib().xrdt_spectrum_build(ctx.h, ptrs[0][0], ptrs[1][0], nh, ptrs[2][0], ns, ptrs[3][0], nd,
+                                     float(sigma0), float(sigma1), ptrs[4][0], 0), ctx.h)
+    return ptrs[4][1]
 
 
 def ct_sinogram(p: Problem, spectrum, a1, a2, Tphotons=None, gain0=None, ctx: Context | None = None):

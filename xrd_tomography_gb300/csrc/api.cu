@@ -40,6 +40,7 @@ enum Slot {
     S_SRCG, S_ENERGY, S_RFWIN, S_OFFS, S_WINLO, S_WINN, S_FINEQ, S_COARSEQ, S_COARSEQD,
     S_RAYS, S_PAIRS, S_NC, S_CC, S_AC,
     S_MA, S_MY, S_MC, S_MX, S_MPART, S_MSENS, S_BC, S_BB, S_BI, S_ERR, S_WALK,
+    S_SPFINE, S_SPSRC, S_SPDET, S_SPOUT,
     S_COUNT
 };
 
@@ -843,6 +844,86 @@ int32_t xrdt_basis_expand(xrdt_ctx *ctx, const float *C, int64_t M, int32_t K, c
     if (hostI) CK(cudaMemcpyAsync(I, dI, sizeof(float) * (size_t)M * N, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     if (ctx->h_counters[2]) return fail(ctx, XRDT_ERR_TIMEOUT, "the tensor-core accumulator never completed");
+    return XRDT_OK;
+}
+
+int32_t xrdt_spectrum_build(xrdt_ctx *ctx, const float *e_hd, const float *n_hd, int32_t n_hd_bins,
+                            const float *src_edges, int32_t ns, const float *det_edges, int32_t nd, double sigma0,
+                            double sigma1, float *spectrum, uint32_t flags)
+{
+    if (!ctx) return XRDT_ERR_NULL;
+    ctx->err.clear();
+    if (!e_hd || !n_hd || !src_edges || !det_edges || !spectrum)
+        return fail(ctx, XRDT_ERR_NULL, "a required array pointer is NULL");
+    if (n_hd_bins < 1 || ns < 1 || nd < 1 || nd > 65535)
+        return fail(ctx, XRDT_ERR_DIMS, "need n_hd_bins >= 1, ns >= 1 and 1 <= nd <= 65535");
+    if (flags) return fail(ctx, XRDT_ERR_UNSUPPORTED, "unknown flag bits");
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    // the inputs are small: read them to the host (from either memory)
+    std::vector<float> e((size_t)n_hd_bins + 1), n((size_t)n_hd_bins), es((size_t)ns + 1), ed((size_t)nd + 1);
+    CK(cudaMemcpy(e.data(), e_hd, sizeof(float) * e.size(), cudaMemcpyDefault));
+    CK(cudaMemcpy(n.data(), n_hd, sizeof(float) * n.size(), cudaMemcpyDefault));
+    CK(cudaMemcpy(es.data(), src_edges, sizeof(float) * es.size(), cudaMemcpyDefault));
+    CK(cudaMemcpy(ed.data(), det_edges, sizeof(float) * ed.size(), cudaMemcpyDefault));
+    auto increasing = [](const std::vector<float> &v) {
+        for (size_t i = 0; i < v.size(); i++) {
+            if (!std::isfinite(v[i])) return false;
+            if (i && !(v[i] > v[i - 1])) return false;
+        }
+        return true;
+    };
+    if (!increasing(e) || !increasing(es) || !increasing(ed))
+        return fail(ctx, XRDT_ERR_INPUT, "bin edges must be finite and increasing");
+    // fine bins (spectrum_builder.m:26, :65, :75)
+    std::vector<SpecFineBin> fb((size_t)n_hd_bins);
+    const double rsqrt2pi = 1.0 / std::sqrt(2.0 * 3.14159265358979323846);
+    for (int h = 0; h < n_hd_bins; h++) {
+        const double l = e[h], r = e[h + 1], c = 0.5 * (l + r);
+        const double sig = sigma0 + sigma1 * c;
+        if (!(sig > 0.0) || !std::isfinite(sig) || !std::isfinite((double)n[h]))
+            return fail(ctx, XRDT_ERR_INPUT, fmt("sigma(E) = %g at fine bin %d: need a positive width and finite counts",
+                                                 sig, h));
+        fb[h] = SpecFineBin{l, r, c, 1.0 / (2.0 * sig * sig), (double)n[h] * rsqrt2pi / sig};
+    }
+    // coarse bins with the range of fine bins that overlap them
+    auto coarse = [&](const std::vector<float> &edges) {
+        std::vector<SpecCoarseBin> cb(edges.size() - 1);
+        int h0 = 0;
+        for (size_t k = 0; k + 1 < edges.size(); k++) {
+            const double e1 = edges[k], e2 = edges[k + 1];
+            while (h0 < n_hd_bins && !(fb[h0].right > e1)) h0++;
+            int h1 = h0;
+            while (h1 < n_hd_bins && fb[h1].left < e2) h1++;
+            cb[k] = SpecCoarseBin{e1, e2, h0, h1};
+        }
+        return cb;
+    };
+    const std::vector<SpecCoarseBin> sb = coarse(es), db = coarse(ed);
+    int rc;
+    void *dfb, *dsb, *ddb;
+    if ((rc = get_buf(ctx, S_SPFINE, sizeof(SpecFineBin) * fb.size(), &dfb)) ||
+        (rc = get_buf(ctx, S_SPSRC, sizeof(SpecCoarseBin) * sb.size(), &dsb)) ||
+        (rc = get_buf(ctx, S_SPDET, sizeof(SpecCoarseBin) * db.size(), &ddb)))
+        return rc;
+    CK(cudaMemcpyAsync(dfb, fb.data(), sizeof(SpecFineBin) * fb.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dsb, sb.data(), sizeof(SpecCoarseBin) * sb.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ddb, db.data(), sizeof(SpecCoarseBin) * db.size(), cudaMemcpyHostToDevice, st));
+    const size_t out_bytes = sizeof(float) * (size_t)ns * nd;
+    const bool host_out = !is_device_ptr(spectrum);
+    float *dout = spectrum;
+    if (host_out) {
+        void *tmp;
+        if ((rc = get_buf(ctx, S_SPOUT, out_bytes, &tmp))) return rc;
+        dout = (float *)tmp;
+    }
+    {
+        ProfScope ps(ctx, XRDT_KERNEL_SPECTRUM);
+        CK(launch_spectrum((const SpecFineBin *)dfb, (const SpecCoarseBin *)dsb, ns, (const SpecCoarseBin *)ddb, nd,
+                           dout, st, &ctx->launches));
+    }
+    if (host_out) CK(cudaMemcpyAsync(spectrum, dout, out_bytes, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));   // the host tables above leave scope
     return XRDT_OK;
 }
 

@@ -151,6 +151,20 @@ cudaError_t launch_fast_forward(const DevProblem &P, const SrcGeom *d_src, const
                                 const int2 *pairs, long long n_list, long long p0, int n_pairs,
                                 const float2 *walk, float *N, float *C, float *A, cudaStream_t s,
                                 int64_t *launches);
+// k_spectrum.cu: the spectrum-response matrix (spectrum_builder.m:64-95).
+// A fine bin: edges, centre, 1/(2 sigma^2) and n/(sqrt(2 pi) sigma); a coarse
+// bin: edges and the range [h0, h1) of fine bins that overlap it.
+struct SpecFineBin {
+    double left, right, centre, inv_2s2, amp;
+};
+struct SpecCoarseBin {
+    double e1, e2;
+    int h0, h1;
+};
+// out[s + d*ns] for every coarse source bin s < ns and detector bin d < nd.
+cudaError_t launch_spectrum(const SpecFineBin *fb, const SpecCoarseBin *sb, int ns, const SpecCoarseBin *db, int nd,
+                            float *out, cudaStream_t s, int64_t *launches);
+
 // k_walk.cu: tab[item][v] = detector-side line integral of voxel v for the
 // pair pairs[item] (or the linear pair p0 + item), item < n_items.  Linear
 // pairs come in whole pixels: p0 and n_items multiples of SRC.

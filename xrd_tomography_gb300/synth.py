@@ -120,6 +120,21 @@ def kramers_spectrum(p: Problem, kvp=80.0, lines=((59.3, 0.35), (67.2, 0.12)),
     return S.astype(np.float32).flatten(order="F")
 
 
+def hd_spectrum(kvp=80.0, e_min=8.0, de=0.05, n=1440, lines=((59.3, 0.35), (67.2, 0.12)), total=1.0e9):
+    """A fine source spectrum in the form spectrum_builder.m:22-30 reads its
+    measured one: bin edges [n+1] (keV) and photons per keV [n].  Kramers
+    bremsstrahlung (kvp - E)/E plus Gaussian K lines (0.5 keV wide, heights
+    relative to the continuum at the line), scaled to total photons; the
+    default grid is the reference's 1440 bins of 0.05 keV from 8 to 80 keV."""
+    edges = e_min + de * np.arange(n + 1)
+    E = 0.5 * (edges[:-1] + edges[1:])
+    N = np.clip(kvp - E, 0.0, None) / E
+    for (El, h) in lines:
+        N = N + h * np.exp(-0.5 * ((E - El) / 0.5) ** 2) * (kvp / El)
+    N *= total / max(float((N * de).sum()), 1e-300)
+    return edges.astype(np.float32), N.astype(np.float32)
+
+
 def _s2_table(rng, nq, na):
     qq = np.linspace(0.0, 1.0, nq)[:, None]
     aa = np.linspace(0.0, 1.0, na)[None, :]
