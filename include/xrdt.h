@@ -201,6 +201,31 @@ int32_t xrdt_forward_rays(xrdt_ctx *ctx, const xrdt_problem *p,
                           float *Nphotons, float *Cphotons, float *A_rows,
                           uint32_t flags);
 
+/* The integer decisions of the fast forward path, for bit-exact comparison
+ * with an FP64 restatement (a test export: the float outputs of
+ * xrdt_forward would hide a one-bin flip under their tolerance).  For the
+ * listed rays (linear indices as in xrdt_forward_rays) and every non-empty
+ * voxel v in the reference's loop order (x outer, y inner;
+ * integrate_diffraction.cu:173-177), made by the same device functions the
+ * production kernels call:
+ *   win  [n_rays][2]     source-energy window lo, hi (find_src_nrg_range.cu:8-25)
+ *   walk [n_rays][nv][4] detector-side sample count and ROI edge entered, then
+ *                        the same for the source side (attenuator.cu:19-52,
+ *                        GetIntersection.cu:9-57; edges in its order bottom,
+ *                        right, top, left; -1 = missed)
+ *   nq   [n_rays][nv][2*dnrg+1]  Compton table bin per window energy
+ *                        (integrate_diffraction.cu:331-337)
+ *   na   [nv]            Compton table column (integrate_diffraction.cu:177-189)
+ *   s2u8 [nq*na]         the quantised table (integrate_diffraction.cu:66-74)
+ * nv (the number of voxels with seg > 0) is returned in *nv; the caller sizes
+ * walk, nq and na for it.  All lists and outputs are host memory;
+ * n_rays <= 65535. */
+int32_t xrdt_debug_decisions(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum,
+                             const int32_t *seg, const float *a1, const float *a2, const float *S2,
+                             float q_min, float q_max, float a_min, float a_max,
+                             const int64_t *rays, int64_t n_rays, int32_t *win, int32_t *walk,
+                             int32_t *na, int32_t *nq, uint8_t *s2u8, int64_t *nv);
+
 /* ---- MLEM with an explicit model matrix (main.m:154-176) --------------- */
 /* The spectrum-response matrix of spectrum_builder.m:64-95, the spectrum
  * input of xrdt_forward (prhs[0]).  A fine source spectrum -- bin edges
@@ -253,7 +278,8 @@ int32_t xrdt_ct_sinogram(xrdt_ctx *ctx, const xrdt_problem *p, const float *spec
  * K contiguous floats -- exactly the Amatrix buffer xrdt_forward writes, K =
  * nwt*n_mat, rays = xrdt_problem_rays (main.m:140 uses its transpose
  * reshape).  y[rays] are measured counts, c[rays] the Compton bias
- * (main.m:162 uses Cphotons(:)).  K must be a multiple of 4, at most 1024.
+ * (main.m:162 uses Cphotons(:)).  K must be a multiple of 4, at most 1024;
+ * device arrays A and x must be 16-byte aligned (XRDT_ERR_UNSUPPORTED).
  * The iteration body is a fused pass over A (one read of A per iteration)
  * and an FP64 reduction/update, replayed as a CUDA graph. */
 int32_t xrdt_mlem_matrix(xrdt_ctx *ctx, const float *A, int64_t rays, int32_t K,
@@ -351,10 +377,11 @@ int32_t xrdt_batch_tune(xrdt_batch *batch, int32_t *adj_warps, int64_t *adj_tile
  * scratch is a fixed 2 MiB + 8 KiB array in the library that every device
  * using it keeps until process exit; K is limited to 1024 as in
  * xrdt_mlem_matrix (larger K: XRDT_ERR_DIMS).  A, y, c and x must be device
- * memory (else XRDT_ERR_UNSUPPORTED); work is queued on `stream` (a
- * cudaStream_t, NULL for the default stream) on the current device and the
- * call returns after the stream has finished.  The first call on a device
- * looks up the scratch address, so make it before any stream capture.  All
+ * memory of the current device, with A and x 16-byte aligned (else
+ * XRDT_ERR_UNSUPPORTED); work is queued on `stream` (a cudaStream_t, NULL
+ * for the default stream) and the call returns after the stream has
+ * finished: it synchronises the stream, so it cannot run inside a stream
+ * capture.  The first call on a device looks up the scratch address.  All
  * calls share the scratch: calls that overlap on the GPU race. */
 int32_t xrdt_mlem_matrix_noalloc(const float *A, int64_t rays, int32_t K,
                                  const float *y, const float *c, float *x,

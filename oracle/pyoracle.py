@@ -16,7 +16,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libxrdt_ref.so")
-REF_SRC = "/root/reference/Forward_projector_kernels"
+# the reference checkout beside the repository, or $XRDT_REF_SRC
+REF_ROOT = os.environ.get("XRDT_REF_SRC") or os.path.abspath(os.path.join(HERE, "..", "..", "reference"))
+REF_SRC = os.path.join(REF_ROOT, "Forward_projector_kernels")
 
 _f = ctypes.POINTER(ctypes.c_float)
 _d = ctypes.POINTER(ctypes.c_double)
@@ -30,7 +32,7 @@ def build(ref: bool | None = None) -> None:
     if ref is None:
         ref = os.path.isdir(REF_SRC)
     if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + REF_ROOT], check=True)
 
 
 _lib = None
@@ -46,6 +48,7 @@ def lib():
         _lib.xrdt_oracle_forward_rays.restype = ctypes.c_int32
         _lib.xrdt_oracle_vox_rays.restype = ctypes.c_int32
         _lib.xrdt_oracle_ct_rays.restype = ctypes.c_int32
+        _lib.xrdt_oracle_decisions.restype = ctypes.c_int32
         _lib.xrdt_oracle_attenuator.restype = ctypes.c_int64
         _lib.xrdt_oracle_get_intersection.restype = ctypes.c_int32
     return _lib
@@ -90,6 +93,34 @@ def forward_rays(inp, rays, want_a=False, want_av=False, threads=0):
     if rc != 0:
         raise ValueError("oracle rejected the input (material id above n_mat)")
     return N, C, A, Av
+
+
+def decisions(inp, rays, threads=0):
+    """The integer decisions of the FP64 forward for the listed rays: a dict
+    of win [n, 2], walk [n, nv, 4] (detector samples, detector edge, source
+    samples, source edge), nq [n, nv, 2*dnrg+1], na [nv] and s2u8 [nq*na];
+    non-empty voxels in the reference's loop order."""
+    p = inp.problem
+    rays = np.ascontiguousarray(rays, np.int64)
+    n = rays.size
+    seg = np.ascontiguousarray(inp.seg, np.int32)
+    nv = int((seg > 0).sum())
+    W = 2 * p.dnrg + 1
+    out = {"win": np.zeros((n, 2), np.int32), "walk": np.zeros((n, nv, 4), np.int32),
+           "nq": np.zeros((n, nv, W), np.int32), "na": np.zeros(max(nv, 1), np.int32),
+           "s2u8": np.zeros(p.nq * p.na, np.uint8)}
+    keep = [np.ascontiguousarray(x, np.float32) for x in (inp.spectrum, inp.Ifine, inp.a1, inp.a2, inp.S2)]
+    rc = lib().xrdt_oracle_decisions(
+        ctypes.byref(p), keep[0].ctypes.data_as(_f), keep[1].ctypes.data_as(_f), seg.ctypes.data_as(_i32),
+        keep[2].ctypes.data_as(_f), keep[3].ctypes.data_as(_f), keep[4].ctypes.data_as(_f),
+        ctypes.c_float(inp.q_min), ctypes.c_float(inp.q_max), ctypes.c_float(inp.a_min), ctypes.c_float(inp.a_max),
+        rays.ctypes.data_as(_i64), ctypes.c_int64(n), out["win"].ctypes.data_as(_i32),
+        out["walk"].ctypes.data_as(_i32), out["na"].ctypes.data_as(_i32), out["nq"].ctypes.data_as(_i32),
+        out["s2u8"].ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), ctypes.c_int32(threads))
+    if rc != 0:
+        raise ValueError("oracle rejected the input (material id above n_mat)")
+    out["na"] = out["na"][:nv]
+    return out
 
 
 def vox_rays(inp, rays, x=None, w=None, threads=0):

@@ -75,8 +75,19 @@ void xrdt_oracle_src_nrg_range(const xrdt_problem *p, int32_t nrg, int32_t *lo, 
 /* GetIntersection.cu:9-57: first of the four ROI edges (bottom, right, top,
  * left) that the segment (x1,y1)->(x2,y2) crosses, with the 1e-5 tolerances
  * of :20,:39,:43,:47; NaN if none. */
+static int get_intersection_edge(double x1, double y1, double x2, double y2, int32_t nx, int32_t ny,
+                                 double *rx, double *ry);
+
 int32_t xrdt_oracle_get_intersection(double x1, double y1, double x2, double y2,
                                      int32_t nx, int32_t ny, double *rx, double *ry)
+{
+    return get_intersection_edge(x1, y1, x2, y2, nx, ny, rx, ry) >= 0;
+}
+
+/* The same, returning the index of the edge entered (0..3 in the order
+ * above) or -1. */
+static int get_intersection_edge(double x1, double y1, double x2, double y2, int32_t nx, int32_t ny,
+                                 double *rx, double *ry)
 {
     const double NX = (double)nx, NY = (double)ny;
     const double x3[4] = {0.0, NX, NX, 0.0};
@@ -100,12 +111,12 @@ int32_t xrdt_oracle_get_intersection(double x1, double y1, double x2, double y2,
                 if (u_b > -eps && u_b < 1.0 + eps) {
                     *rx = x1 + x2_x1 * u_a;
                     *ry = y1 + y2_y1 * u_a;
-                    return 1;
+                    return i;
                 }
             }
         }
     }
-    return 0;
+    return -1;
 }
 
 /* tex2D of Forward_XRD.cu:229-233: linear filtering, unnormalised
@@ -138,14 +149,27 @@ static void tex_bilinear(const float *a1, const float *a2, int nx, int ny,
 /* attenuator.cu:9-109.  Samples at r_int + Lhat*(DQ*k) for every k with
  * DQ*k <= Lr (:44-69), k below maxBatch*threads (:44, integrate_diffraction.cu:160-161),
  * summed then multiplied by DQ (:104-105). */
+static int64_t attenuator_edge(const xrdt_problem *p, const float *a1, const float *a2,
+                               double ex, double ey, double vx, double vy,
+                               double *A1, double *A2, int *edge);
+
 int64_t xrdt_oracle_attenuator(const xrdt_problem *p, const float *a1, const float *a2,
                                double ex, double ey, double vx, double vy,
                                double *A1, double *A2)
 {
+    return attenuator_edge(p, a1, a2, ex, ey, vx, vy, A1, A2, NULL);
+}
+
+/* The same, also reporting the ROI edge the ray enters through. */
+static int64_t attenuator_edge(const xrdt_problem *p, const float *a1, const float *a2,
+                               double ex, double ey, double vx, double vy,
+                               double *A1, double *A2, int *edge)
+{
     const int NX = p->nx, NY = p->ny;
     const double DQ = p->dq_step;
     double rx, ry;
-    xrdt_oracle_get_intersection(ex, ey, vx, vy, NX, NY, &rx, &ry);
+    const int e = get_intersection_edge(ex, ey, vx, vy, NX, NY, &rx, &ry);
+    if (edge) *edge = e;
     double Lx = vx - rx, Ly = vy - ry;
     double Lr = sqrt(Lx * Lx + Ly * Ly);
     double rL = 1.0 / sqrt(Lx * Lx + Ly * Ly);
@@ -180,8 +204,13 @@ static void forward_one_ray(const xrdt_problem *p, const float *spectrum, const 
                             const unsigned char *S2u8, const coarse_bin *cb,
                             double q_min, double q_max, double a_min, double a_max,
                             int64_t ray, double *N_out, double *C_out, double *A_row,
-                            double *Av_row, const double *xv, double *yv, double *gv, double wgt)
+                            double *Av_row, const double *xv, double *yv, double *gv, double wgt,
+                            int32_t *dec_walk, int32_t *dec_nq, int32_t *dec_na)
 {
+    /* dec_*: where set, the integer decisions of every non-empty voxel in loop
+     * order: walk[v] = (detector-side samples, its edge, source-side samples,
+     * its edge), nq[v][j] for source bin nrg_src_min + j, na[v]. */
+    int64_t dec_v = 0;
     /* Per-voxel mode (xv or gv set): only the coarse-q model row matters. */
     const int want_nc = !(xv || gv);
     const int NX = p->nx, NY = p->ny;
@@ -282,8 +311,17 @@ static void forward_one_ray(const xrdt_problem *p, const float *spectrum, const 
             /* :259-260 -- the detector-side integral is named A_src2vox and
              * the source-side one A_vox2det; kept as written. */
             double As2v_x, As2v_y, Av2d_x, Av2d_y;
-            xrdt_oracle_attenuator(p, a1, a2, Rdet_x, Rdet_y, Rvox_x, Rvox_y, &As2v_x, &As2v_y);
-            xrdt_oracle_attenuator(p, a1, a2, Rsrc_x, Rsrc_y, Rvox_x, Rvox_y, &Av2d_x, &Av2d_y);
+            int edge_d, edge_s;
+            int64_t n_d = attenuator_edge(p, a1, a2, Rdet_x, Rdet_y, Rvox_x, Rvox_y, &As2v_x, &As2v_y, &edge_d);
+            int64_t n_s = attenuator_edge(p, a1, a2, Rsrc_x, Rsrc_y, Rvox_x, Rvox_y, &Av2d_x, &Av2d_y, &edge_s);
+            if (dec_walk) {
+                int32_t *w4 = dec_walk + 4 * dec_v;
+                w4[0] = (int32_t)n_d;
+                w4[1] = edge_d;
+                w4[2] = (int32_t)n_s;
+                w4[3] = edge_s;
+            }
+            if (dec_na) dec_na[dec_v] = na;
 
             for (int nrg_src = nrg_src_min; nrg_src <= nrg_src_max; nrg_src++) { /* :266 */
                 double Esrc1 = p->e_src_min + (double)nrg_src * dEs;
@@ -334,6 +372,7 @@ static void forward_one_ray(const xrdt_problem *p, const float *spectrum, const 
                 int nq = cuda_floor_int((log2wvt - q_min) / dq);
                 if (nq < 0) nq = 0;
                 else if (nq >= NQ) nq = NQ - 1;
+                if (dec_nq) dec_nq[dec_v * (2 * p->dnrg + 1) + (nrg_src - nrg_src_min)] = nq;
                 f1 = eout * eout * eout;
                 f2 = p->kn0 + p->kn1 * eout + p->kn2 * eout * eout;
                 double Pout_c = exp(-(Av2d_x / f1 + Av2d_y / f2));
@@ -341,6 +380,7 @@ static void forward_one_ray(const xrdt_problem *p, const float *spectrum, const 
                 Cnow += channel_match * Pin * Pout_c * RF * geomproduct * Compton_factor * a2now *
                         (double)S2u8[nq + na * NQ];
             }
+            dec_v++;
         }
     }
     *N_out = Nnow;
@@ -385,10 +425,56 @@ int32_t xrdt_oracle_forward_rays(const xrdt_problem *p,
         if (Av_row) memset(Av_row, 0, sizeof(double) * (size_t)avrow);
         forward_one_ray(p, spectrum, Ifine, seg, a1, a2, S2u8, cb,
                         (double)q_min, (double)q_max, (double)a_min, (double)a_max,
-                        rays[i], &N_out[i], &C_out[i], A_row, Av_row, NULL, NULL, NULL, 0.0);
+                        rays[i], &N_out[i], &C_out[i], A_row, Av_row, NULL, NULL, NULL, 0.0, NULL, NULL, NULL);
     }
     free(cb);
     free(S2u8);
+    return 0;
+}
+
+/* The integer decisions of forward_one_ray for the listed rays (every
+ * non-empty voxel in loop order): the source-energy window, the ROI edge and
+ * sample count of both line integrals, the Compton table bin per window
+ * energy and column per voxel, and the u8 table.  walk [n][nv][4], nq
+ * [n][nv][2*dnrg+1], na [nv], win [n][2], s2u8 [nq*na]. */
+int32_t xrdt_oracle_decisions(const xrdt_problem *p, const float *spectrum, const float *Ifine,
+                              const int32_t *seg, const float *a1, const float *a2, const float *S2,
+                              float q_min, float q_max, float a_min, float a_max,
+                              const int64_t *rays, int64_t n_rays, int32_t *win, int32_t *walk,
+                              int32_t *na, int32_t *nq, uint8_t *s2u8, int32_t n_threads)
+{
+    const int64_t nvox = (int64_t)p->nx * p->ny;
+    int64_t nv = 0;
+    for (int64_t i = 0; i < nvox; i++) {
+        if (seg[i] > p->n_mat) return -1;
+        if (seg[i] > 0) nv++;
+    }
+    const int64_t nS = (int64_t)p->nq * p->na;
+    for (int64_t i = 0; i < nS; i++) {
+        int s = cuda_floor_int((double)S2[i]);
+        if (s < 0) s = 0;
+        else if (s > 255) s = 255;
+        s2u8[i] = (uint8_t)s;
+    }
+    coarse_bin *cb = (coarse_bin *)malloc(sizeof(coarse_bin) * (size_t)p->nwt);
+    for (int k = 0; k < p->nwt; k++) xrdt_oracle_wvt_value(p, k, &cb[k].qnow, &cb[k].dqnow);
+    const int W = 2 * p->dnrg + 1;
+#ifdef _OPENMP
+    if (n_threads > 0) omp_set_num_threads(n_threads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+    for (int64_t i = 0; i < n_rays; i++) {
+        const int nrg = (int)(rays[i] / ((int64_t)p->n_src * p->n_col * p->n_row));
+        int lo, hi;
+        xrdt_oracle_src_nrg_range(p, nrg, &lo, &hi);
+        win[2 * i] = lo;
+        win[2 * i + 1] = hi;
+        double nn, cc;
+        forward_one_ray(p, spectrum, Ifine, seg, a1, a2, s2u8, cb, (double)q_min, (double)q_max,
+                        (double)a_min, (double)a_max, rays[i], &nn, &cc, NULL, NULL, NULL, NULL, NULL, 0.0,
+                        walk + i * nv * 4, nq + i * nv * W, i == 0 ? na : NULL);
+    }
+    free(cb);
     return 0;
 }
 
@@ -426,7 +512,8 @@ int32_t xrdt_oracle_vox_rays(const xrdt_problem *p, const float *spectrum, const
         double nn = 0.0, cc = 0.0, yy = 0.0;
         /* one pass per ray: the forward sum and the adjoint accumulation */
         forward_one_ray(p, spectrum, NULL, seg, a1, a2, NULL, cb, 0.0, 1.0, 0.0, 1.0, rays[i], &nn, &cc,
-                        NULL, NULL, x, &yy, gpriv ? gpriv + (size_t)t * (size_t)ng : NULL, w ? w[i] : 0.0);
+                        NULL, NULL, x, &yy, gpriv ? gpriv + (size_t)t * (size_t)ng : NULL, w ? w[i] : 0.0,
+                        NULL, NULL, NULL);
         if (y_out) y_out[i] = yy;
     }
     if (g_out) {

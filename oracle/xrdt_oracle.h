@@ -66,6 +66,18 @@ int32_t xrdt_oracle_vox_rays(const xrdt_problem *p, const float *spectrum, const
                              const int64_t *rays, int64_t n_rays, double *y_out, double *g_out,
                              int32_t n_threads);
 
+/* The integer decisions of the FP64 forward for the listed rays and every
+ * non-empty voxel in loop order: win [n][2] source-energy window,
+ * walk [n][nv][4] (detector-side samples, ROI edge, source-side samples, ROI
+ * edge), nq [n][nv][2*dnrg+1] Compton table bins, na [nv] Compton table
+ * columns, s2u8 [nq*na] quantised table.  Returns 0, or -1 for a material id
+ * above n_mat. */
+int32_t xrdt_oracle_decisions(const xrdt_problem *p, const float *spectrum, const float *Ifine,
+                              const int32_t *seg, const float *a1, const float *a2, const float *S2,
+                              float q_min, float q_max, float a_min, float a_max,
+                              const int64_t *rays, int64_t n_rays, int32_t *win, int32_t *walk,
+                              int32_t *na, int32_t *nq, uint8_t *s2u8, int32_t n_threads);
+
 /* Transmission through the map per listed ray (Nphotons index) and the
  * same without the phantom: Tphotons and gain0 of the CT sinogram. */
 int32_t xrdt_oracle_ct_rays(const xrdt_problem *p, const float *spectrum, const float *a1, const float *a2,

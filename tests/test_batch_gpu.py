@@ -6,11 +6,10 @@ import pytest
 
 import xrd_tomography_gb300 as xt
 from xrd_tomography_gb300 import synth
-from tests.tolerances import FAST_RTOL, max_rel_err
+from tests.tolerances import FAST_RTOL, MLEM_FLOOR, MLEM_RTOL, max_rel_err
 
 pytestmark = pytest.mark.gpu
 
-MLEM_RTOL = 1e-4
 
 
 @pytest.fixture(scope="module")
@@ -105,7 +104,7 @@ def test_batch_mlem_matches_single_operators(ctx, torch_cuda):
     batch.mlem(ys, cs, xb, 2)      # continues from the current estimates
     torch.cuda.synchronize()
     for k in range(len(ops)):
-        assert max_rel_err(xb[k].cpu().numpy(), singles[k].cpu().numpy(), floor=1e-4) < MLEM_RTOL, k
+        assert max_rel_err(xb[k].cpu().numpy(), singles[k].cpu().numpy(), floor=MLEM_FLOOR) < MLEM_RTOL, k
     with pytest.raises(ValueError):
         batch.forward([x.cpu() for x in x0], ys)
     batch.close()

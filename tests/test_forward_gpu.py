@@ -117,8 +117,12 @@ def test_repeat_calls_agree(ctx):
     p = inp.problem
     a = xt.forward(p, *inp.args(), ctx=ctx)
     b = xt.forward(p, *inp.args(), ctx=ctx)
-    for x, y in zip(a, b):
-        assert max_rel_err(x, y) < 1e-6
+    # N and C: no atomics and a fixed summation order, the same bits every time
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])
+    # the model matrix adds the warps' voxel chunks with shared-memory
+    # atomics, whose order varies: a few ulps at most
+    np.testing.assert_array_max_ulp(a[2], b[2], maxulp=4)
 
 
 # ---- reference configuration, against the reference's own outputs --------

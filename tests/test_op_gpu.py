@@ -6,11 +6,9 @@ import pytest
 
 import xrd_tomography_gb300 as xt
 from xrd_tomography_gb300 import synth
-from tests.tolerances import FAST_RTOL, PLAIN_RTOL, max_rel_err
+from tests.tolerances import FAST_RTOL, MLEM_FLOOR, MLEM_RTOL, PLAIN_RTOL, max_rel_err
 
 pytestmark = pytest.mark.gpu
-
-MLEM_RTOL = 1e-4   # FP32 iterates with FP64 sums, after tens of iterations
 
 
 @pytest.fixture(scope="module")
@@ -202,10 +200,17 @@ def test_tiny_mlem_matches_dense_restatement(ctx, oracle_lib):
     c = c * (ybar.max() / 1e3)
     x0 = np.where(np.repeat(np.asarray(inp.seg).reshape(-1) > 0, p.nwt), 1.0, 0.0)
     op = make_op(inp, ctx)
-    for iters in (1, 5, 20):
-        x = op.mlem(y.astype(np.float32), c.astype(np.float32), x0.astype(np.float32), iters)
-        xr = mlem_dense(A, y, c, x0, iters)
-        assert max_rel_err(x, xr, floor=1e-4) < MLEM_RTOL, iters
+    y32, c32 = y.astype(np.float32), c.astype(np.float32)
+    # Through 20 iterations every estimate is within MLEM_RTOL of FP64.  At 50
+    # the largest element error is 1.3-1.6e-5: the operator's entries carry
+    # about 1e-6 relative error where a ray is strongly attenuated (exp(-X)
+    # with X up to 17 at the lowest energies, from FP32 line integrals good
+    # to 6e-8), and a per-unknown bias of the adjoint grows about 15-fold over
+    # 50 updates.  That bound is asserted separately below.
+    for iters, tol in ((1, MLEM_RTOL), (5, MLEM_RTOL), (20, MLEM_RTOL), (50, 2 * MLEM_RTOL)):
+        x = op.mlem(y32, c32, x0.astype(np.float32), iters)
+        xr = mlem_dense(A, y32.astype(np.float64), c32.astype(np.float64), x0, iters)
+        assert max_rel_err(x, xr, floor=MLEM_FLOOR) < tol, iters
     op.close()
 
 
@@ -235,7 +240,7 @@ def test_full_size_mlem_graph_equals_composed_calls(ctx, torch_cuda):
     x = x0.clone()
     op.mlem(y, c, x, 3)
     torch.cuda.synchronize()
-    assert max_rel_err(x.cpu().numpy(), xr.cpu().numpy(), floor=1e-4) < MLEM_RTOL
+    assert max_rel_err(x.cpu().numpy(), xr.cpu().numpy(), floor=MLEM_FLOOR) < MLEM_RTOL
     # the estimate moves towards the data: the Poisson log-likelihood rises
     def loglik(xx):
         m = op.forward(xx, torch.empty(p.rays, device="cuda")).double() + c.double()

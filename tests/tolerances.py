@@ -7,12 +7,17 @@ since a count 1e-6 times smaller than its neighbours carries no information
 at FP32 accumulation.
 PLAIN_RTOL: the FP64 kernel at the reference's launch shape, whose outputs are
 rounded to float once.
+MLEM_RTOL: an MLEM estimate after up to 50 iterations against the same
+iterations in FP64, element by element above MLEM_FLOOR times the largest
+entry (below it against that floor).
 """
 import numpy as np
 
 FAST_RTOL = 1e-5
 PLAIN_RTOL = 1e-6
 FLOOR = 1e-6
+MLEM_RTOL = 1e-5
+MLEM_FLOOR = 1e-4
 
 
 def max_rel_err(got, ref, floor=FLOOR):

@@ -75,6 +75,9 @@ SIGNATURES = {
     "xrdt_batch_tune": (ctypes.c_int32, [_vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int64),
                                          ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
     "xrdt_op_adjoint_rays": (ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_int64, _vp, ctypes.c_uint32]),
+    "xrdt_debug_decisions": (ctypes.c_int32, [_vp, _P, _vp, _vp, _vp, _vp, _vp, ctypes.c_float, ctypes.c_float,
+                                              ctypes.c_float, ctypes.c_float, _vp, ctypes.c_int64, _vp, _vp, _vp,
+                                              _vp, _vp, ctypes.POINTER(ctypes.c_int64)]),
     "xrdt_forward_rays": (ctypes.c_int32, [_vp, _P, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_float,
                                            ctypes.c_float, ctypes.c_float, ctypes.c_float, _vp, ctypes.c_int64,
                                            _vp, _vp, _vp, ctypes.c_uint32]),
@@ -245,6 +248,34 @@ def forward_rays(p: Problem, rays, spectrum, Ifine, seg, a1, a2, S2, q_min, q_ma
     return N, C, A
 
 
+def debug_decisions(p: Problem, rays, spectrum, seg, a1, a2, S2, q_min, q_max, a_min, a_max,
+                    ctx: Context | None = None):
+    """xrdt_debug_decisions: the fast path's integer decisions for the listed
+    rays, as a dict of numpy arrays: win [n, 2], walk [n, nv, 4] (detector
+    samples, detector edge, source samples, source edge), nq [n, nv, W],
+    na [nv], s2u8 [nq*na]; voxels in the reference's loop order."""
+    ctx = ctx or default_context()
+    rays = np.ascontiguousarray(rays, np.int64)
+    n = rays.size
+    nv_max = int((np.asarray(seg) > 0).sum())
+    W = 2 * p.dnrg + 1
+    win = np.zeros((n, 2), np.int32)
+    walk = np.zeros((n, nv_max, 4), np.int32)
+    nq = np.zeros((n, nv_max, W), np.int32)
+    na = np.zeros(max(nv_max, 1), np.int32)
+    s2u8 = np.zeros(p.nq * p.na, np.uint8)
+    nv = ctypes.c_int64()
+    keep = [np.ascontiguousarray(a, dt) for a, dt in ((spectrum, np.float32), (seg, np.int32), (a1, np.float32),
+                                                      (a2, np.float32), (S2, np.float32))]
+    _check(lib().xrdt_debug_decisions(ctx.h, ctypes.byref(p), *[k.ctypes.data for k in keep], float(q_min),
+                                      float(q_max), float(a_min), float(a_max), rays.ctypes.data, n,
+                                      win.ctypes.data, walk.ctypes.data, na.ctypes.data, nq.ctypes.data,
+                                      s2u8.ctypes.data, ctypes.byref(nv)), ctx.h)
+    if nv.value != nv_max:
+        raise RuntimeError("voxel count mismatch")
+    return {"win": win, "walk": walk, "nq": nq, "na": na[:nv_max], "s2u8": s2u8}
+
+
 def basis_expand(C, B, I=None, ctx: Context | None = None):
     """xrdt_basis_expand: I = C @ B in FP32 (3xTF32 on the tensor cores).
     C [M, K] and B [K, N] row-major; returns I [M, N] (numpy unless I is a
@@ -328,6 +359,12 @@ def mlem_matrix_noalloc(A, y, c, x, iters: int, stream: int | None = None):
     for t in (A, y, c, x):
         if not hasattr(t, "data_ptr") or not t.is_cuda or not t.is_contiguous():
             raise ValueError("xrdt_mlem_matrix_noalloc takes contiguous CUDA tensors only")
+        if str(t.dtype) != "torch.float32":
+            raise ValueError("xrdt_mlem_matrix_noalloc takes float32 tensors only")
+    # the kernels read A[rays, K], y[rays] and c[rays] without host staging:
+    # a short buffer would be read out of bounds on the device
+    if A.numel() != y.numel() * x.numel() or c.numel() != y.numel():
+        raise ValueError("need A.numel() == y.numel() * x.numel() and c.numel() == y.numel()")
     _check(lib().xrdt_mlem_matrix_noalloc(A.data_ptr(), int(y.numel()), int(x.numel()), y.data_ptr(),
                                           c.data_ptr(), x.data_ptr(), iters, _vp(stream) if stream else None))
     return x

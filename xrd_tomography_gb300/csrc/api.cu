@@ -40,7 +40,7 @@ enum Slot {
     S_SRCG, S_ENERGY, S_RFWIN, S_OFFS, S_WINLO, S_WINN, S_FINEQ, S_COARSEQ, S_COARSEQD,
     S_RAYS, S_PAIRS, S_NC, S_CC, S_AC,
     S_MA, S_MY, S_MC, S_MX, S_MPART, S_MSENS, S_BC, S_BB, S_BI, S_ERR, S_WALK,
-    S_SPFINE, S_SPSRC, S_SPDET, S_SPOUT,
+    S_SPFINE, S_SPSRC, S_SPDET, S_SPOUT, S_DWALK, S_DNQ,
     S_COUNT
 };
 
@@ -263,8 +263,12 @@ void build_host_tables(const xrdt_problem *p, const DevProblem &P, const float *
         const double wf = 2.0 * r.Esrc / P.hbarc;
         r.wfac_hi = (float)wf;
         r.wfac_lo = (float)(wf - (double)r.wfac_hi);
-        r.sig_c1 = (float)((2.0 / P.hbarc) * (2.0 / P.hbarc) * P.dEs * P.dEs / 12.0);
-        r.sig_c2 = (float)((r.Esrc / P.hbarc) * (r.Esrc / P.hbarc) / 4.0);
+        const double c1 = (2.0 / P.hbarc) * (2.0 / P.hbarc) * P.dEs * P.dEs / 12.0;
+        const double c2 = (r.Esrc / P.hbarc) * (r.Esrc / P.hbarc) / 4.0;
+        r.sig_c1 = (float)c1;
+        r.sig_c2 = (float)c2;
+        r.sig_c1_lo = (float)(c1 - (double)r.sig_c1);
+        r.sig_c2_lo = (float)(c2 - (double)r.sig_c2);
         r.einf = (float)r.ein;
         r.Esrc1f = (float)r.Esrc1;
         r.Esrc2f = (float)r.Esrc2;
@@ -808,6 +812,102 @@ int32_t xrdt_forward_rays(xrdt_ctx *ctx, const xrdt_problem *p, const float *spe
                         rays ? rays : &none, n_rays, Nphotons, Cphotons, A_rows, flags);
 }
 
+int32_t xrdt_debug_decisions(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, const int32_t *seg,
+                             const float *a1, const float *a2, const float *S2, float q_min, float q_max,
+                             float a_min, float a_max, const int64_t *rays, int64_t n_rays, int32_t *win,
+                             int32_t *walk, int32_t *na, int32_t *nq, uint8_t *s2u8, int64_t *nv_out)
+{
+    if (!ctx) return XRDT_ERR_NULL;
+    ctx->err.clear();
+    if (!p || !spectrum || !seg || !a1 || !a2 || !S2 || !nv_out || (n_rays && (!rays || !win || !walk || !nq)) ||
+        !na || !s2u8)
+        return fail(ctx, XRDT_ERR_NULL, "a required array pointer is NULL");
+    int rc = xrdt_problem_validate(p);
+    if (rc) return fail(ctx, rc, fmt("problem rejected: %s", xrdt_status_string(rc)));
+    if (n_rays < 0 || n_rays > 65535) return fail(ctx, XRDT_ERR_DIMS, "need 0 <= n_rays <= 65535");
+    const int64_t all_rays = xrdt_problem_rays(p);
+    for (int64_t i = 0; i < n_rays; i++)
+        if (rays[i] < 0 || rays[i] >= all_rays)
+            return fail(ctx, XRDT_ERR_INPUT, fmt("ray %lld out of range", (long long)rays[i]));
+    for (const void *q : {(const void *)rays, (const void *)win, (const void *)walk, (const void *)na,
+                          (const void *)nq, (const void *)s2u8})
+        if (q && is_device_ptr(q)) return fail(ctx, XRDT_ERR_UNSUPPORTED, "lists and outputs must be host memory");
+    DevProblem P;
+    std::string err;
+    build_dev_problem(p, q_min, q_max, a_min, a_max, &P, &err);
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const int64_t nvox = (int64_t)p->nx * p->ny;
+    const void *d_spec, *d_seg, *d_a1, *d_a2, *d_S2;
+    if ((rc = stage_in(ctx, S_SPEC, spectrum, sizeof(float) * p->nrg_src * p->nrg_det, &d_spec))) return rc;
+    if ((rc = stage_in(ctx, S_SEG, seg, sizeof(int32_t) * nvox, &d_seg))) return rc;
+    if ((rc = stage_in(ctx, S_A1, a1, sizeof(float) * nvox, &d_a1))) return rc;
+    if ((rc = stage_in(ctx, S_A2, a2, sizeof(float) * nvox, &d_a2))) return rc;
+    if ((rc = stage_in(ctx, S_S2, S2, sizeof(float) * (size_t)p->nq * p->na, &d_S2))) return rc;
+    // the production preparation: voxel list, Compton columns, cell map, u8 table
+    std::vector<SrcGeom> hsg(p->n_src);
+    for (int s = 0; s < p->n_src; s++) src_geom(p, s, &hsg[s]);
+    void *d_srcg, *tmp;
+    if ((rc = get_buf(ctx, S_SRCG, sizeof(SrcGeom) * p->n_src, &d_srcg))) return rc;
+    CK(cudaMemcpyAsync(d_srcg, hsg.data(), sizeof(SrcGeom) * p->n_src, cudaMemcpyHostToDevice, st));
+    PrepBuffers B;
+    memset(&B, 0, sizeof B);
+    if ((rc = get_buf(ctx, S_CELLS, sizeof(float4) * 4 * (size_t)(p->nx + 1) * (p->ny + 1), &tmp))) return rc;
+    B.cells = (float4 *)tmp;
+    if ((rc = get_buf(ctx, S_VXY, sizeof(int) * nvox, &tmp))) return rc;
+    B.vox_xy = (int *)tmp;
+    if ((rc = get_buf(ctx, S_VMAT, sizeof(int) * nvox, &tmp))) return rc;
+    B.vox_mat = (int *)tmp;
+    if ((rc = get_buf(ctx, S_VNA, sizeof(int) * nvox, &tmp))) return rc;
+    B.vox_na = (int *)tmp;
+    if ((rc = get_buf(ctx, S_VA2, sizeof(float) * nvox, &tmp))) return rc;
+    B.vox_a2 = (float *)tmp;
+    if ((rc = get_buf(ctx, S_CNT, sizeof(int) * 4, &tmp))) return rc;
+    B.counters = (int *)tmp;
+    if ((rc = get_buf(ctx, S_S2U8, (size_t)p->nq * p->na, &tmp))) return rc;
+    B.s2u8 = (unsigned char *)tmp;
+    CK(launch_prep_voxels(P, (const int32_t *)d_seg, (const float *)d_a1, (const float *)d_a2, B, st,
+                          &ctx->launches));
+    CK(launch_prep_map(P, (const float *)d_a1, (const float *)d_a2, (const float *)d_S2, B, st, &ctx->launches));
+    CK(cudaMemcpyAsync(ctx->h_counters, B.counters, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    const int nv = ctx->h_counters[0];
+    if (ctx->h_counters[1])
+        return fail(ctx, XRDT_ERR_INPUT, fmt("segmentation holds a material id above n_mat = %d", p->n_mat));
+    *nv_out = nv;
+    std::vector<float> hspec((size_t)p->nrg_src * p->nrg_det);
+    CK(cudaMemcpy(hspec.data(), d_spec, sizeof(float) * hspec.size(), cudaMemcpyDeviceToHost));
+    HostTables ht;
+    build_host_tables(p, P, hspec.data(), &ht);
+    const int W = 2 * p->dnrg + 1;
+    for (int64_t i = 0; i < n_rays; i++) {
+        const int nrg = (int)(rays[i] / ((int64_t)p->n_src * P.n_det));
+        win[2 * i] = ht.win_lo[nrg];
+        win[2 * i + 1] = ht.win_lo[nrg] + W - 1;
+    }
+    CK(cudaMemcpyAsync(s2u8, B.s2u8, (size_t)p->nq * p->na, cudaMemcpyDeviceToHost, st));
+    if (nv > 0) CK(cudaMemcpyAsync(na, B.vox_na, sizeof(int) * nv, cudaMemcpyDeviceToHost, st));
+    if (n_rays > 0 && nv > 0) {
+        void *d_energy, *d_wlo, *d_rays, *d_walk, *d_nq;
+        if ((rc = get_buf(ctx, S_ENERGY, sizeof(EnergyRow) * ht.energy.size(), &d_energy))) return rc;
+        CK(cudaMemcpyAsync(d_energy, ht.energy.data(), sizeof(EnergyRow) * ht.energy.size(), cudaMemcpyHostToDevice,
+                           st));
+        if ((rc = get_buf(ctx, S_WINLO, sizeof(int) * ht.win_lo.size(), &d_wlo))) return rc;
+        CK(cudaMemcpyAsync(d_wlo, ht.win_lo.data(), sizeof(int) * ht.win_lo.size(), cudaMemcpyHostToDevice, st));
+        if ((rc = get_buf(ctx, S_RAYS, sizeof(int64_t) * n_rays, &d_rays))) return rc;
+        CK(cudaMemcpyAsync(d_rays, rays, sizeof(int64_t) * n_rays, cudaMemcpyHostToDevice, st));
+        if ((rc = get_buf(ctx, S_DWALK, sizeof(int4) * (size_t)n_rays * nv, &d_walk))) return rc;
+        if ((rc = get_buf(ctx, S_DNQ, sizeof(int) * (size_t)n_rays * nv * W, &d_nq))) return rc;
+        CK(launch_decisions(P, (const SrcGeom *)d_srcg, (const EnergyRow *)d_energy, (const int *)d_wlo,
+                            (const int64_t *)d_rays, (int)n_rays, B.vox_xy, nv, (int4 *)d_walk, (int *)d_nq, st,
+                            &ctx->launches));
+        CK(cudaMemcpyAsync(walk, d_walk, sizeof(int4) * (size_t)n_rays * nv, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(nq, d_nq, sizeof(int) * (size_t)n_rays * nv * W, cudaMemcpyDeviceToHost, st));
+    }
+    CK(cudaStreamSynchronize(st));
+    return XRDT_OK;
+}
+
 int32_t xrdt_basis_expand(xrdt_ctx *ctx, const float *C, int64_t M, int32_t K, const float *B, int32_t N, float *I,
                           uint32_t flags)
 {
@@ -1013,6 +1113,8 @@ int32_t xrdt_mlem_matrix(xrdt_ctx *ctx, const float *A, int64_t rays, int32_t K,
         dx = (float *)tmp;
         CK(cudaMemcpyAsync(dx, x, sizeof(float) * K, cudaMemcpyHostToDevice, st));
     }
+    if (((uintptr_t)dA | (uintptr_t)dx) & 15)
+        return fail(ctx, XRDT_ERR_UNSUPPORTED, "device arrays A and x must be 16-byte aligned");
     int sms = 0;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
     const int nparts = mlem_pass_blocks(sms, K);

@@ -37,20 +37,6 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 
-// Compton table bin of integrate_diffraction.cu:331-337 decided in FP64, as
-// the oracle decides it; used only when the FP32 value lies within 2e-4 of a
-// bin edge.  Kept out of line so that the rare FP64 path is a real branch
-// and not predicated into every iteration of the energy loop.
-__device__ __noinline__ int compton_bin_f64(const DevProblem &P, double ein, float omc_hi, float omc_lo)
-{
-    const double omcd = (double)omc_hi + (double)omc_lo;
-    const double sd = sqrt(fabs(omcd) / 2.0);
-    const double erd = 1.0 + ein * omcd;
-    const double wd = ein * sd;
-    const double l2d = log2(wd * sqrt(erd + wd * wd) / erd);
-    return floor_to_int((l2d - P.q_min) / P.dq_tab);
-}
-
 struct Layout {
     size_t en, rf, offse, winlo, wn, ifine, fq, cq, s2, tn, tns, cs, ck, ta, total;
 };
@@ -214,7 +200,7 @@ k_fwd(const FwdArgs args)
             const int xy = args.vox_xy[v];
             const float vx = ((float)(xy & 0xffff) + 0.5f) * c.vox;
             const float vy = ((float)(xy >> 16) + 0.5f) * c.vox;
-            const VoxGeom vg = vox_geom(G, vx, vy);
+            const VoxGeom vg = vox_geom<false>(G, vx, vy);
             const int mv = args.vox_mat[v];
             const int nav = args.vox_na[v];
             const float a2v = args.vox_a2[v];
@@ -230,7 +216,7 @@ k_fwd(const FwdArgs args)
                 const float sl = __shfl_sync(0xffffffffu, vg.s.lo, i);
                 const float oh = __shfl_sync(0xffffffffu, vg.omc.hi, i);
                 const float ol = __shfl_sync(0xffffffffu, vg.omc.lo, i);
-                const float sg = __shfl_sync(0xffffffffu, vg.sg, i);
+                const float sg = __shfl_sync(0xffffffffu, vg.sg.hi, i);
                 const float gp = __shfl_sync(0xffffffffu, vg.gp, i);
                 const float Wg = __shfl_sync(0xffffffffu, vg.Wg, i);
                 const float cos2 = __shfl_sync(0xffffffffu, vg.cos2, i);
@@ -312,8 +298,9 @@ k_fwd(const FwdArgs args)
                     // ---- Compton, :318-356 ----
                     {
                         const float ein = en_ein[el];
-                        const float x = ein * oh;                 // eratio - 1
-                        const float eratio = 1.f + x;
+                        // no contraction: the Compton bin check forms eratio the same way
+                        const float x = __fmul_rn(ein, oh);       // eratio - 1
+                        const float eratio = __fadd_rn(1.f, x);
                         const float inv_er = rcp_approx(eratio);
                         const int eg = lo_e + el;
                         // detector bins whose window holds e and whose channel the
@@ -331,16 +318,8 @@ k_fwd(const FwdArgs args)
                         }
                         const int n1 = min(wn[2 * el + 1], floor_bounded(((Eo_lo + dEsf) * inv_er - edmin) * inv_dEd));
                         if (n0 <= n1) {
-                            const float wC = ein * sh;
-                            const float arg = eratio + wC * wC;
-                            const float l2 = lg2_approx(wC * arg * rsqrt_approx(arg) * inv_er);
-                            const float tq = (l2 - qmin_t) * inv_dqt;
-                            float ftq;
-                            int nq = floor_bounded(tq, &ftq);   // clamped to the table below
-                            const float fr = tq - ftq;
-                            if (!(fr > 2e-4f && fr < 1.f - 2e-4f))  // near a table edge
-                                nq = compton_bin_f64(P, args.T.energy[eg].ein, oh, ol);
-                            nq = nq < 0 ? 0 : (nq >= P.nq ? P.nq - 1 : nq);
+                            const int nq = compton_bin(P, ein, eratio, inv_er, sh, oh, ol, args.T.energy[eg].ein,
+                                                       qmin_t, inv_dqt);
                             const float eout = ein * inv_er;
                             const float f1 = eout * eout * eout;
                             const float f2 = fmaf(kn2 * eout, eout, fmaf(kn1, eout, kn0));

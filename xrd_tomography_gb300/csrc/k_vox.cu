@@ -49,13 +49,26 @@ constexpr int kFwdWarps = kFwdThreads / 32;
 // Per-(voxel, energy) factors shared by the forward and the adjoint: the
 // prefactor pref = Pin Pout geom Rayleigh / (sigma sqrt(2 pi)) without RF,
 // the wavevector transfer as a pair, the Gaussian exponent scale (log2
-// units) and the window half-width.
+// units, as a pair) and the window half-width.
 struct EnergyTerm {
-    float pref, w_hi, w_lo, cexp, half;
+    float pref, w_hi, w_lo, c_hi, c_lo, half;
 };
 
+// Per-(pair, voxel) inputs of sigma^2 = c1 s^2 + c2 sg / s^2 as pairs.
+struct SigmaGeom {
+    ff s2, sg_s2;
+};
+
+__device__ __forceinline__ SigmaGeom sigma_geom(float sh, float sl, ff sg)
+{
+    SigmaGeom g;
+    g.s2 = ff_sqr(ff{sh, sl});
+    g.sg_s2 = ff_div(sg, g.s2);
+    return g;
+}
+
 __device__ __forceinline__ EnergyTerm energy_term(const float *en, int E, int el, float Adx, float Ady, float Asx,
-                                                  float Asy, float sh, float sl, float s2f, float sg_s2, float Wg,
+                                                  float Asy, float sh, float sl, const SigmaGeom &sgm, float Wg,
                                                   float rsqrt2pi)
 {
     const float if1 = en[el], if2 = en[E + el];
@@ -70,18 +83,30 @@ __device__ __forceinline__ EnergyTerm energy_term(const float *en, int E, int el
         w_lo = w_lo - (s - w_hi);
         w_hi = s;
     }
-    const float sig2 = fmaf(en[4 * E + el], s2f, en[5 * E + el] * sg_s2);
-    const float rs = rsqrtf(sig2);
-    t.cexp = -0.5f * kLog2e * rs * rs;
-    const float PP = ex2_approx(-(Xin + Xout) * kLog2e);
+    // sigma^2 as a pair: deep in the Gaussian's tail the exponent amplifies
+    // its relative error by (q distance / sigma)^2 / 2
+    const ff sig2 = ff_add(ff_mul(ff{en[4 * E + el], en[6 * E + el]}, sgm.s2),
+                           ff_mul(ff{en[5 * E + el], en[7 * E + el]}, sgm.sg_s2));
+    // 1/sigma to within an ulp: one Newton step on rsqrt, with the low part
+    const float r0 = rsqrtf(sig2.hi);
+    const float h = fmaf(-0.5f * sig2.hi * r0, r0, 0.5f) - 0.5f * sig2.lo * r0 * r0;
+    const float rs = fmaf(r0, h, r0);
+    const ff c = gauss_scale(sig2);
+    t.c_hi = c.hi;
+    t.c_lo = c.lo;
+    // exp(-X) as 2^(-X log2 e) with log2 e as a pair
+    const float X = Xin + Xout;
+    const float PP = ex2_approx(-fmaf(X, kLog2e, X * kLog2e_lo));
     t.pref = PP * Wg * rsqrt2pi * rs;
-    t.half = kSig * sig2 * rs;
+    t.half = kSig * sig2.hi * rs;
     t.w_hi = w_hi;
     t.w_lo = w_lo;
     return t;
 }
 
-// Energy rows in shared memory: 1/f1, 1/f2, wfac_hi, wfac_lo, sig_c1, sig_c2.
+// Energy rows in shared memory: 1/f1, 1/f2, wfac_hi, wfac_lo, sig_c1,
+// sig_c2, and the low parts of sig_c1, sig_c2.
+constexpr int kEnRows = 8;
 __device__ __forceinline__ void stage_energy_rows(const VoxJob &J, float *en, int tid, int nthreads)
 {
     for (int i = tid; i < J.E; i += nthreads) {
@@ -92,6 +117,8 @@ __device__ __forceinline__ void stage_energy_rows(const VoxJob &J, float *en, in
         en[3 * J.E + i] = r.wfac_lo;
         en[4 * J.E + i] = r.sig_c1;
         en[5 * J.E + i] = r.sig_c2;
+        en[6 * J.E + i] = r.sig_c1_lo;
+        en[7 * J.E + i] = r.sig_c2_lo;
     }
 }
 
@@ -129,7 +156,7 @@ __host__ __device__ inline FwdLayout vox_fwd_layout(const DevProblem &P, int E)
     size_t o = 0;
     L.tn = o; o = al16(o + sizeof(double) * E);
     L.tns = o; o = al16(o + sizeof(float2) * kFwdWarps * E);
-    L.en = o; o = al16(o + sizeof(float) * 6 * E);
+    L.en = o; o = al16(o + sizeof(float) * kEnRows * E);
     L.rf = o; o = al16(o + sizeof(float) * P.nrg_det * W);
     L.winlo = o; o = al16(o + sizeof(int) * P.nrg_det);
     L.wn = o; o = al16(o + sizeof(int) * 2 * E);
@@ -166,6 +193,7 @@ __device__ __forceinline__ void vox_fwd_pair(const VoxJob &J, int64_t pidx, unsi
     for (int i = tid; i < P.nrg_det * W; i += kFwdThreads) rf[i] = J.op.rf_win[i];
     for (int i = tid; i < P.nrg_det; i += kFwdThreads) winlo[i] = J.op.win_lo[i];
     for (int i = tid; i < K; i += kFwdThreads) cq[i] = J.op.coarse_q[i];
+    static_assert(sizeof(PairRec) / 4 <= kFwdThreads, "one word per thread");
     if (tid < (int)(sizeof(PairRec) / 4))
         reinterpret_cast<int *>(&pair)[tid] = reinterpret_cast<const int *>(J.op.pairs + pidx)[tid];
     const float rsqrt2pi = c.rsqrt2pi;
@@ -182,7 +210,7 @@ __device__ __forceinline__ void vox_fwd_pair(const VoxJob &J, int64_t pidx, unsi
         const int xy = J.op.vox_xy[v];
         const float vx = ((float)(xy & 0xffff) + 0.5f) * c.vox;
         const float vy = ((float)(xy >> 16) + 0.5f) * c.vox;
-        const VoxGeom vg = vox_geom(pair.G, vx, vy);
+        const VoxGeom vg = vox_geom<true>(pair.G, vx, vy);
         const float2 Asv = J.op.atten_src[(int64_t)src * nv + v];
         // the detector-side integral feeds Pin (integrate_diffraction.cu:259-260):
         // read from the operator's table, or walked here
@@ -212,24 +240,22 @@ __device__ __forceinline__ void vox_fwd_pair(const VoxJob &J, int64_t pidx, unsi
             }
             const float sh = __shfl_sync(0xffffffffu, vg.s.hi, i);
             const float sl = __shfl_sync(0xffffffffu, vg.s.lo, i);
-            const float sg = __shfl_sync(0xffffffffu, vg.sg, i);
+            const ff sg = {__shfl_sync(0xffffffffu, vg.sg.hi, i), __shfl_sync(0xffffffffu, vg.sg.lo, i)};
             const float Wg = __shfl_sync(0xffffffffu, vg.Wg, i);
             const float Asx = __shfl_sync(0xffffffffu, Asv.x, i);
             const float Asy = __shfl_sync(0xffffffffu, Asv.y, i);
-            const float s2f = sh * sh;
-            const float sg_s2 = __fdividef(sg, s2f);
+            const SigmaGeom sgm = sigma_geom(sh, sl, sg);
             const float *xrow = xd + (int64_t)(chunk * 32 + i) * K;
 #pragma unroll 1
             for (int el = lane; el < E; el += 32) {
-                const EnergyTerm t = energy_term(en, E, el, Ad.x, Ad.y, Asx, Asy, sh, sl, s2f, sg_s2, Wg, rsqrt2pi);
+                const EnergyTerm t = energy_term(en, E, el, Ad.x, Ad.y, Asx, Asy, sh, sl, sgm, Wg, rsqrt2pi);
                 if (t.pref == 0.f) continue;   // attenuation underflow: no contribution
                 int klo, khi;
                 coarse_window(t.w_hi, t.half, qlo_f, c.qpar_a, c.qpar_b, K, &klo, &khi);
                 float acc = 0.f;
                 for (int k = klo; k <= khi; k++) {
                     const float4 q = cq[k];
-                    const float d = (t.w_hi - q.x) + (t.w_lo - q.y);
-                    acc = fmaf(ex2_approx(t.cexp * d * d), __ldg(xrow + k), acc);
+                    acc = fmaf(gauss_f32(t.w_hi, t.w_lo, q.x, q.y, t.c_hi, t.c_lo), __ldg(xrow + k), acc);
                 }
                 float2 s = TNw[el];
                 kahan_add(s.x, s.y, t.pref * acc);
@@ -326,11 +352,16 @@ k_vox_adj(const VoxBatch B)
         const F32Consts &c = J.c;
         const int E = J.E, K = P.nwt;
         float *en = (float *)sm;                                            // [6][E]
-        float4 *cq = (float4 *)(sm + al16(sizeof(float) * 6 * E));          // [K]
+        float4 *cq = (float4 *)(sm + al16(sizeof(float) * kEnRows * E));    // [K]
         float4 *rows = cq + K;                                              // [warps][E]
         float2 *gacc = (float2 *)(rows + (size_t)nwarps * E);               // [warps][32][K]
         PairRec *prs = (PairRec *)(gacc + (size_t)nwarps * 32 * K);         // [warps]
+        float *rows_lo = (float *)(prs + nwarps);                           // [warps][E]
+        int2 *wins = (int2 *)(sm + al16((size_t)((unsigned char *)(rows_lo + (size_t)nwarps * E) - sm)));
+                                                                            // [warps][E]
         float4 *rw = rows + (size_t)wid * E;
+        float *rwl = rows_lo + (size_t)wid * E;
+        int2 *ww = wins + (size_t)wid * E;
         float2 *gw = gacc + (size_t)wid * 32 * K;
         PairRec &pr = prs[wid];
         stage_energy_rows(J, en, tid, blockDim.x);
@@ -357,11 +388,11 @@ k_vox_adj(const VoxBatch B)
 
         for (int64_t pp = p0; pp < p1; pp++) {
             __syncwarp();   // the previous pair's constants are no longer read
-            if (lane < (int)(sizeof(PairRec) / 4))
-                reinterpret_cast<int *>(&pr)[lane] = reinterpret_cast<const int *>(J.op.pairs + pp)[lane];
+            for (int i = lane; i < (int)(sizeof(PairRec) / 4); i += 32)
+                reinterpret_cast<int *>(&pr)[i] = reinterpret_cast<const int *>(J.op.pairs + pp)[i];
             __syncwarp();
             const int src = (int)(pp % P.n_src);
-            const VoxGeom vg = vox_geom(pr.G, vx, vy);
+            const VoxGeom vg = vox_geom<true>(pr.G, vx, vy);
             const float2 Asv = J.op.atten_src[(int64_t)src * nv + v];
             const float2 *wt = J.op.walk;
             float2 Adv = make_float2(0.f, 0.f);
@@ -388,34 +419,91 @@ k_vox_adj(const VoxBatch B)
                 }
                 const float sh = __shfl_sync(0xffffffffu, vg.s.hi, i);
                 const float sl = __shfl_sync(0xffffffffu, vg.s.lo, i);
-                const float sg = __shfl_sync(0xffffffffu, vg.sg, i);
+                const ff sg = {__shfl_sync(0xffffffffu, vg.sg.hi, i), __shfl_sync(0xffffffffu, vg.sg.lo, i)};
                 const float Wg = __shfl_sync(0xffffffffu, vg.Wg, i);
                 const float Asx = __shfl_sync(0xffffffffu, Asv.x, i);
                 const float Asy = __shfl_sync(0xffffffffu, Asv.y, i);
-                const float s2f = sh * sh;
-                const float sg_s2 = __fdividef(sg, s2f);
-                for (int el = lane; el < E; el += 32) {
-                    const EnergyTerm t =
-                        energy_term(en, E, el, Ad.x, Ad.y, Asx, Asy, sh, sl, s2f, sg_s2, Wg, rsqrt2pi);
-                    float cf = __ldg(wp + el) * t.pref;
-                    // a window entirely outside the coarse grid contributes nothing
-                    if (t.w_hi + t.half < q_lo || t.w_hi - t.half > q_hi) cf = 0.f;
-                    rw[el] = make_float4(cf, t.w_hi, t.w_lo, t.cexp);
+                const SigmaGeom sgm = sigma_geom(sh, sl, sg);
+                // lane = energy: the energy's factors and its coarse-bin
+                // window (the bins within 7.5 sigma; the terms beyond are
+                // below 7e-13 of the peak), with the running maximum of the
+                // windows' upper ends in ww[e].x
+                int run_max = -1;
+                for (int eb = 0; eb < E; eb += 32) {
+                    const int el = eb + lane;
+                    int klo = K, khi = -1;
+                    if (el < E) {
+                        const EnergyTerm t =
+                            energy_term(en, E, el, Ad.x, Ad.y, Asx, Asy, sh, sl, sgm, Wg, rsqrt2pi);
+                        const float cf = __ldg(wp + el) * t.pref;
+                        const float half = t.half * (kSigAdj / kSig);
+                        // a window entirely outside the coarse grid contributes nothing
+                        if (cf != 0.f && !(t.w_hi + half < q_lo || t.w_hi - half > q_hi))
+                            coarse_window(t.w_hi, half, q_lo, c.qpar_a, c.qpar_b, K, &klo, &khi);
+                        rw[el] = make_float4(cf, t.w_hi, t.w_lo, t.c_hi);
+                        rwl[el] = t.c_lo;
+                        ww[el].y = klo;
+                    }
+                    int m = khi;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int n = __shfl_up_sync(0xffffffffu, m, o);
+                        if (lane >= o) m = max(m, n);
+                    }
+                    m = max(m, run_max);
+                    if (el < E) ww[el].x = m;
+                    run_max = __shfl_sync(0xffffffffu, m, 31);
                 }
                 __syncwarp();
+                // running minimum of the windows' lower ends from the top
+                // energy down, in ww[e].y
+                int run_min = K;
+                for (int eb = ((E - 1) >> 5) << 5; eb >= 0; eb -= 32) {
+                    const int el = eb + lane;
+                    int m = el < E ? ww[el].y : K;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int n = __shfl_down_sync(0xffffffffu, m, o);
+                        if (lane + o < 32) m = min(m, n);
+                    }
+                    m = min(m, run_min);
+                    if (el < E) ww[el].y = m;
+                    run_min = __shfl_sync(0xffffffffu, m, 0);
+                }
+                __syncwarp();
+                // lane = coarse bin k over the bins some window reaches.  The
+                // energies whose window holds k lie in [e0, e1]: below e0
+                // every window ends before k, above e1 every window starts
+                // after it (both running bounds are monotone, so a binary
+                // search finds them).
+                const int kmin = run_min, kmax = run_max;
                 float2 *gi = gw + i * K;
-                for (int k = lane; k < K; k += 32) {
+                for (int kb = kmin; kb <= kmax; kb += 32) {
+                    const int k = kb + lane;
+                    if (k > kmax) break;
+                    int lo = 0, hi = E;
+                    while (lo < hi) {
+                        const int mid = (lo + hi) >> 1;
+                        if (ww[mid].x < k) lo = mid + 1;
+                        else hi = mid;
+                    }
+                    const int e0 = lo;
+                    hi = E;
+                    while (lo < hi) {
+                        const int mid = (lo + hi) >> 1;
+                        if (ww[mid].y <= k) lo = mid + 1;
+                        else hi = mid;
+                    }
+                    const int e1 = lo;   // one past the last
                     const float4 q = cq[k];
                     float acc = 0.f;
-                    for (int e = 0; e < E; e++) {
+                    for (int e = e0; e < e1; e++) {
                         const float4 rr = rw[e];
-                        if (rr.x == 0.f) continue;   // uniform across the warp
-                        const float d = (rr.y - q.x) + (rr.z - q.y);
-                        acc = fmaf(rr.x, ex2_approx(rr.w * d * d), acc);
+                        acc = fmaf(rr.x, gauss_f32(rr.y, rr.z, q.x, q.y, rr.w, rwl[e]), acc);
                     }
-                    float2 s = gi[k];
-                    kahan_add(s.x, s.y, acc * q.z);
-                    gi[k] = s;
+                    float2 sacc = gi[k];
+                    kahan_add(sacc.x, sacc.y, acc * q.z);
+                    gi[k] = sacc;
                 }
                 __syncwarp();
             }
@@ -593,8 +681,9 @@ size_t vox_fwd_smem(const DevProblem &P) { return vox_fwd_layout(P, P.e_hi - P.e
 size_t vox_adj_smem(const DevProblem &P, int warps)
 {
     const int E = P.e_hi - P.e_lo + 1, K = P.nwt;
-    return al16(sizeof(float) * 6 * E) + sizeof(float4) * K + sizeof(float4) * (size_t)warps * E +
-           sizeof(float2) * (size_t)warps * 32 * K + sizeof(PairRec) * warps;
+    return al16(sizeof(float) * kEnRows * E) + sizeof(float4) * K + sizeof(float4) * (size_t)warps * E +
+           sizeof(float2) * (size_t)warps * 32 * K + sizeof(PairRec) * warps + sizeof(float) * (size_t)warps * E +
+           16 + sizeof(int2) * (size_t)warps * E;
 }
 
 int vox_fwd_blocks_per_sm(size_t smem)

@@ -61,14 +61,18 @@ int scratch_addresses(int device, float **partial, double **sens)
     return XRDT_OK;
 }
 
-bool on_device(const void *p)
+// Device memory of `device` (or managed memory): a buffer of another GPU
+// would be read through peer access, and the scratch belongs to the current
+// device only.
+bool on_device(const void *p, int device)
 {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    if (a.type == cudaMemoryTypeManaged) return true;
+    return a.type == cudaMemoryTypeDevice && a.device == device;
 }
 
 } // namespace
@@ -78,13 +82,16 @@ extern "C" int32_t xrdt_mlem_matrix_noalloc(const float *A, int64_t rays, int32_
 {
     if (!A || !y || !c || !x) return XRDT_ERR_NULL;
     if (rays < 1 || K < 4 || K > kMaxK || (K & 3) || iters < 0) return XRDT_ERR_DIMS;
-    if (!on_device(A) || !on_device(y) || !on_device(c) || !on_device(x)) return XRDT_ERR_UNSUPPORTED;
     int device = 0, sms = 0;
     if (cudaGetDevice(&device) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
         cudaGetLastError();
         return XRDT_ERR_CUDA;
     }
+    if (!on_device(A, device) || !on_device(y, device) || !on_device(c, device) || !on_device(x, device))
+        return XRDT_ERR_UNSUPPORTED;
+    // the MLEM pass reads rows of A and x as 16-byte vectors
+    if (((uintptr_t)A | (uintptr_t)x) & 15) return XRDT_ERR_UNSUPPORTED;
     float *partial;
     double *sens;
     int rc = scratch_addresses(device, &partial, &sens);

@@ -22,6 +22,7 @@ struct PairGeom {
     ff nsx2, nsy2;                // in-plane source orientation as pairs
     float nsx, nsy, nsz, ndx, ndy, sphi, cphi;
     float k2;                     // tan(geomphi) / |nsrc_xy|
+    ff k2f;                       // the same as a pair
     float tan_full, adet12, vox2, focal2_12;
 };
 
@@ -29,7 +30,7 @@ struct PairGeom {
 struct VoxGeom {
     ff s;        // sin(theta/2)
     ff omc;      // 1 - cos(theta)
-    float sg;    // (sS2 + vV2 + dD2) / (|a|^2 |b|^2)
+    ff sg;       // (sS2 + vV2 + dD2) / (|a|^2 |b|^2)
     float gp;    // geom_src2vox * geom_vox2det
     float Wg;    // gp * Rayleigh factor
     float cos2;  // cos^2(theta)
@@ -45,7 +46,14 @@ struct PairRec {
 namespace {
 
 constexpr float kSig = 7.5f;            // Gaussian window, in sigma (tail below 7e-13)
+// The adjoint's window: every term that FP32 can represent.  2^(c d^2) flushes
+// to zero below 2^-126, i.e. beyond sqrt(2 * 126 / log2(e)) = 13.2 sigma, so
+// summing out to 13.25 sigma gives exactly the dense sum.  A sensitivity
+// made of far-tail terms only can still be comparable to the 1e-7 that MLEM
+// adds to it (main.m:162), so the adjoint cannot drop them.
+constexpr float kSigAdj = 13.25f;
 constexpr float kLog2e = 1.4426950408889634f;
+constexpr float kLog2e_lo = (float)(1.4426950408889634074 - (double)kLog2e);
 
 __device__ __forceinline__ void kahan_add(float &s, float &c, float x)
 {
@@ -82,6 +90,93 @@ __device__ __forceinline__ float rsqrt_approx(float x)
     return y;
 }
 
+constexpr float kLn2 = 0.6931471805599453f;
+constexpr float kTwelfth_hi = (float)(1.0 / 12.0);
+constexpr float kTwelfth_lo = (float)(1.0 / 12.0 - (double)kTwelfth_hi);
+// 0.5 log2(e) as a float pair: the Gaussian exp(-d^2 / (2 sigma^2)) is
+// evaluated as 2^(c d^2) with c = -0.5 log2(e) / sigma^2
+constexpr double kHalfLog2e = 0.72134752044448170368;
+constexpr float kHalfLog2e_hi = (float)kHalfLog2e;
+constexpr float kHalfLog2e_lo = (float)(kHalfLog2e - (double)kHalfLog2e_hi);
+
+// c = -0.5 log2(e) / sigma^2 as a float pair, from sigma^2 as a pair.  The
+// residual of the correctly rounded quotient is exact through the FMA.
+__device__ __forceinline__ ff gauss_scale(ff sig2)
+{
+    const float rcp = rcp_approx(sig2.hi);
+    const float ch = -kHalfLog2e_hi * rcp;
+    // the quotient's residual, exact through the FMA to a bit or two
+    float r = fmaf(-ch, sig2.hi, -kHalfLog2e_hi);
+    r = fmaf(-ch, sig2.lo, r) - kHalfLog2e_lo;
+    return {ch, r * rcp};
+}
+
+// 2^(c (w - q)^2) with the argument in FP32 but c as a pair: the scale c
+// carries the systematic part of the error (sigma), the difference and its
+// square round independently per term.
+__device__ __forceinline__ float gauss_f32(float wh, float wl, float qh, float ql, float ch, float cl)
+{
+    const float d = (wh - qh) + (wl - ql);
+    const float d2 = d * d;
+    return ex2_approx(fmaf(ch, d2, cl * d2));
+}
+
+// 2^(c (w - q)^2) with w, q and c as float pairs.  The argument is formed
+// as a pair (exact difference, exact square through the FMA), so its error
+// is a few units of 2^-44 relative instead of a few FP32 ulps: deep in the
+// Gaussian's tail, where the argument is tens, an FP32 argument would move
+// the term by about 1e-6 relative.  The low part enters as 2^lo = 1 + lo ln2.
+__device__ __forceinline__ float gauss_ff(float wh, float wl, float qh, float ql, float ch, float cl)
+{
+    const float t = wh - qh;   // exact while w and q are within a factor of two
+    const float u = wl - ql;
+    const float dh = t + u;
+    const float dl = u - (dh - t);
+    const float d2h = dh * dh;
+    float d2l = fmaf(dh, dh, -d2h);
+    d2l = fmaf(dh + dh, dl, d2l);
+    const float ah = ch * d2h;
+    float al = fmaf(ch, d2h, -ah);
+    al = fmaf(ch, d2l, al);
+    al = fmaf(cl, d2h, al);
+    const float e = ex2_approx(ah);
+    return fmaf(e, al * kLn2, e);
+}
+
+// Compton table bin of integrate_diffraction.cu:331-337 decided in FP64, as
+// the oracle decides it; used only when the FP32 value lies within 2e-4 of a
+// bin edge.  Kept out of line so that the rare FP64 path is a real branch
+// and not predicated into every iteration of the energy loop.
+__device__ __noinline__ int compton_bin_f64(const DevProblem &P, double ein, float omc_hi, float omc_lo)
+{
+    const double omcd = (double)omc_hi + (double)omc_lo;
+    const double sd = sqrt(fabs(omcd) / 2.0);
+    const double erd = 1.0 + ein * omcd;
+    const double wd = ein * sd;
+    const double l2d = log2(wd * sqrt(erd + wd * wd) / erd);
+    return floor_to_int((l2d - P.q_min) / P.dq_tab);
+}
+
+// Compton table bin nq = floor((log2(w sqrt(eratio + w^2) / eratio) - q_min) / dq)
+// with w = ein sin(theta/2), clamped to [0, NQ) (integrate_diffraction.cu:331-337).
+// Decided in FP32 from the voxel's 1 - cos(theta) (pair (oh, ol)) and
+// sin(theta/2) (hi part sh); within 2e-4 of a bin edge it is decided again in
+// FP64.  eratio = 1 + ein oh and inv_er = 1/eratio as the caller formed them.
+__device__ __forceinline__ int compton_bin(const DevProblem &P, float ein, float eratio, float inv_er, float sh,
+                                           float oh, float ol, double ein_d, float qmin_t, float inv_dqt)
+{
+    const float wC = ein * sh;
+    const float arg = eratio + wC * wC;
+    const float l2 = lg2_approx(wC * arg * rsqrt_approx(arg) * inv_er);
+    const float tq = (l2 - qmin_t) * inv_dqt;
+    float ftq;
+    int nq = floor_bounded(tq, &ftq);   // clamped to the table below
+    const float fr = tq - ftq;
+    if (!(fr > 2e-4f && fr < 1.f - 2e-4f))  // near a table edge
+        nq = compton_bin_f64(P, ein_d, oh, ol);
+    return nq < 0 ? 0 : (nq >= P.nq ? P.nq - 1 : nq);
+}
+
 // FP64 walk set-up out of line: the rare fallback of walk_setup_f32 stays a
 // real branch instead of being predicated into the caller's loop.
 __device__ __noinline__ void walk_setup_f64(const DevProblem &P, double ex, double ey, double vx, double vy,
@@ -111,6 +206,7 @@ __device__ __forceinline__ void pair_geom(const DevProblem &P, const SrcGeom &g,
     G->nsz = (float)nsz;
     G->k1 = ff_from_double(P.tan_half / nsxy);
     G->k2 = (float)(P.tan_full / nsxy);
+    G->k2f = ff_from_double(P.tan_full / nsxy);
     G->ndx = (float)g.sphi;
     G->ndy = (float)(-g.cphi);
     G->sphi = (float)g.sphi;
@@ -126,6 +222,10 @@ __device__ __forceinline__ void pair_geom(const DevProblem &P, const SrcGeom &g,
 // |a x b|^2 / (|a||b| (|a||b| + a.b)), which has no cancellation at small
 // angles; the blur vectors S = ((a x b) x a)/|a|^2 = b - (a.b/|a|^2) a and
 // D = ((a x b) x b)/|b|^2 = -a + (a.b/|b|^2) b in FP32.
+// SIGMA_PAIR: sigma's blur terms as float pairs (the per-voxel operator,
+// whose adjoint sums deep Gaussian tails); otherwise in FP32 (the material
+// forward projector, whose counts are dominated by the Gaussians' cores).
+template <bool SIGMA_PAIR>
 __device__ __forceinline__ VoxGeom vox_geom(const PairGeom &G, float vx, float vy)
 {
     const ff ax = ff_fsub(vx, G.Rsx), ay = ff_fsub(vy, G.Rsy);
@@ -151,22 +251,58 @@ __device__ __forceinline__ VoxGeom vox_geom(const PairGeom &G, float vx, float v
     // FP32 remainder of the geometry
     const float Ax = ax.hi, Ay = ay.hi, Az = az.hi, Bx = bx.hi, By = by.hi, Bz = bz.hi;
     const float Cx = cx.hi, Cy = cy.hi, Cz = cz.hi, An = an.hi, Bn = bn.hi;
-    const float ia = __fdividef(1.f, An), ib = __fdividef(1.f, Bn);
+    const float ia = __fdividef(1.f, An);
     const float Sx = (Cy * Az - Cz * Ay) * ia, Sy = (Cz * Ax - Cx * Az) * ia, Sz = (Cx * Ay - Cy * Ax) * ia;
-    const float Dx = (Cy * Bz - Cz * By) * ib, Dy = (Cz * Bx - Cx * Bz) * ib, Dz = (Cx * By - Cy * Bx) * ib;
-    const float Vx = -(Sx + Dx), Vy = -(Sy + Dy), Vz = -(Sz + Dz);
-    const float Dndet = Dx * G.ndx + Dy * G.ndy;
     const float Snsrc = Sx * G.nsx + Sy * G.nsy + Sz * G.nsz;
-    const float dD2 = (Dx * Dx + Dy * Dy + Dz * Dz - Dndet * Dndet) * G.adet12;
-    const float vV2 = (G.vox2 * (Vx * Vx + Vy * Vy) + Hvox * Hvox * Vz * Vz) * (1.f / 12.f);
     const float sS2 = (Sx * Sx + Sy * Sy + Sz * Sz - Snsrc * Snsrc) * G.focal2_12;
+    if (!SIGMA_PAIR) {
+        const float ib = __fdividef(1.f, Bn);
+        const float Dx = (Cy * Bz - Cz * By) * ib, Dy = (Cz * Bx - Cx * Bz) * ib, Dz = (Cx * By - Cy * Bx) * ib;
+        const float Vx = -(Sx + Dx), Vy = -(Sy + Dy), Vz = -(Sz + Dz);
+        const float Dndet = Dx * G.ndx + Dy * G.ndy;
+        const float dD2 = (Dx * Dx + Dy * Dy + Dz * Dz - Dndet * Dndet) * G.adet12;
+        const float vV2 = (G.vox2 * (Vx * Vx + Vy * Vy) + Hvox * Hvox * Vz * Vz) * (1.f / 12.f);
+        r.sg = ff{(sS2 + vV2 + dD2) * ia * ib, 0.f};
+    } else {
+        // The blur terms that make up most of sigma^2 as pairs: the Gaussian's
+        // tail amplifies their relative error by (q distance / sigma)^2 / 2, and
+        // FP32 leaves them about two ulps off.  V = -(S + D) = u x C with
+        // u = a/|a|^2 + b/|b|^2 (S = C x a/|a|^2, D = C x b/|b|^2, C = a x b), and
+        // |D|^2 - (D.n_det)^2 = Dz^2 + (Dx n_y - Dy n_x)^2 for the in-plane unit
+        // normal n_det.
+        const ff iaf = ff_div(ff{1.f, 0.f}, an), ibf = ff_div(ff{1.f, 0.f}, bn);
+        const ff ux = ff_add(ff_mul(ax, iaf), ff_mul(bx, ibf));
+        const ff uy = ff_add(ff_mul(ay, iaf), ff_mul(by, ibf));
+        const ff uz = ff_add(ff_mul(az, iaf), ff_mul(bz, ibf));
+        const ff Vx = ff_sub(ff_mul(uy, cz), ff_mul(uz, cy));
+        const ff Vy = ff_sub(ff_mul(uz, cx), ff_mul(ux, cz));
+        const ff Vz = ff_sub(ff_mul(ux, cy), ff_mul(uy, cx));
+        const ff Hv = ff_mul(proj, G.k2f);
+        const ff vV = ff_add(ff_mulf(ff_add(ff_sqr(Vx), ff_sqr(Vy)), G.vox2), ff_mul(ff_sqr(Hv), ff_sqr(Vz)));
+        const ff Dx = ff_mul(ff_sub(ff_mul(cy, bz), ff_mul(cz, by)), ibf);
+        const ff Dy = ff_mul(ff_sub(ff_mul(cz, bx), ff_mul(cx, bz)), ibf);
+        const ff Dz = ff_mul(ff_sub(ff_mul(cx, by), ff_mul(cy, bx)), ibf);
+        const ff Dt = ff_sub(ff_mulf(Dx, G.ndy), ff_mulf(Dy, G.ndx));
+        const ff dD = ff_mulf(ff_add(ff_sqr(Dz), ff_sqr(Dt)), G.adet12);
+        const ff blur = ff_add(ff_add(ff_mul(vV, ff{kTwelfth_hi, kTwelfth_lo}), dD), ff{sS2, 0.f});
+        r.sg = ff_mul(ff_mul(blur, iaf), ibf);
+    }
     const float Rdotn = -G.sphi * Ax + G.cphi * Ay;
-    const float cospsi = Rdotn * rsqrtf(Ax * Ax + Ay * Ay);
-    const float gsv = cospsi * rsqrtf(An) * G.tan_full;
-    const float gvd = -(G.ndx * Bx + G.ndy * By) * rsqrtf(Bn * Bn * Bn);
-    r.gp = gsv * gvd;
+    if (!SIGMA_PAIR) {
+        const float cospsi = Rdotn * rsqrtf(Ax * Ax + Ay * Ay);
+        const float gsv = cospsi * rsqrtf(An) * G.tan_full;
+        const float gvd = -(G.ndx * Bx + G.ndy * By) * rsqrtf(Bn * Bn * Bn);
+        r.gp = gsv * gvd;
+    } else {
+        // correctly rounded roots and quotients: the adjoint's column sums
+        // inherit any bias of these factors, and MLEM amplifies it tenfold
+        const float axy = __fsqrt_rn(fmaf(Ax, Ax, Ay * Ay));
+        const float gsv = __fdiv_rn(__fdiv_rn(Rdotn, axy), __fsqrt_rn(An)) * G.tan_full;
+        const float nb = __fsqrt_rn(Bn);
+        const float gvd = __fdiv_rn(-(G.ndx * Bx + G.ndy * By), Bn * nb);
+        r.gp = gsv * gvd;
+    }
     r.Wg = r.gp * ((1.f + r.cos2) * 0.5f);
-    r.sg = (sS2 + vV2 + dD2) * ia * ib;
     return r;
 }
 

@@ -16,6 +16,8 @@ struct WalkSetup {
     float rx, ry;   // ROI entry point (GetIntersection) minus one voxel in x and y
     float Lx, Ly;   // DQ times the unit direction entry -> voxel
     int n;          // number of samples: k = 0 .. n-1
+    int edge;       // ROI edge entered (GetIntersection's order: bottom, right,
+                    // top, left), -1 when the segment misses the ROI
 };
 
 // GetIntersection + the sample count of attenuator.cu:19-52: every k in
@@ -25,7 +27,7 @@ __device__ inline void walk_setup(const DevProblem &P, double ex, double ey, dou
                                   WalkSetup *w)
 {
     double rx, ry;
-    get_intersection(ex, ey, vx, vy, P.nx, P.ny, &rx, &ry);
+    get_intersection(ex, ey, vx, vy, P.nx, P.ny, &rx, &ry, &w->edge);
     double Lx = vx - rx, Ly = vy - ry;
     const double L2 = dadd(dmul(Lx, Lx), dmul(Ly, Ly));
     const double Lr = sqrt(L2);
@@ -63,6 +65,7 @@ __device__ __forceinline__ bool walk_setup_f32(const DevProblem &P, const F32Con
     const float dx = vx - ex, dy = vy - ey;
     float rx = 0.f, ry = 0.f;
     bool found = false;
+    int edge = -1;
 #pragma unroll
     for (int i = 0; i < 4; i++) {
         const float x3 = (i == 1 || i == 2) ? NX : 0.f;
@@ -82,6 +85,7 @@ __device__ __forceinline__ bool walk_setup_f32(const DevProblem &P, const F32Con
                 rx = fmaf(dx, ua, ex);
                 ry = fmaf(dy, ua, ey);
                 found = true;
+                edge = i;
                 break;
             }
         }
@@ -103,6 +107,7 @@ __device__ __forceinline__ bool walk_setup_f32(const DevProblem &P, const F32Con
     w->Lx = Lx * rL * DQ;
     w->Ly = Ly * rL * DQ;
     w->n = (int)n;
+    w->edge = edge;
     return true;
 }
 

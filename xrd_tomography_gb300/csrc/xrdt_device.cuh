@@ -87,7 +87,7 @@ __host__ __device__ inline void src_nrg_range(const DevProblem &P, int same_grid
 
 // GetIntersection.cu:9-57 in double: first ROI edge crossed by the segment.
 __host__ __device__ inline bool get_intersection(double x1, double y1, double x2, double y2,
-                                                 int nx, int ny, double *rx, double *ry)
+                                                 int nx, int ny, double *rx, double *ry, int *edge = nullptr)
 {
     const double NX = (double)nx, NY = (double)ny;
     const double eps = (double)0.00001f;
@@ -106,6 +106,7 @@ __host__ __device__ inline bool get_intersection(double x1, double y1, double x2
                 if (u_b > -eps && u_b < 1.0 + eps) {
                     *rx = dadd(x1, dmul(x2_x1, u_a));
                     *ry = dadd(y1, dmul(y2_y1, u_a));
+                    if (edge) *edge = i;
                     return true;
                 }
             }
@@ -113,6 +114,7 @@ __host__ __device__ inline bool get_intersection(double x1, double y1, double x2
     }
     *rx = NAN;
     *ry = NAN;
+    if (edge) *edge = -1;
     return false;
 }
 

@@ -58,7 +58,9 @@ struct EnergyRow {
     float inv_f1, inv_f2;       // 1/ein^3, 1/KN(ein)
     float wfac_hi, wfac_lo;     // 2*Esrc/hbarc as a float pair
     float sig_c1, sig_c2;       // sigma^2 = c1*s^2 + c2*sg/s^2
-    float einf, Esrc1f, Esrc2f, pad;
+    float einf, Esrc1f, Esrc2f;
+    float sig_c1_lo, sig_c2_lo; // low parts of c1, c2 as float pairs
+    float pad;
 };
 
 std::string fmt(const char *f, ...);
@@ -171,6 +173,13 @@ cudaError_t launch_spectrum(const SpecFineBin *fb, const SpecCoarseBin *sb, int 
 cudaError_t launch_det_walk(const DevProblem &P, const SrcGeom *sg, const int2 *pairs, long long p0,
                             long long n_items, const int *vox_xy, int nv, const float4 *cells, float2 *tab,
                             cudaStream_t s, int64_t *launches);
+// k_decisions.cu: the integer decisions of the fast path for listed rays
+// (test export): walk[i][v] = (detector-side sample count, its ROI edge,
+// source-side sample count, its ROI edge); nq[i][v][j] = Compton table bin of
+// source bin win_lo[nrg] + j, j < 2*dnrg+1.
+cudaError_t launch_decisions(const DevProblem &P, const SrcGeom *sg, const EnergyRow *energy, const int *win_lo,
+                             const int64_t *rays, int n_rays, const int *vox_xy, int nv, int4 *walk, int *nq,
+                             cudaStream_t s, int64_t *launches);
 // out[i] = compact[idx[i]] for N, C and the rows of A (row length mw).
 cudaError_t launch_gather_rays(const int64_t *idx, int64_t n, const float *Nc, const float *Cc,
                                const float *Ac, int mw, float *N, float *C, float *A, cudaStream_t s,
