@@ -110,3 +110,46 @@ def test_batch_mlem_matches_single_operators(ctx, torch_cuda):
     batch.close()
     for op in ops:
         op.close()
+
+
+def test_mixed_batch_streams_the_operators_without_tables(ctx, torch_cuda, monkeypatch):
+    """A batch whose operators partly keep their detector-side tables and
+    partly walk them in tiles (a walk buffer of a few pixel columns, so the
+    streamed problems span several tiles, some shared): forward, adjoint and
+    MLEM against the same operators run alone with their tables kept."""
+    torch = torch_cuda
+    inps = problems()
+    kept = [xt.Operator(i.problem, i.spectrum, i.seg, i.a1, i.a2, ctx=ctx) for i in inps]
+    monkeypatch.setenv("XRDT_WALK_CACHE", "0")
+    nv_max = max(op.voxels for op in kept)
+    src_max = max(i.problem.n_src for i in inps)
+    monkeypatch.setenv("XRDT_WALK_TILE_BYTES", str(8 * nv_max * src_max * 5))
+    streamed = [xt.Operator(i.problem, i.spectrum, i.seg, i.a1, i.a2, ctx=ctx) for i in inps[1:3]]
+    monkeypatch.delenv("XRDT_WALK_CACHE")
+    mixed = [kept[0], streamed[0], streamed[1], kept[3]]
+    batch = xt.Batch(mixed, ctx=ctx)
+    xs = [torch.from_numpy(rand_x(inp, 40 + k)).cuda() for k, inp in enumerate(inps)]
+    ws = [torch.rand(inp.problem.rays, generator=torch.Generator().manual_seed(50 + k)).cuda()
+          for k, inp in enumerate(inps)]
+    ys = [torch.empty(inp.problem.rays, device="cuda") for inp in inps]
+    gs = [torch.empty(op.unknowns, device="cuda") for op in mixed]
+    batch.forward(xs, ys)
+    batch.adjoint(ws, gs)
+    torch.cuda.synchronize()
+    for k, (inp, op) in enumerate(zip(inps, kept)):
+        y1 = op.forward(xs[k], torch.empty(inp.problem.rays, device="cuda"))
+        g1 = op.adjoint(ws[k], torch.empty(op.unknowns, device="cuda"))
+        torch.cuda.synchronize()
+        assert torch.equal(ys[k], y1), k
+        assert max_rel_err(gs[k].cpu().numpy(), g1.cpu().numpy()) < 1e-6, k
+    yms = [(y.double() * (1e3 / float(y.max()))).float() + 1.0 for y in ys]
+    cs = [torch.full_like(y, 0.5) for y in yms]
+    x0s = [torch.where(x > 0, 1.0, 0.0).float() for x in xs]
+    xb = [x.clone() for x in x0s]
+    batch.mlem(yms, cs, xb, 4)
+    for k, op in enumerate(kept):
+        x1 = x0s[k].clone()
+        op.mlem(yms[k], cs[k], x1, 4)
+        torch.cuda.synchronize()
+        assert max_rel_err(xb[k].cpu().numpy(), x1.cpu().numpy(), floor=MLEM_FLOOR) < 1e-6, k
+    batch.close()

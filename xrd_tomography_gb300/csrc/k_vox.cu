@@ -197,7 +197,6 @@ __device__ __forceinline__ void vox_fwd_pair(const VoxJob &J, int64_t pidx, unsi
     if (tid < (int)(sizeof(PairRec) / 4))
         reinterpret_cast<int *>(&pair)[tid] = reinterpret_cast<const int *>(J.op.pairs + pidx)[tid];
     const float rsqrt2pi = c.rsqrt2pi;
-    const float DQf = c.DQ;
     const float qlo_f = c.q_lo;
     const float *__restrict__ xd = J.xd;
     __syncthreads();
@@ -212,32 +211,13 @@ __device__ __forceinline__ void vox_fwd_pair(const VoxJob &J, int64_t pidx, unsi
         const float vy = ((float)(xy >> 16) + 0.5f) * c.vox;
         const VoxGeom vg = vox_geom<true>(pair.G, vx, vy);
         const float2 Asv = J.op.atten_src[(int64_t)src * nv + v];
-        // the detector-side integral feeds Pin (integrate_diffraction.cu:259-260):
-        // read from the operator's table, or walked here
-        const float2 *wt = J.op.walk;
-        float2 Adv = make_float2(0.f, 0.f);
-        WalkSetup ws;
-        ws.rx = ws.ry = ws.Lx = ws.Ly = 0.f;
-        ws.n = 0;
-        if (wt)
-            Adv = wt[pidx * nv + v];
-        else if (!walk_setup_f32(P, c, pair.G.Rdx.hi, pair.G.Rdy.hi, vx, vy, &ws))
-            walk_setup_f64(P, pair.Rdx, pair.Rdy, (double)vx, (double)vy, &ws);
+        // the detector-side integral feeds Pin (integrate_diffraction.cu:259-260),
+        // read from the table of this job's pairs (kept, or walked for the tile)
+        const float2 Adv = J.op.walk[(pidx - J.pair0) * nv + v];
 
         const int nin = min(32, nv - chunk * 32);
         for (int i = 0; i < nin; i++) {
-            float2 Ad;
-            if (wt) {
-                Ad = make_float2(__shfl_sync(0xffffffffu, Adv.x, i), __shfl_sync(0xffffffffu, Adv.y, i));
-            } else {
-                WalkSetup wi;
-                wi.rx = __shfl_sync(0xffffffffu, ws.rx, i);
-                wi.ry = __shfl_sync(0xffffffffu, ws.ry, i);
-                wi.Lx = __shfl_sync(0xffffffffu, ws.Lx, i);
-                wi.Ly = __shfl_sync(0xffffffffu, ws.Ly, i);
-                wi.n = __shfl_sync(0xffffffffu, ws.n, i);
-                Ad = walk_coop(J.op.cells, P.nx, P.ny, wi, DQf, lane);
-            }
+            const float2 Ad = make_float2(__shfl_sync(0xffffffffu, Adv.x, i), __shfl_sync(0xffffffffu, Adv.y, i));
             const float sh = __shfl_sync(0xffffffffu, vg.s.hi, i);
             const float sl = __shfl_sync(0xffffffffu, vg.s.lo, i);
             const ff sg = {__shfl_sync(0xffffffffu, vg.sg.hi, i), __shfl_sync(0xffffffffu, vg.sg.lo, i)};
@@ -317,7 +297,7 @@ k_vox_fwd(const VoxBatch B)
             cur = p;
             __syncthreads();
         }
-        vox_fwd_pair<MLEM>(job, item - off[p], sm, pair);
+        vox_fwd_pair<MLEM>(job, job.pair0 + (item - off[p]), sm, pair);
     }
 }
 
@@ -374,11 +354,9 @@ k_vox_adj(const VoxBatch B)
         const int nv = J.op.nv;
         const int chunk = bx * nwarps + wid;
         if (chunk * 32 >= nv) continue;   // an idle warp; the next item starts with a barrier
-        const int64_t npairs = (int64_t)P.n_src * P.n_det;
-        const int64_t p0 = (int64_t)by * J.ppg;
-        const int64_t p1 = min(npairs, p0 + J.ppg);
+        const int64_t p0 = J.pair0 + (int64_t)by * J.ppg;
+        const int64_t p1 = min(J.pair1, p0 + J.ppg);
         const float rsqrt2pi = c.rsqrt2pi;
-        const float DQf = c.DQ;
         const float q_lo = c.q_lo, q_hi = c.q_hi;
         const int nin = min(32, nv - chunk * 32);
         const int v = chunk * 32 + min(lane, nin - 1);
@@ -394,29 +372,10 @@ k_vox_adj(const VoxBatch B)
             const int src = (int)(pp % P.n_src);
             const VoxGeom vg = vox_geom<true>(pr.G, vx, vy);
             const float2 Asv = J.op.atten_src[(int64_t)src * nv + v];
-            const float2 *wt = J.op.walk;
-            float2 Adv = make_float2(0.f, 0.f);
-            WalkSetup ws;
-            ws.rx = ws.ry = ws.Lx = ws.Ly = 0.f;
-            ws.n = 0;
-            if (wt)
-                Adv = wt[pp * nv + v];
-            else if (!walk_setup_f32(P, c, pr.G.Rdx.hi, pr.G.Rdy.hi, vx, vy, &ws))
-                walk_setup_f64(P, pr.Rdx, pr.Rdy, (double)vx, (double)vy, &ws);
+            const float2 Adv = J.op.walk[(pp - J.pair0) * nv + v];
             const float *wp = J.what + pp * E;
             for (int i = 0; i < nin; i++) {
-                float2 Ad;
-                if (wt) {
-                    Ad = make_float2(__shfl_sync(0xffffffffu, Adv.x, i), __shfl_sync(0xffffffffu, Adv.y, i));
-                } else {
-                    WalkSetup wi;
-                    wi.rx = __shfl_sync(0xffffffffu, ws.rx, i);
-                    wi.ry = __shfl_sync(0xffffffffu, ws.ry, i);
-                    wi.Lx = __shfl_sync(0xffffffffu, ws.Lx, i);
-                    wi.Ly = __shfl_sync(0xffffffffu, ws.Ly, i);
-                    wi.n = __shfl_sync(0xffffffffu, ws.n, i);
-                    Ad = walk_coop(J.op.cells, P.nx, P.ny, wi, DQf, lane);
-                }
+                const float2 Ad = make_float2(__shfl_sync(0xffffffffu, Adv.x, i), __shfl_sync(0xffffffffu, Adv.y, i));
                 const float sh = __shfl_sync(0xffffffffu, vg.s.hi, i);
                 const float sl = __shfl_sync(0xffffffffu, vg.s.lo, i);
                 const ff sg = {__shfl_sync(0xffffffffu, vg.sg.hi, i), __shfl_sync(0xffffffffu, vg.sg.lo, i)};
@@ -508,8 +467,13 @@ k_vox_adj(const VoxBatch B)
                 __syncwarp();
             }
         }
+        // a job that is one tile of a problem adds to the partial rows the
+        // earlier tiles left (tiles run in a fixed order on one stream)
         float *out = J.part + ((int64_t)by * nv + (int64_t)chunk * 32) * K;
-        for (int i = lane; i < nin * K; i += 32) out[i] = gw[i].x - gw[i].y;
+        if (J.accumulate)
+            for (int i = lane; i < nin * K; i += 32) out[i] += gw[i].x - gw[i].y;
+        else
+            for (int i = lane; i < nin * K; i += 32) out[i] = gw[i].x - gw[i].y;
     }
 }
 

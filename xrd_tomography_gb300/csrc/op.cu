@@ -66,6 +66,27 @@ struct Plan {
     bool tuned = false;
     cudaGraphExec_t mlem_exec = nullptr;
     int64_t mlem_cfg[3] = {};          // adj_warps, adj_tiles, fwd_grid of the captured graph
+    int64_t mlem_launches = 0;         // kernels in one iteration's graph
+    // Streaming: operators that keep no detector-side table of their own have
+    // their pairs cut into segments whose tables are walked, tile by tile,
+    // into one shared buffer within every call; each tile is then projected
+    // and back-projected before the next one is walked.
+    struct Seg {
+        int op;
+        int64_t p0, p1;      // pairs [p0, p1) of the operator
+        int64_t woff;        // first float2 of its rows in walkbuf; -1: the operator's own table
+    };
+    struct Tile {
+        std::vector<Seg> segs;
+        VoxJob *jobs_h = nullptr, *jobs_d = nullptr;
+        int64_t *off_d = nullptr;
+        std::vector<int64_t> off;   // 5 x (segments + 1), rows 0 and 1 used
+    };
+    bool streamed = false;
+    int64_t tile_budget = 0;           // bytes of walkbuf
+    std::vector<Tile> tiles;
+    float2 *walkbuf = nullptr;
+    std::vector<int> rows;             // partial-sum rows each operator's tiles use
 };
 
 namespace {
@@ -109,6 +130,12 @@ int op_alloc_t(xrdt_op *op, size_t count, T **out)
 void plan_free(Plan *pl)
 {
     if (!pl) return;
+    for (Plan::Tile &t : pl->tiles) {
+        if (t.jobs_h) cudaFreeHost(t.jobs_h);
+        if (t.jobs_d) cudaFree(t.jobs_d);
+        if (t.off_d) cudaFree(t.off_d);
+    }
+    if (pl->walkbuf) cudaFree(pl->walkbuf);
     if (pl->mlem_exec) cudaGraphExecDestroy(pl->mlem_exec);
     if (pl->jobs_h) cudaFreeHost(pl->jobs_h);
     if (pl->jobs_d) cudaFree(pl->jobs_d);
@@ -199,7 +226,38 @@ void plan_split(Plan *pl, int warps, int64_t tiles)
     pl->adj_tiles = tiles;
     pl->adj_smem = smem;
     const int bps = vox_adj_blocks_per_sm(warps, smem);
-    const int64_t items = pl->off[1 * (size_t)(n + 1) + n];
+    int64_t items = pl->off[1 * (size_t)(n + 1) + n];
+    if (pl->streamed) {
+        // each tile's segments split their pairs with the batch's pairs per
+        // group, capped at the operator's partial-sum rows; the reduction
+        // adds the rows any tile of the operator used
+        pl->rows.assign(n, 1);
+        items = 0;
+        for (Plan::Tile &t : pl->tiles) {
+            const int ns = (int)t.segs.size();
+            t.off.assign(5 * (size_t)(ns + 1), 0);
+            for (int k = 0; k < ns; k++) {
+                const Plan::Seg &sg = t.segs[k];
+                const xrdt_op *op = pl->ops[sg.op];
+                VoxJob J = pl->jobs_h[sg.op];
+                const int64_t len = sg.p1 - sg.p0;
+                int64_t g = std::min<int64_t>((len + ppg - 1) / ppg, op->groups_cap);
+                if (g < 1) g = 1;
+                J.groups = (int)g;
+                J.ppg = (int)((len + g - 1) / g);
+                J.pair0 = sg.p0;
+                J.pair1 = sg.p1;
+                J.accumulate = 1;
+                J.op.walk = sg.woff < 0 ? op->v.walk : pl->walkbuf + sg.woff;
+                t.jobs_h[k] = J;
+                pl->rows[sg.op] = std::max(pl->rows[sg.op], (int)g);
+                t.off[0 * (ns + 1) + k + 1] = t.off[0 * (ns + 1) + k] + len;
+                t.off[1 * (ns + 1) + k + 1] = t.off[1 * (ns + 1) + k] + (op->v.nv > 0 ? (int64_t)J.chunk_blocks * g : 0);
+            }
+            items = std::max(items, t.off[1 * (ns + 1) + ns]);
+        }
+        for (int i = 0; i < n; i++) pl->jobs_h[i].groups = pl->rows[i];
+    }
     pl->adj_grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)pl->sms * bps, items));
 }
 
@@ -210,7 +268,91 @@ int plan_upload(Plan *pl)
     CK(cudaMemcpyAsync(pl->jobs_d, pl->jobs_h, sizeof(VoxJob) * n, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(pl->off_d, pl->off.data(), sizeof(int64_t) * pl->off.size(), cudaMemcpyHostToDevice,
                        ctx->stream));
+    for (Plan::Tile &t : pl->tiles) {
+        // the tile's descriptors carry the per-call pointers of their problems
+        for (size_t k = 0; k < t.segs.size(); k++) {
+            const VoxJob &M = pl->jobs_h[t.segs[k].op];
+            VoxJob &J = t.jobs_h[k];
+            J.xd = M.xd; J.xc = M.xc; J.y = M.y; J.ymeas = M.ymeas; J.cbg = M.cbg; J.what = M.what;
+            J.part = M.part; J.sens = M.sens; J.g = M.g; J.w = M.w; J.xfull = M.xfull; J.xout = M.xout;
+        }
+        CK(cudaMemcpyAsync(t.jobs_d, t.jobs_h, sizeof(VoxJob) * t.segs.size(), cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(t.off_d, t.off.data(), sizeof(int64_t) * t.off.size(), cudaMemcpyHostToDevice,
+                           ctx->stream));
+    }
     return XRDT_OK;
+}
+
+VoxBatch tile_batch(const Plan *pl, const Plan::Tile &t)
+{
+    VoxBatch B;
+    B.jobs = t.jobs_d;
+    B.off = t.off_d;
+    B.counters = pl->counters_d;
+    B.n = (int)t.segs.size();
+    B.adj_warps = pl->adj_warps;
+    return B;
+}
+
+int64_t tile_items(const Plan::Tile &t, int row) { return t.off[(size_t)row * (t.segs.size() + 1) + t.segs.size()]; }
+
+// Walks the detector-side tables of a tile's segments into the shared buffer.
+cudaError_t tile_walks(const Plan *pl, const Plan::Tile &t, cudaStream_t st, int64_t *launches)
+{
+    for (const Plan::Seg &sg : t.segs) {
+        if (sg.woff < 0) continue;
+        const xrdt_op *op = pl->ops[sg.op];
+        cudaError_t e = launch_det_walk(op->v.P, op->src, nullptr, sg.p0, sg.p1 - sg.p0, op->v.vox_xy, op->v.nv,
+                                        op->v.cells, pl->walkbuf + sg.woff, st, launches);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+// Clears the partial-sum rows the tiles add to.
+cudaError_t zero_rows(const Plan *pl, cudaStream_t st)
+{
+    for (size_t i = 0; i < pl->ops.size(); i++) {
+        const xrdt_op *op = pl->ops[i];
+        if (op->v.nv == 0) continue;
+        cudaError_t e = cudaMemsetAsync(op->part, 0, sizeof(float) * (size_t)pl->rows[i] * op->v.nv * op->p.nwt, st);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+// The adjoint of every tile (after its walks) into the cleared partial rows;
+// what[] must hold the per-energy weights of all pairs.
+cudaError_t stream_adjoint(Plan *pl, cudaStream_t st, int64_t *launches)
+{
+    cudaError_t e = zero_rows(pl, st);
+    for (const Plan::Tile &t : pl->tiles) {
+        if (e == cudaSuccess) e = tile_walks(pl, t, st, launches);
+        const int64_t items = tile_items(t, 1);
+        if (e == cudaSuccess && items > 0)
+            e = launch_vox_adjoint(tile_batch(pl, t), (int)std::min<int64_t>(pl->adj_grid, items), pl->adj_smem, st,
+                                   launches);
+    }
+    return e;
+}
+
+// The forward of every tile (after its walks); MLEM: with the ratios and
+// per-energy weights, then the tile's adjoint, so a tile's table is walked
+// once per iteration.
+cudaError_t stream_forward(Plan *pl, bool mlem, cudaStream_t st, int64_t *launches)
+{
+    cudaError_t e = mlem ? zero_rows(pl, st) : cudaSuccess;
+    for (const Plan::Tile &t : pl->tiles) {
+        if (e == cudaSuccess) e = tile_walks(pl, t, st, launches);
+        const int64_t fi = tile_items(t, 0), ai = tile_items(t, 1);
+        if (e == cudaSuccess && fi > 0)
+            e = launch_vox_forward(tile_batch(pl, t), mlem, (int)std::min<int64_t>(pl->fwd_grid, fi), pl->fwd_smem,
+                                   st, launches);
+        if (mlem && e == cudaSuccess && ai > 0)
+            e = launch_vox_adjoint(tile_batch(pl, t), (int)std::min<int64_t>(pl->adj_grid, ai), pl->adj_smem, st,
+                                   launches);
+    }
+    return e;
 }
 
 VoxBatch plan_batch(const Plan *pl)
@@ -225,6 +367,70 @@ VoxBatch plan_batch(const Plan *pl)
 }
 
 int64_t plan_total(const Plan *pl, int row) { return pl->off[(size_t)row * (pl->ops.size() + 1) + pl->ops.size()]; }
+
+// Cuts the pairs of the operators without a table of their own into
+// segments of whole pixels (every view) and packs them, in operator order,
+// into tiles whose tables fit the walk buffer.  The buffer holds a quarter of
+// the free device memory, at most 8 GiB, or XRDT_WALK_TILE_BYTES when that is
+// set; one pixel column of the largest phantom is the least it holds.
+// Operators that keep a table ride along in the first tile.
+int plan_make_tiles(Plan *pl)
+{
+    xrdt_ctx *ctx = pl->ctx;
+    int64_t budget = 0;
+    const char *tb = getenv("XRDT_WALK_TILE_BYTES");
+    if (tb && *tb) budget = atoll(tb);
+    if (budget <= 0) {
+        size_t fr = 0, tot = 0;
+        if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+            cudaGetLastError();
+            fr = 0;
+        }
+        budget = std::min<int64_t>((int64_t)(fr / 4), (int64_t)8 << 30);
+    }
+    for (const xrdt_op *op : pl->ops)
+        if (op->v.nv > 0 && !op->v.walk)
+            budget = std::max<int64_t>(budget, (int64_t)sizeof(float2) * op->p.n_src * op->v.nv);
+    pl->tile_budget = budget;
+    const int64_t cap = budget / (int64_t)sizeof(float2);   // float2 rows of the buffer
+    pl->tiles.clear();
+    pl->tiles.emplace_back();
+    int64_t used = 0, most = 0;
+    for (int i = 0; i < (int)pl->ops.size(); i++) {
+        const xrdt_op *op = pl->ops[i];
+        const int64_t np = pairs_of(op), nv = op->v.nv;
+        if (nv == 0) continue;
+        if (op->v.walk) {
+            pl->tiles.front().segs.push_back({i, 0, np, -1});
+            continue;
+        }
+        const int64_t unit = op->p.n_src;   // whole pixels of every view
+        const int64_t seg = std::max<int64_t>(unit, cap / nv / unit * unit);
+        for (int64_t p0 = 0; p0 < np; p0 += seg) {
+            const int64_t len = std::min(seg, np - p0);
+            if (used > 0 && used + len * nv > cap) {
+                pl->tiles.emplace_back();
+                used = 0;
+            }
+            pl->tiles.back().segs.push_back({i, p0, p0 + len, used});
+            used += len * nv;
+            most = std::max(most, used);
+        }
+    }
+    cudaError_t e = cudaMalloc((void **)&pl->walkbuf, sizeof(float2) * (size_t)std::max<int64_t>(most, 1));
+    for (Plan::Tile &t : pl->tiles) {
+        const size_t ns = std::max<size_t>(t.segs.size(), 1);
+        if (e == cudaSuccess) e = cudaMallocHost((void **)&t.jobs_h, sizeof(VoxJob) * ns);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&t.jobs_d, sizeof(VoxJob) * ns);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&t.off_d, sizeof(int64_t) * 5 * (ns + 1));
+        if (e == cudaSuccess) memset(t.jobs_h, 0, sizeof(VoxJob) * ns);
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, XRDT_ERR_ALLOC, fmt("walk tiles: %s", cudaGetErrorString(e)));
+    }
+    return XRDT_OK;
+}
 
 int plan_create(xrdt_ctx *ctx, xrdt_op *const *ops, int n, Plan **out)
 {
@@ -254,9 +460,20 @@ int plan_create(xrdt_ctx *ctx, xrdt_op *const *ops, int n, Plan **out)
         J.what = op->what;
         J.part = op->part;
         J.sens = op->sens;
+        J.pair0 = 0;
+        J.pair1 = pairs_of(op);
+        J.accumulate = 0;
         fsmem = std::max(fsmem, vox_fwd_smem(op->v.P));
+        if (op->v.nv > 0 && !op->v.walk) pl->streamed = true;
     }
     pl->fwd_smem = fsmem;
+    if (pl->streamed) {
+        int rc = plan_make_tiles(pl);
+        if (rc) {
+            plan_free(pl);
+            return rc;
+        }
+    }
     // the widest adjoint block the shared memory allows
     int optin = 0;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
@@ -288,7 +505,10 @@ int plan_sens(Plan *pl)
         ProfScope ps(ctx, XRDT_KERNEL_VOX_UPDATE);
         CK(launch_vox_wtab(B, plan_total(pl, 4), true, st, &ctx->launches));
     }
-    {
+    if (pl->streamed) {
+        ProfScope ps(ctx, XRDT_KERNEL_VOX_ADJOINT);
+        CK(stream_adjoint(pl, st, &ctx->launches));
+    } else {
         ProfScope ps(ctx, XRDT_KERNEL_VOX_ADJOINT);
         CK(launch_vox_adjoint(B, pl->adj_grid, pl->adj_smem, st, &ctx->launches));
     }
@@ -335,6 +555,7 @@ std::string tune_key(const Plan *pl)
     for (const xrdt_op *op : pl->ops)
         key += fmt("|%dx%d,v%d,s%d,d%d,e%d,k%d", op->p.nx, op->p.ny, op->v.nv, op->p.n_src, op->v.P.n_det,
                    op->v.P.e_hi - op->v.P.e_lo + 1, op->p.nwt);
+    if (pl->streamed) key += fmt("|tiles%lld", (long long)pl->tile_budget);
     return key;
 }
 
@@ -398,6 +619,9 @@ int plan_tune(Plan *pl)
     int rc = plan_upload(pl);
     if (rc) return rc;
     CK(launch_vox_wtab(plan_batch(pl), plan_total(pl, 4), true, st, &ctx->launches));
+    // streamed: the candidates are timed on the first tile, walked once here
+    // (they add into partial rows that every real call clears first)
+    if (pl->streamed) CK(tile_walks(pl, pl->tiles.front(), st, &ctx->launches));
     cudaEvent_t a, b;
     CK(cudaEventCreate(&a));
     CK(cudaEventCreate(&b));
@@ -416,7 +640,15 @@ int plan_tune(Plan *pl)
             plan_split(pl, w, slots * per_slot[ti]);
             if ((rc = plan_upload(pl))) break;
             cudaError_t e = cudaEventRecord(a, st);
-            if (e == cudaSuccess) e = launch_vox_adjoint(plan_batch(pl), pl->adj_grid, pl->adj_smem, st, &ctx->launches);
+            if (e == cudaSuccess && pl->streamed) {
+                const Plan::Tile &t0 = pl->tiles.front();
+                const int64_t items = tile_items(t0, 1);
+                if (items > 0)
+                    e = launch_vox_adjoint(tile_batch(pl, t0), (int)std::min<int64_t>(pl->adj_grid, items),
+                                           pl->adj_smem, st, &ctx->launches);
+            } else if (e == cudaSuccess) {
+                e = launch_vox_adjoint(plan_batch(pl), pl->adj_grid, pl->adj_smem, st, &ctx->launches);
+            }
             if (e == cudaSuccess) e = cudaEventRecord(b, st);
             if (e == cudaSuccess) e = cudaEventSynchronize(b);
             float ms = 0.f;
@@ -472,7 +704,13 @@ int plan_forward(Plan *pl, const float *const *x, float *const *y)
     }
     // a problem without voxels gets zeros: its pairs sum nothing
     ProfScope ps(ctx, XRDT_KERNEL_VOX_FORWARD);
-    CK(launch_vox_forward(B, false, pl->fwd_grid, pl->fwd_smem, st, &ctx->launches));
+    if (pl->streamed) {
+        for (int i = 0; i < n; i++)
+            if (pl->ops[i]->v.nv == 0) CK(cudaMemsetAsync(y[i], 0, sizeof(float) * (size_t)pl->ops[i]->rays, st));
+        CK(stream_forward(pl, false, st, &ctx->launches));
+    } else {
+        CK(launch_vox_forward(B, false, pl->fwd_grid, pl->fwd_smem, st, &ctx->launches));
+    }
     return XRDT_OK;
 }
 
@@ -498,7 +736,8 @@ int plan_adjoint(Plan *pl, const float *const *w, float *const *g)
     }
     {
         ProfScope ps(ctx, XRDT_KERNEL_VOX_ADJOINT);
-        CK(launch_vox_adjoint(B, pl->adj_grid, pl->adj_smem, st, &ctx->launches));
+        if (pl->streamed) CK(stream_adjoint(pl, st, &ctx->launches));
+        else CK(launch_vox_adjoint(B, pl->adj_grid, pl->adj_smem, st, &ctx->launches));
     }
     ProfScope ps(ctx, XRDT_KERNEL_VOX_UPDATE);
     CK(launch_vox_reduce(B, plan_total(pl, 2), 2, st, &ctx->launches));
@@ -538,9 +777,16 @@ int plan_mlem(Plan *pl, const float *const *y, const float *const *c, float *con
             cudaGraph_t graph;
             CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
             int64_t dummy = 0;
-            cudaError_t le = launch_vox_forward(B, true, pl->fwd_grid, pl->fwd_smem, st, &dummy);
-            if (le == cudaSuccess) le = launch_vox_adjoint(B, pl->adj_grid, pl->adj_smem, st, &dummy);
+            cudaError_t le;
+            if (pl->streamed) {
+                // per tile: walk, forward with the ratios, adjoint
+                le = stream_forward(pl, true, st, &dummy);
+            } else {
+                le = launch_vox_forward(B, true, pl->fwd_grid, pl->fwd_smem, st, &dummy);
+                if (le == cudaSuccess) le = launch_vox_adjoint(B, pl->adj_grid, pl->adj_smem, st, &dummy);
+            }
             if (le == cudaSuccess) le = launch_vox_reduce(B, plan_total(pl, 2), 1, st, &dummy);
+            pl->mlem_launches = dummy;
             cudaError_t ce = cudaStreamEndCapture(st, &graph);
             if (le != cudaSuccess) {
                 if (ce == cudaSuccess) cudaGraphDestroy(graph);
@@ -557,7 +803,7 @@ int plan_mlem(Plan *pl, const float *const *y, const float *const *c, float *con
             ProfScope ps(ctx, XRDT_KERNEL_VOX_FORWARD);   // the whole iteration (three kernels)
             for (int it = 0; it < iters; it++) CK(cudaGraphLaunch(pl->mlem_exec, st));
         }
-        ctx->launches += 3 * (int64_t)iters;
+        ctx->launches += pl->mlem_launches * (int64_t)iters;
     }
     // empty voxels have no sensitivity: the update sets them to 0
     for (int i = 0; i < n; i++) {

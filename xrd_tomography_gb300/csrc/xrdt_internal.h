@@ -234,6 +234,10 @@ struct VoxJob {
     const float *w;            // [rays] adjoint weights
     const float *xfull;        // [nx*ny*nwt] coefficients to gather
     float *xout;               // [nx*ny*nwt] coefficients to scatter to
+    // pairs [pair0, pair1) of the problem that this job covers (all of them,
+    // or one tile); op.walk holds their detector-side integrals from row 0
+    int64_t pair0, pair1;
+    int accumulate;            // adjoint: add to the partial rows instead of writing them
     int pad;
 };
 // Kernel argument of the batched operator kernels.  off holds five prefix
