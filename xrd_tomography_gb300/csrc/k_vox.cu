@@ -54,16 +54,19 @@ struct EnergyTerm {
     float pref, w_hi, w_lo, c_hi, c_lo, half;
 };
 
-// Per-(pair, voxel) inputs of sigma^2 = c1 s^2 + c2 sg / s^2 as pairs.
+// Per-(pair, voxel) parts of sigma^2 = c1 s^2 + c2(e) sg / s^2 as pairs:
+// c1 s^2 (c1, the energy-bin width term, is the same for every source bin)
+// and sg / s^2.
 struct SigmaGeom {
-    ff s2, sg_s2;
+    ff t1, sg_s2;
 };
 
-__device__ __forceinline__ SigmaGeom sigma_geom(float sh, float sl, ff sg)
+__device__ __forceinline__ SigmaGeom sigma_geom(float sh, float sl, ff sg, ff c1)
 {
     SigmaGeom g;
-    g.s2 = ff_sqr(ff{sh, sl});
-    g.sg_s2 = ff_div(sg, g.s2);
+    const ff s2 = ff_sqr(ff{sh, sl});
+    g.t1 = ff_mul(c1, s2);
+    g.sg_s2 = ff_div(sg, s2);
     return g;
 }
 
@@ -85,8 +88,7 @@ __device__ __forceinline__ EnergyTerm energy_term(const float *en, int E, int el
     }
     // sigma^2 as a pair: deep in the Gaussian's tail the exponent amplifies
     // its relative error by (q distance / sigma)^2 / 2
-    const ff sig2 = ff_add(ff_mul(ff{en[4 * E + el], en[6 * E + el]}, sgm.s2),
-                           ff_mul(ff{en[5 * E + el], en[7 * E + el]}, sgm.sg_s2));
+    const ff sig2 = ff_add(sgm.t1, ff_mul(ff{en[5 * E + el], en[7 * E + el]}, sgm.sg_s2));
     // 1/sigma to within an ulp: one Newton step on rsqrt, with the low part
     const float r0 = rsqrtf(sig2.hi);
     const float h = fmaf(-0.5f * sig2.hi * r0, r0, 0.5f) - 0.5f * sig2.lo * r0 * r0;
@@ -224,7 +226,7 @@ __device__ __forceinline__ void vox_fwd_pair(const VoxJob &J, int64_t pidx, unsi
             const float Wg = __shfl_sync(0xffffffffu, vg.Wg, i);
             const float Asx = __shfl_sync(0xffffffffu, Asv.x, i);
             const float Asy = __shfl_sync(0xffffffffu, Asv.y, i);
-            const SigmaGeom sgm = sigma_geom(sh, sl, sg);
+            const SigmaGeom sgm = sigma_geom(sh, sl, sg, ff{en[4 * E], en[6 * E]});
             const float *xrow = xd + (int64_t)(chunk * 32 + i) * K;
 #pragma unroll 1
             for (int el = lane; el < E; el += 32) {
@@ -339,9 +341,11 @@ k_vox_adj(const VoxBatch B)
         float *rows_lo = (float *)(prs + nwarps);                           // [warps][E]
         int2 *wins = (int2 *)(sm + al16((size_t)((unsigned char *)(rows_lo + (size_t)nwarps * E) - sm)));
                                                                             // [warps][E]
+        unsigned char *eranges = (unsigned char *)(wins + (size_t)nwarps * E);   // [warps][2][K]
         float4 *rw = rows + (size_t)wid * E;
         float *rwl = rows_lo + (size_t)wid * E;
         int2 *ww = wins + (size_t)wid * E;
+        unsigned char *e_first = eranges + (size_t)wid * 2 * K, *e_end = e_first + K;
         float2 *gw = gacc + (size_t)wid * 32 * K;
         PairRec &pr = prs[wid];
         stage_energy_rows(J, en, tid, blockDim.x);
@@ -382,11 +386,11 @@ k_vox_adj(const VoxBatch B)
                 const float Wg = __shfl_sync(0xffffffffu, vg.Wg, i);
                 const float Asx = __shfl_sync(0xffffffffu, Asv.x, i);
                 const float Asy = __shfl_sync(0xffffffffu, Asv.y, i);
-                const SigmaGeom sgm = sigma_geom(sh, sl, sg);
+                const SigmaGeom sgm = sigma_geom(sh, sl, sg, ff{en[4 * E], en[6 * E]});
                 // lane = energy: the energy's factors and its coarse-bin
-                // window (the bins within 7.5 sigma; the terms beyond are
-                // below 7e-13 of the peak), with the running maximum of the
-                // windows' upper ends in ww[e].x
+                // window (the bins within 13.25 sigma: every term FP32 can
+                // represent), with the running maximum of the windows' upper
+                // ends in ww[e].x
                 int run_max = -1;
                 for (int eb = 0; eb < E; eb += 32) {
                     const int el = eb + lane;
@@ -430,30 +434,33 @@ k_vox_adj(const VoxBatch B)
                     run_min = __shfl_sync(0xffffffffu, m, 0);
                 }
                 __syncwarp();
-                // lane = coarse bin k over the bins some window reaches.  The
-                // energies whose window holds k lie in [e0, e1]: below e0
-                // every window ends before k, above e1 every window starts
-                // after it (both running bounds are monotone, so a binary
-                // search finds them).
+                // The energies whose window holds bin k lie in [e0(k), e1(k)):
+                // below e0 every window ends before k (the running maximum of
+                // the upper ends is below k), from e1 on every window starts
+                // after it (the running minimum of the lower ends is above
+                // k).  Both bounds are monotone in k, so energy e is e0 for the
+                // bins (M[e-1], M[e]] and e1 for [m[e-1], m[e]); lane = energy
+                // writes those entries for the bins in [kmin, kmax].
                 const int kmin = run_min, kmax = run_max;
+                for (int eb = 0; eb < E && kmin <= kmax; eb += 32) {
+                    const int el = eb + lane;
+                    if (el < E) {
+                        const int2 cur = ww[el];
+                        const int2 prv = el > 0 ? ww[el - 1] : make_int2(-1, kmin);
+                        for (int k = max(prv.x + 1, kmin); k <= min(cur.x, kmax); k++) e_first[k] = (unsigned char)el;
+                        if (el > 0)
+                            for (int k = max(prv.y, kmin); k <= min(cur.y - 1, kmax); k++) e_end[k] = (unsigned char)el;
+                        if (el == E - 1)
+                            for (int k = max(cur.y, kmin); k <= kmax; k++) e_end[k] = (unsigned char)E;
+                    }
+                }
+                __syncwarp();
+                // lane = coarse bin k over the bins some window reaches
                 float2 *gi = gw + i * K;
                 for (int kb = kmin; kb <= kmax; kb += 32) {
                     const int k = kb + lane;
                     if (k > kmax) break;
-                    int lo = 0, hi = E;
-                    while (lo < hi) {
-                        const int mid = (lo + hi) >> 1;
-                        if (ww[mid].x < k) lo = mid + 1;
-                        else hi = mid;
-                    }
-                    const int e0 = lo;
-                    hi = E;
-                    while (lo < hi) {
-                        const int mid = (lo + hi) >> 1;
-                        if (ww[mid].y <= k) lo = mid + 1;
-                        else hi = mid;
-                    }
-                    const int e1 = lo;   // one past the last
+                    const int e0 = e_first[k], e1 = e_end[k];
                     const float4 q = cq[k];
                     float acc = 0.f;
                     for (int e = e0; e < e1; e++) {
@@ -647,7 +654,7 @@ size_t vox_adj_smem(const DevProblem &P, int warps)
     const int E = P.e_hi - P.e_lo + 1, K = P.nwt;
     return al16(sizeof(float) * kEnRows * E) + sizeof(float4) * K + sizeof(float4) * (size_t)warps * E +
            sizeof(float2) * (size_t)warps * 32 * K + sizeof(PairRec) * warps + sizeof(float) * (size_t)warps * E +
-           16 + sizeof(int2) * (size_t)warps * E;
+           16 + sizeof(int2) * (size_t)warps * E + (size_t)warps * 2 * K;
 }
 
 int vox_fwd_blocks_per_sm(size_t smem)

@@ -83,6 +83,12 @@ __device__ __forceinline__ float lg2_approx(float x)
     asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
 }
+__device__ __forceinline__ float sqrt_approx(float x)
+{
+    float y;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 __device__ __forceinline__ float rsqrt_approx(float x)
 {
     float y;
@@ -317,8 +323,10 @@ __device__ __forceinline__ void coarse_window(float w, float half, float q_lo, f
     const float ua = w - half - q_lo, ub = w + half - q_lo;
     const float da = fmaf(4.f * qa, ua, qb * qb), db = fmaf(4.f * qa, ub, qb * qb);
     if (da >= 0.f && db >= 0.f) {
-        const float na_ = 2.f * ua / (qb + sqrtf(da));
-        const float nb_ = 2.f * ub / (qb + sqrtf(db));
+        // approximate root and quotient: the bin window is widened by one bin
+        // on each side anyway
+        const float na_ = __fdividef(2.f * ua, qb + sqrt_approx(da));
+        const float nb_ = __fdividef(2.f * ub, qb + sqrt_approx(db));
         lo = max(lo, floor_nc(na_) - 1);
         hi = min(hi, floor_nc(nb_) + 1);
     }
