@@ -44,11 +44,11 @@ sys.path.insert(0, ROOT)
 
 WORKLOAD = 1            # index of the synthetic configuration
 FLUSH_BYTES = 256 << 20
-# DRAM bytes (read + write) of one k_fwd launch, from an ncu capture of
-# this benchmark's command: per workload index, the mean over the launches of
-# one step (the projection goes through in tiles of pairs: on the 256x256
-# workload five tiles of 17280 pairs and one of 5760)
-K_FWD_DRAM_BYTES = {1: (5 * (5486237455 + 16250158) + (1863039180 + 6348800)) // 6}
+# DRAM bytes (read + write) of k_fwd per (pair, non-empty voxel), from one
+# ncu capture of a single launch on the 128x128 workload (4096 pairs x 5009
+# voxels); the traffic is the launch's walk table plus a fixed part, so the
+# 256x256 figure below is that rate times the pair-voxels of its mean launch
+K_FWD_DRAM_BYTES_PER_PAIR_VOXEL = None
 # issue slots busy in k_fwd (ncu SpeedOfLight, 128x128 workload): the kernel
 # is bound by instruction issue, not by the SFU rate of the roofline below
 K_FWD_ISSUE_BUSY = 0.8338
@@ -62,8 +62,12 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU baseline sample")
     ap.add_argument("--no-baselines", action="store_true", help="skip the CPU and plain-FP64 baselines")
-    ap.add_argument("--workload", type=int, default=WORKLOAD, choices=[0, 1, 2, 4],
-                    help="synthetic configuration (1 is the benchmark; 0 and 2 are small profiling cases)")
+    ap.add_argument("--workload", type=int, default=WORKLOAD, choices=[0, 1, 2, 3, 4],
+                    help="synthetic configuration (1 is the benchmark; 0 and 2 are small profiling cases; "
+                         "3 runs batched MLEM on the 64 phantoms of the batched configuration at their stated "
+                         "sizes, several minutes per iteration)")
+    ap.add_argument("--batch", type=int, default=64, help="--workload 3: number of phantoms")
+    ap.add_argument("--iters", type=int, default=1, help="--workload 3: timed MLEM iterations")
     return ap.parse_args()
 
 
@@ -186,11 +190,21 @@ def cpu_sample_rate(inp, budget_s: float, rng_seed: int = 0):
     pyoracle.forward_rays(inp, calib, threads=threads)
     t_calib = time.perf_counter() - t0
     n = int(max(threads, min(p.rays, threads * max(1.0, budget_s / max(t_calib, 1e-3)))))
-    rays = rng.choice(p.rays, n, replace=False)
+    rays = np.sort(rng.choice(p.rays, n, replace=False))
     t0 = time.perf_counter()
-    pyoracle.forward_rays(inp, rays, threads=threads)
+    No, Co, _, _ = pyoracle.forward_rays(inp, rays, threads=threads)
     dt = time.perf_counter() - t0
-    return ref_equiv_terms(inp, n) / dt / 1e9, threads, n, dt
+    return ref_equiv_terms(inp, n) / dt / 1e9, threads, n, dt, rays, No, Co
+
+
+def err_summary(got, ref, floor=1e-6):
+    """Max and mean relative error of got against the FP64 values ref; an
+    entry below floor times the largest is compared against that floor."""
+    got = np.asarray(got, np.float64)
+    ref = np.asarray(ref, np.float64)
+    den = np.maximum(np.abs(ref), floor * max(float(np.abs(ref).max()), 1e-300))
+    e = np.abs(got - ref) / den
+    return {"max_rel": float(e.max()), "mean_rel": float(e.mean()), "n": int(e.size)}
 
 
 def run_reference(args):
@@ -332,17 +346,15 @@ def vox_mlem_bench(xt, synth, ctx, stream, dev, iters=50):
     f = ctx.kernel_stats(xt.api.KERNEL_VOX_FORWARD)
     a = ctx.kernel_stats(xt.api.KERNEL_VOX_ADJOINT)
     ctx.set_profiling(False)
-    # plain FP64 path on a ray subset
+    # plain FP64 path on a ray subset, its kernels timed with CUDA events
     rng = np.random.default_rng(3)
     sub = np.sort(rng.choice(p.rays, min(p.rays, plain_wave(dev)), replace=False))
     xh = x.cpu().numpy()
     wh = w[torch.from_numpy(sub).to(dev)].cpu().numpy()
-    t0 = time.perf_counter()
-    op.forward_rays_fp64(xh, sub)
-    t1 = time.perf_counter()
-    op.adjoint_rays_fp64(wh, sub)
-    t2 = time.perf_counter()
-    plain_iter_ms = ((t1 - t0) + (t2 - t1)) * 1e3 * p.rays / sub.size
+    plain_iter_ms = plain_vox_ms(xt, ctx, op, xh, wh, sub) * p.rays / sub.size
+    # the operator's forward against the oracle on sampled rays
+    err = vox_err_vs_oracle(inp, x.cpu().numpy(), op.forward(x, torch.empty(p.rays, device=dev)).cpu().numpy(),
+                            n=64, seed=4)
     op.close()
     return {"workload": f"{p.nx}x{p.ny} phantom, {p.nwt} coarse-q coefficients per voxel "
                         f"({int((np.asarray(inp.seg) > 0).sum())} non-empty voxels), {p.rays} rays, "
@@ -351,8 +363,31 @@ def vox_mlem_bench(xt, synth, ctx, stream, dev, iters=50):
             "forward_ms": f[1] / max(1, f[0]), "adjoint_ms": a[1] / max(1, a[0]),
             "poisson_loglik_after": loglik,
             "plain_fp64_ms_per_iter": plain_iter_ms,
-            "plain_fp64_sample": f"forward and adjoint on {sub.size} of {p.rays} rays, scaled to all rays",
-            "speedup_vs_plain_fp64": plain_iter_ms / ms_iter}
+            "plain_fp64_sample": f"forward and adjoint on {sub.size} of {p.rays} rays (kernel time, CUDA events), "
+                                 f"scaled to all rays",
+            "speedup_vs_plain_fp64": plain_iter_ms / ms_iter,
+            "forward_err_vs_oracle": err}
+
+
+def plain_vox_ms(xt, ctx, op, x_host, w_host, rays):
+    """Device milliseconds of the FP64 kernel at the reference's launch shape
+    for the forward and the adjoint of the listed rays (CUDA events around
+    each launch; the host-side staging of the call is not counted)."""
+    ctx.set_profiling(True)
+    op.forward_rays_fp64(x_host, rays)
+    op.adjoint_rays_fp64(w_host, rays)
+    n, ms, _ = ctx.kernel_stats(xt.api.KERNEL_PLAIN)
+    ctx.set_profiling(False)
+    return ms
+
+
+def vox_err_vs_oracle(inp, x_host, y_gpu, n, seed):
+    """The per-voxel operator's forward against the FP64 oracle on n sampled rays."""
+    from oracle import pyoracle
+    pyoracle.build(ref=False)
+    rays = np.sort(np.random.default_rng(seed).choice(inp.problem.rays, n, replace=False))
+    y_ref, _ = pyoracle.vox_rays(inp, rays, x=x_host)
+    return err_summary(np.asarray(y_gpu)[rays], y_ref)
 
 
 def batch_mlem_bench(xt, synth, ctx, stream, dev, n=8, iters=10):
@@ -398,17 +433,13 @@ def batch_mlem_bench(xt, synth, ctx, stream, dev, n=8, iters=10):
         ev[1].record(stream)
         torch.cuda.synchronize(dev)
         ms_seq += ev[0].elapsed_time(ev[1]) / iters
-    # plain FP64 forward + adjoint on a few rays of every problem
+    # plain FP64 forward + adjoint on a few rays of every problem (kernel time)
     plain_ms = 0.0
     rng = np.random.default_rng(9)
     for k, (inp, op) in enumerate(zip(inps, ops)):
         sub = np.sort(rng.choice(inp.problem.rays, min(inp.problem.rays, plain_wave(dev)), replace=False))
-        xh = x0[k].cpu().numpy()
-        wh = np.ones(sub.size, np.float32)
-        t0 = time.perf_counter()
-        op.forward_rays_fp64(xh, sub)
-        op.adjoint_rays_fp64(wh, sub)
-        plain_ms += (time.perf_counter() - t0) * 1e3 * inp.problem.rays / sub.size
+        plain_ms += plain_vox_ms(xt, ctx, op, x0[k].cpu().numpy(), np.ones(sub.size, np.float32), sub) * \
+            inp.problem.rays / sub.size
     pv = sum(int((i.seg > 0).sum()) * i.problem.n_src * i.problem.n_col * i.problem.n_row for i in inps)
     sizes = [f"{i.problem.nx}^2/{i.problem.n_src}v/{i.problem.n_col}px" for i in inps]
     batch.close()
@@ -420,10 +451,108 @@ def batch_mlem_bench(xt, synth, ctx, stream, dev, n=8, iters=10):
             "pair_voxels_per_iter": pv, "g_pair_voxels_per_s": pv / (ms_batch * 1e-3) / 1e9,
             "sequential_ms_per_iter": ms_seq, "batching_speedup": ms_seq / ms_batch,
             "plain_fp64_ms_per_iter": plain_ms, "speedup_vs_plain_fp64": plain_ms / ms_batch,
-            "plain_fp64_sample": f"forward and adjoint on {plain_wave(dev)} rays of every problem (16 blocks per SM), "
-                                 f"scaled to all rays",
+            "plain_fp64_sample": f"forward and adjoint on {plain_wave(dev)} rays of every problem (16 blocks per SM, "
+                                 f"kernel time from CUDA events), scaled to all rays",
             "autotuned": {"adjoint_warps": warps, "adjoint_tiles": tiles, "forward_grid": fgrid,
                           "adjoint_grid": agrid}}
+
+
+def run_batched_stated(args):
+    """--workload 3: batched per-voxel MLEM on the batched configuration at its
+    stated sizes -- args.batch phantoms (64) with sides uniform in 64-384
+    voxels, 60-360 views, 128-768 px, 64 energy bins, 32 coefficients per
+    voxel -- as one xrdt_batch: every operator streams its detector-side
+    table in tiles inside each iteration, one CUDA graph per iteration.  One
+    warm-up call (the sensitivity, the graph capture and one iteration), then
+    args.iters timed iterations.  The counts are seeded Poisson draws around
+    a flat level (the iteration's work does not depend on their values)."""
+    import torch
+    import xrd_tomography_gb300 as xt
+    from xrd_tomography_gb300 import synth
+    from xrd_tomography_gb300 import build as lib_build
+
+    ws, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    lib_build.build()
+    os.environ.setdefault("XRDT_WALK_CACHE", "0")
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    ctx = xt.Context(local, stream=stream.cuda_stream)
+    t_setup = time.perf_counter()
+    inps = synth.batch_inputs(args.batch)
+    ops = [xt.Operator(i.problem, i.spectrum, i.seg, i.a1, i.a2, ctx=ctx) for i in inps]
+    gen = torch.Generator(device=dev).manual_seed(23)
+    ys, cs, xs = [], [], []
+    for inp, op in zip(inps, ops):
+        r = inp.problem.rays
+        ys.append(torch.poisson(torch.full((r,), 100.0, device=dev), generator=gen))
+        cs.append(torch.full((r,), 5.0, device=dev))
+        on = torch.from_numpy(np.repeat(np.asarray(inp.seg).reshape(-1) > 0, inp.problem.nwt)).to(dev)
+        xs.append(torch.where(on, 1.0, 0.0).float())
+    batch = xt.Batch(ops, ctx=ctx)
+    warps, tiles, fgrid, agrid = batch.tune()
+    batch.mlem(ys, cs, xs, 1)
+    torch.cuda.synchronize(dev)
+    t_setup = time.perf_counter() - t_setup
+    launches0 = ctx.launches
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    barrier(ws)
+    with ClockSampler(local) as clk:
+        ev[0].record(stream)
+        batch.mlem(ys, cs, xs, args.iters)
+        ev[1].record(stream)
+        torch.cuda.synchronize(dev)
+    ms_iter = all_max(ws, ev[0].elapsed_time(ev[1]) / args.iters, dev)
+    gpu_launches = ctx.launches - launches0
+    pv = [int((np.asarray(i.seg) > 0).sum()) * i.problem.n_src * i.problem.n_col * i.problem.n_row for i in inps]
+    # plain FP64 path on four problems (smallest, largest, two others), scaled
+    # by pair-voxels to the batch
+    order = np.argsort(pv)
+    picks = sorted({int(order[0]), int(order[-1]), int(order[len(order) // 3]), int(order[2 * len(order) // 3])})
+    rng = np.random.default_rng(9)
+    plain_ms, plain_pv = 0.0, 0
+    for k in picks:
+        inp, op = inps[k], ops[k]
+        sub = np.sort(rng.choice(inp.problem.rays, min(inp.problem.rays, plain_wave(dev)), replace=False))
+        plain_ms += plain_vox_ms(xt, ctx, op, xs[k].cpu().numpy(), np.ones(sub.size, np.float32), sub) * \
+            inp.problem.rays / sub.size
+        plain_pv += pv[k]
+    plain_iter_ms = plain_ms * sum(pv) / plain_pv
+    # the operators' forward against the oracle on sampled rays of three problems
+    errs = {}
+    for k in (int(order[0]), int(order[len(order) // 2]), int(order[-1])):
+        inp, op = inps[k], ops[k]
+        y = op.forward(xs[k], torch.empty(inp.problem.rays, device=dev))
+        errs[f"{inp.problem.nx}^2/{inp.problem.n_src}v/{inp.problem.n_col}px"] = \
+            vox_err_vs_oracle(inp, xs[k].cpu().numpy(), y.cpu().numpy(), n=8, seed=k)
+    clocks = clk.summary()
+    if rank == 0:
+        line = {
+            "metric": "batched per-voxel MLEM iterations per second (forward + adjoint + update)",
+            "value": 1e3 / ms_iter, "unit": "iter/s", "n_gpus": ws, "steps": args.iters, "warmup": 1,
+            "ms_per_step": ms_iter, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (FP64 geometry decisions and global sums)", "data": "synthetic (seeded)",
+            "config": {"workload": f"{args.batch} phantoms of the batched configuration at its stated sizes "
+                                   f"(sides 64-384, 60-360 views, 128-768 px), 64 energy bins, "
+                                   f"{inps[0].problem.nwt} coefficients per voxel, one xrdt_batch, detector-side "
+                                   f"tables streamed in tiles",
+                       "pair_voxels_per_iter": int(sum(pv)), "rays": int(sum(i.problem.rays for i in inps)),
+                       "sizes": [f"{i.problem.nx}^2/{i.problem.n_src}v/{i.problem.n_col}px" for i in inps]},
+            "g_pair_voxels_per_s": sum(pv) / (ms_iter * 1e-3) / 1e9,
+            "plain_fp64_ms_per_iter": plain_iter_ms,
+            "speedup_vs_plain_fp64": plain_iter_ms / ms_iter,
+            "plain_fp64_sample": f"forward and adjoint of {plain_wave(dev)} rays of problems {picks} "
+                                 f"(kernel time, CUDA events), scaled by pair-voxels to the batch",
+            "forward_err_vs_oracle": errs,
+            "autotuned": {"adjoint_warps": warps, "adjoint_tiles": tiles, "forward_grid": fgrid,
+                          "adjoint_grid": agrid},
+            "setup_s": t_setup, "gpu_launches": gpu_launches, "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    barrier(ws)
+    batch.close()
+    ctx.close()
 
 
 def run_ours(args):
@@ -534,19 +663,19 @@ def run_ours(args):
         ex2_peak = probe.xrdt_probe_peak(1)
         fma_peak = probe.xrdt_probe_peak(0)
         fp64_peak = probe.xrdt_probe_peak(2)
+        pair_voxels = float(p.n_src) * p.n_col * p.n_row * int((inp.seg > 0).sum())
         per_launch_ms = fwd_ms / max(1, fwd_n)
         work = fwd_work / max(1, fwd_n)
         achieved = work / (per_launch_ms * 1e-3) / 1e9
         line["roofline"] = {
             "bound": "sfu", "achieved": achieved, "peak": ex2_peak / 1e9, "unit": "G exp2/s",
             "frac": achieved / (ex2_peak / 1e9) if ex2_peak > 0 else None,
-            "traffic": K_FWD_DRAM_BYTES.get(args.workload),
-            "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum per k_fwd launch, mean over "
-                              "the tiles of a step (profiles/k_fwd_256x256_dram.md)"
-                              if args.workload in K_FWD_DRAM_BYTES else None,
+            "traffic": (K_FWD_DRAM_BYTES_PER_PAIR_VOXEL * pair_voxels / max(1, fwd_n / args.steps)
+                        if K_FWD_DRAM_BYTES_PER_PAIR_VOXEL else None),
+            "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one k_fwd launch on the 128x128 "
+                              "workload (ncu), per (pair, voxel), scaled to this workload's mean launch",
             "issue_slots_busy": K_FWD_ISSUE_BUSY,
-            "issue_source": "ncu sm__instruction_throughput / Issue Slots Busy of k_fwd "
-                            "(profiles/k_fwd_128x128_sections.md)",
+            "issue_source": "ncu Issue Slots Busy of k_fwd on the 128x128 workload",
             "kernel": "k_fwd (factored forward projector)",
             "work_per_launch": work, "launch_ms": per_launch_ms,
             "peak_source": "measured on this GPU by xrdt_probe_peak (ex2.approx, all SMs)",
@@ -563,10 +692,16 @@ def run_ours(args):
             plain_v = ref_equiv_terms(inp, sub.size) / dt / 1e9
             line["plain_fp64_gpu"] = {"value": plain_v, "unit": "G ray-voxel-q/s", "sample_rays": int(sub.size),
                                       "speedup_of_value": value / plain_v}
-            cv, cores, n, dt = cpu_sample_rate(inp, args.cpu_seconds)
+            cv, cores, n, dt, srays, No, Co = cpu_sample_rate(inp, args.cpu_seconds)
             line["cpu_baseline"] = {"value": cv, "unit": "G ray-voxel-q/s", "cores": cores, "kind": "port",
                                     "sample": f"{n} randomly drawn rays of the {p.rays}-ray projection "
                                               f"({dt:.1f} s, FP64 oracle, OpenMP over rays)"}
+            # the timed projection's outputs against the oracle on the same rays
+            idx = torch.from_numpy(srays).to(dev)
+            line["err_vs_oracle"] = {
+                "N": err_summary(Nd[idx].cpu().numpy(), No), "C": err_summary(Cd[idx].cpu().numpy(), Co),
+                "rays": f"the {n} rays of the CPU sample; relative error, entries below 1e-6 of the "
+                        f"sample's largest compared against that floor"}
         print(json.dumps(line), flush=True)
     barrier(ws)
     ctx.close()
@@ -576,6 +711,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == 3:
+        run_batched_stated(args)
     else:
         run_ours(args)
 

@@ -260,6 +260,8 @@ void build_host_tables(const xrdt_problem *p, const DevProblem &P, const float *
         const double f1 = r.ein * r.ein * r.ein, f2 = P.kn0 + P.kn1 * r.ein + P.kn2 * r.ein * r.ein;
         r.inv_f1 = (float)(1.0 / f1);
         r.inv_f2 = (float)(1.0 / f2);
+        r.inv_f1_lo = (float)(1.0 / f1 - (double)r.inv_f1);
+        r.inv_f2_lo = (float)(1.0 / f2 - (double)r.inv_f2);
         const double wf = 2.0 * r.Esrc / P.hbarc;
         r.wfac_hi = (float)wf;
         r.wfac_lo = (float)(wf - (double)r.wfac_hi);
@@ -272,7 +274,6 @@ void build_host_tables(const xrdt_problem *p, const DevProblem &P, const float *
         r.einf = (float)r.ein;
         r.Esrc1f = (float)r.Esrc1;
         r.Esrc2f = (float)r.Esrc2;
-        r.pad = 0.f;
     }
     // spectrum windows: detector bin n takes source bins win_lo[n] .. + W-1
     // with weights RF = spectrum[e + n*nrg_src]; win_n[e] = the detector bins

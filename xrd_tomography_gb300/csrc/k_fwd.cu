@@ -53,7 +53,7 @@ __host__ __device__ inline Layout fwd_layout(const DevProblem &P, int E, int SL,
     L.tn = o; o = align16(o + sizeof(double) * E);
     L.tns = o; o = align16(o + sizeof(float2) * kWarps * E);
     L.ck = o; o = align16(o + sizeof(float2) * kWarps * P.nrg_det);
-    L.en = o; o = align16(o + sizeof(float) * 9 * E);
+    L.en = o; o = align16(o + sizeof(float) * 11 * E);
     L.rf = o; o = align16(o + sizeof(float) * P.nrg_det * W);
     L.offse = o; o = align16(o + sizeof(float) * E * SL);
     L.winlo = o; o = align16(o + sizeof(int) * P.nrg_det);
@@ -107,6 +107,7 @@ k_fwd(const FwdArgs args)
     float *en_if1 = en, *en_if2 = en + E, *en_wh = en + 2 * E, *en_wl = en + 3 * E;
     float *en_c1 = en + 4 * E, *en_c2 = en + 5 * E, *en_ein = en + 6 * E, *en_e1 = en + 7 * E;
     float *en_wn0f = en + 8 * E;   // first detector bin of wn as a float
+    float *en_if1l = en + 9 * E, *en_if2l = en + 10 * E;   // low parts of 1/f1, 1/f2
     float *rf = (float *)(sm + L.rf);
     float *offse = (float *)(sm + L.offse);   // [E][SL] Esrc1(e) - Edet1(wn_lo(e) + s)
     int *winlo = (int *)(sm + L.winlo);
@@ -140,6 +141,8 @@ k_fwd(const FwdArgs args)
         const EnergyRow r = args.T.energy[P.e_lo + i];
         en_if1[i] = r.inv_f1;
         en_if2[i] = r.inv_f2;
+        en_if1l[i] = r.inv_f1_lo;
+        en_if2l[i] = r.inv_f2_lo;
         en_wh[i] = r.wfac_hi;
         en_wl[i] = r.wfac_lo;
         en_c1[i] = r.sig_c1;
@@ -230,9 +233,13 @@ k_fwd(const FwdArgs args)
 #pragma unroll 1
                 for (int el = pe0 + lane; el < pe1; el += 32) {
                     // ---- (voxel, source energy) term, :266-356 ----
+                    // attenuation exponents with 1/f1, 1/f2 as pairs: X reaches
+                    // tens at the lowest energies, where FP32 constants alone
+                    // would move exp(-X) by a few 1e-6
                     const float if1 = en_if1[el], if2 = en_if2[el];
-                    const float Xin = fmaf(Ad.x, if1, Ad.y * if2);
-                    const float Xout = fmaf(Asx, if1, Asy * if2);
+                    const float if1l = en_if1l[el], if2l = en_if2l[el];
+                    const float Xin = fmaf(Ad.x, if1, fmaf(Ad.y, if2, fmaf(Ad.x, if1l, Ad.y * if2l)));
+                    const float Xout = fmaf(Asx, if1, fmaf(Asy, if2, fmaf(Asx, if1l, Asy * if2l)));
                     const float wh0 = en_wh[el], wl0 = en_wl[el];
                     float w_hi = wh0 * sh;
                     float w_lo = fmaf(wh0, sh, -w_hi) + fmaf(wh0, sl, wl0 * sh);
@@ -244,7 +251,8 @@ k_fwd(const FwdArgs args)
                     const float sig2 = fmaf(en_c1[el], s2f, en_c2[el] * sg_s2);
                     const float rs = rsqrtf(sig2);
                     const float cexp = -0.5f * kLog2e * rs * rs;
-                    const float PP = ex2_approx(-(Xin + Xout) * kLog2e);
+                    const float Xio = Xin + Xout;
+                    const float PP = ex2_approx(-fmaf(Xio, kLog2e, Xio * kLog2e_lo));
                     nexp += 1;
                     const float pref = PP * Wg * rsqrt2pi * rs;
                     const float half = kSig * sig2 * rs;
@@ -320,11 +328,19 @@ k_fwd(const FwdArgs args)
                         if (n0 <= n1) {
                             const int nq = compton_bin(P, ein, eratio, inv_er, sh, oh, ol, args.T.energy[eg].ein,
                                                        qmin_t, inv_dqt);
+                            // Pc = exp(-(Xin + Xc)) with Xc the source-side exponent at
+                            // the outgoing energy eout = ein / eratio, formed as the
+                            // Rayleigh one plus the small Compton change, so that Pc
+                            // keeps the accuracy of PP:
+                            //   Asx (1/eout^3 - 1/ein^3) = Asx/ein^3 ((1 + x)^3 - 1)
+                            //   Asy (1/KN(eout) - 1/KN(ein))
+                            //     = Asy (ein - eout)(kn1 + kn2 (ein + eout)) / (KN(ein) KN(eout))
                             const float eout = ein * inv_er;
-                            const float f1 = eout * eout * eout;
-                            const float f2 = fmaf(kn2 * eout, eout, fmaf(kn1, eout, kn0));
-                            const float Xc = fmaf(Asx, rcp_approx(f1), Asy * rcp_approx(f2));
-                            const float Pc = ex2_approx(-(Xin + Xc) * kLog2e);
+                            const float f2o = fmaf(kn2 * eout, eout, fmaf(kn1, eout, kn0));
+                            const float cube = x * fmaf(x, x + 3.f, 3.f);            // (1 + x)^3 - 1
+                            const float dX = fmaf(Asx * if1, cube,
+                                                  Asy * (x * eout) * fmaf(kn2, ein + eout, kn1) * if2 * rcp_approx(f2o));
+                            const float Pc = PP * ex2_approx(-dX * kLog2e);
                             nexp += 1;
                             // an underflowed Pc adds exact zeros below: no branch
                             const float Cf = eratio * eratio * (eratio + inv_er - 1.f + cos2) * 0.5f;

@@ -135,22 +135,23 @@ __global__ void k_voxel_compton(DevProblem P, const float *__restrict__ a1, cons
     }
 }
 
-// One warp per (source, voxel): attenuator(Rsrc, Rvox) of integrate_diffraction.cu:260.
+// One lane per (source, voxel): attenuator(Rsrc, Rvox) of
+// integrate_diffraction.cu:260, set up in FP64 and walked cell by cell from
+// the voxel (walk_cells).  A warp takes 32 neighbouring voxels of one source.
 __global__ void k_src_atten(DevProblem P, const SrcGeom *__restrict__ sg, const int *__restrict__ vox_xy,
                             int nv, const float4 *__restrict__ cells, float2 *__restrict__ out)
 {
-    const int lane = threadIdx.x & 31;
     const int64_t nwork = (int64_t)P.n_src * nv;
-    const int64_t wstride = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t w = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); w < nwork; w += wstride) {
+    const unsigned ncell_m1 = (unsigned)((P.nx + 1) * (P.ny + 1) - 1);
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < nwork; w += stride) {
         const int src = (int)(w / nv), v = (int)(w % nv);
         const int xy = vox_xy[v];
         const double vx = ((double)(xy & 0xffff) + 0.5) * P.vox;
         const double vy = ((double)(xy >> 16) + 0.5) * P.vox;
         WalkSetup ws;
         walk_setup(P, sg[src].Rsrc_x, sg[src].Rsrc_y, vx, vy, &ws);
-        const float2 A = walk_coop(cells, P.nx, P.ny, ws, (float)P.DQ, lane);
-        if (lane == 0) out[(int64_t)src * nv + v] = A;
+        out[(int64_t)src * nv + v] = walk_cells(cells, 1, P.nx + 1, ncell_m1, ws, (float)vx, (float)vy, (float)P.DQ);
     }
 }
 
@@ -191,10 +192,14 @@ cudaError_t launch_src_atten(const DevProblem &P, const SrcGeom *d_src, int nv, 
                              cudaStream_t s, int64_t *launches)
 {
     if (nv == 0) return cudaSuccess;
-    const int64_t warps = (int64_t)P.n_src * nv;
-    int64_t blocks = (warps + 7) / 8;
-    if (blocks > 152 * 64) blocks = 152 * 64;
-    k_src_atten<<<(int)blocks, 256, 0, s>>>(P, d_src, B.vox_xy, nv, B.cells, B.atten_src);
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    const int64_t items = (int64_t)P.n_src * nv;
+    int64_t blocks = (items + 127) / 128;
+    if (blocks > (int64_t)sms * 16) blocks = (int64_t)sms * 16;
+    k_src_atten<<<(int)blocks, 128, 0, s>>>(P, d_src, B.vox_xy, nv, B.cells, B.atten_src);
     if (launches) (*launches)++;
     return cudaGetLastError();
 }

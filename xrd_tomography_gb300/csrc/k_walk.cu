@@ -92,14 +92,21 @@ k_det_walk(DevProblem P, F32Consts c, const SrcGeom *__restrict__ sg, const int2
             WalkSetup ws;
             ws.Lx = ws.Ly = 0.f;
             ws.n = 0;
-            if (valid && !walk_setup_f32(P, c, exf, eyf, vx, vy, &ws))
-                walk_setup_f64(P, ex, ey, (double)vx, (double)vy, &ws);
+            ws.dlt = ws.ux = ws.uy = ff{0.f, 0.f};
+            if (valid) {
+                // decided in FP32 (guard bands) or FP64; the anchor of an FP32
+                // decision comes from the endpoint as a float pair
+                if (walk_setup_f32(P, c, exf, eyf, vx, vy, &ws))
+                    walk_anchor_ff(c, ff_from_double(ex), ff_from_double(ey), vx, vy, &ws);
+                else
+                    walk_setup_f64(P, ex, ey, (double)vx, (double)vy, &ws);
+            }
             // rays mostly along x lie side by side along y: column-major copy
             const unsigned along_x = __ballot_sync(0xffffffffu, valid && fabsf(ws.Lx) > fabsf(ws.Ly));
             const unsigned any = __ballot_sync(0xffffffffu, valid);
             const bool colmajor = 2 * __popc(along_x) > __popc(any);
-            const float2 A = colmajor ? walk_cells(cells_t, P.ny + 1, 1, ncell_m1, ws, c.DQ)
-                                      : walk_cells(cells, 1, P.nx + 1, ncell_m1, ws, c.DQ);
+            const float2 A = colmajor ? walk_cells(cells_t, P.ny + 1, 1, ncell_m1, ws, vx, vy, c.DQ)
+                                      : walk_cells(cells, 1, P.nx + 1, ncell_m1, ws, vx, vy, c.DQ);
             if (valid) out[v] = A;
         }
     }
@@ -124,8 +131,12 @@ cudaError_t launch_det_walk(const DevProblem &P, const SrcGeom *sg, const int2 *
         n_groups = (long long)P.n_src * ((nd + kRays - 1) / kRays);
     }
     const long long nwork = n_groups * ((nv + kVoxPerStrip - 1) / kVoxPerStrip);
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
     long long blocks = (nwork + kWalkWarps - 1) / kWalkWarps;
-    if (blocks > 152LL * 64) blocks = 152LL * 64;
+    if (blocks > (long long)sms * 64) blocks = (long long)sms * 64;
     k_det_walk<<<(unsigned)blocks, kWalkThreads, 0, s>>>(P, make_f32_consts(P), sg, pairs, n_items, d0, nd, n_groups,
                                                           vox_xy, nv, cells, tab);
     if (launches) (*launches)++;

@@ -9,6 +9,7 @@
 #pragma once
 
 #include "xrdt_device.cuh"
+#include "ff.cuh"
 
 namespace xrdt {
 
@@ -18,6 +19,11 @@ struct WalkSetup {
     int n;          // number of samples: k = 0 .. n-1
     int edge;       // ROI edge entered (GetIntersection's order: bottom, right,
                     // top, left), -1 when the segment misses the ROI
+    // The same samples anchored at the voxel v, for walk_cells: sample k sits
+    // at v + (dlt + (n-1-k) DQ) u with u the unit vector from the voxel back
+    // to the entry point and dlt = Lr - (n-1) DQ the distance of the last
+    // sample from the voxel, both as float pairs.
+    ff dlt, ux, uy;
 };
 
 // GetIntersection + the sample count of attenuator.cu:19-52: every k in
@@ -47,6 +53,38 @@ __device__ inline void walk_setup(const DevProblem &P, double ex, double ey, dou
     w->Lx = (float)(Lx * P.DQ);
     w->Ly = (float)(Ly * P.DQ);
     w->n = (int)n;
+    if (n > 0) {
+        w->dlt = ff_from_double(Lr - P.DQ * (double)(n - 1));
+        w->ux = ff_from_double(-Lx);
+        w->uy = ff_from_double(-Ly);
+    } else {
+        w->dlt = w->ux = w->uy = ff{0.f, 0.f};
+    }
+}
+
+// The voxel-anchored form of a set-up whose edge and sample count are
+// decided (walk_setup_f32), from the endpoint (ex, ey) as float pairs: with
+// D = v - e, the entry point on edge x = X0 lies at Lr = |D| (vx - X0)/Dx
+// from the voxel (y = Y0: |D| (vy - Y0)/Dy), and u = -D/|D|.
+__device__ __forceinline__ void walk_anchor_ff(const F32Consts &C, ff ex, ff ey, float vx, float vy, WalkSetup *w)
+{
+    if (w->n <= 0) {
+        w->dlt = w->ux = w->uy = ff{0.f, 0.f};
+        return;
+    }
+    const ff Dx = ff_fsub(vx, ex), Dy = ff_fsub(vy, ey);
+    const ff D = ff_sqrt(ff_add(ff_sqr(Dx), ff_sqr(Dy)));
+    ff ratio;
+    switch (w->edge) {
+    case 0: ratio = ff_div(ff{vy, 0.f}, Dy); break;              // y = 0
+    case 1: ratio = ff_div(ff{vx - C.nxf, 0.f}, Dx); break;      // x = NX
+    case 2: ratio = ff_div(ff{vy - C.nyf, 0.f}, Dy); break;      // y = NY
+    default: ratio = ff_div(ff{vx, 0.f}, Dx); break;             // x = 0
+    }
+    const ff Lr = ff_mul(D, ratio);
+    w->dlt = ff_sub(Lr, ff_mulf(ff{(float)(w->n - 1), 0.f}, C.DQ));
+    w->ux = ff_neg(ff_div(Dx, D));
+    w->uy = ff_neg(ff_div(Dy, D));
 }
 
 // FP32 version of walk_setup for the endpoint (ex, ey) rounded to float.
@@ -191,13 +229,12 @@ __device__ __forceinline__ void ld_cell256(const float4 *p, float4 &c0, float4 &
 }
 
 __device__ __forceinline__ float2 walk_cells(const float4 *__restrict__ cells, int sx, int sy, unsigned ncell_m1,
-                                             const WalkSetup &w, float DQ)
+                                             const WalkSetup &w, float vx, float vy, float DQ)
 {
     const float magic = 12582912.f;
     const float nf = (float)w.n;
-    // reversed ray: sample j at R + (n-1-j) L
-    const float2 L = make_float2(-w.Lx, -w.Ly);
-    const float2 R = __ffma2_rn(make_float2(w.Lx, w.Ly), make_float2(nf - 1.f, nf - 1.f), make_float2(w.rx, w.ry));
+    // samples from the voxel outwards: sample j at v + (dlt + j DQ) u
+    const float2 L = make_float2(w.ux.hi * DQ, w.uy.hi * DQ);
     // minus the inverse steps, clamped so that a run is never overestimated
     const float ilx = fabsf(L.x) > 1e-4f ? -1.f / L.x : (L.x < 0.f ? 1e4f : -1e4f);
     const float ily = fabsf(L.y) > 1e-4f ? -1.f / L.y : (L.y < 0.f ? 1e4f : -1e4f);
@@ -207,14 +244,34 @@ __device__ __forceinline__ float2 walk_cells(const float4 *__restrict__ cells, i
     const float lxly = L.x * L.y;
     float2 acc = make_float2(0.f, 0.f), comp = make_float2(0.f, 0.f);
     for (float k0 = 0.f; k0 < nf;) {
-        const float2 P0 = __ffma2_rn(L, make_float2(k0, k0), R);
-        const float2 t = __fadd2_rn(P0, make_float2(magic, magic));
+        // distance s = dlt + k0 DQ and displacement t = s u as float pairs
+        // (exact products through the FMA): the sample's offset from its cell
+        // centre is then good to about 1e-7 voxel, where a position formed
+        // at a magnitude of hundreds of voxels in FP32 would be off by 1e-5
+        // and shift the interpolant by as much at material edges
+        // (explicitly rounded operations: a contracted multiply-add would
+        // count a product's error twice)
+        const float kq = __fmul_rn(k0, DQ);
+        const float kqe = fmaf(k0, DQ, -kq);
+        const float sh = __fadd_rn(w.dlt.hi, kq);
+        const float bb = __fsub_rn(sh, w.dlt.hi);
+        const float sl = __fadd_rn(__fadd_rn(__fsub_rn(w.dlt.hi, __fsub_rn(sh, bb)), __fsub_rn(kq, bb)),
+                                   __fadd_rn(kqe, w.dlt.lo));
+        const float px = __fmul_rn(sh, w.ux.hi), py = __fmul_rn(sh, w.uy.hi);
+        const float ex = __fadd_rn(fmaf(sh, w.ux.hi, -px), fmaf(sh, w.ux.lo, __fmul_rn(sl, w.ux.hi)));
+        const float ey = __fadd_rn(fmaf(sh, w.uy.hi, -py), fmaf(sh, w.uy.lo, __fmul_rn(sl, w.uy.hi)));
+        // the cell whose centre is nearest (any cell holding the point gives
+        // the same value: the interpolant is continuous), then the offset
+        const float2 t = make_float2(__fadd_rn(__fadd_rn(vx, px), magic), __fadd_rn(__fadd_rn(vy, py), magic));
         const int ix = __float_as_int(t.x) - 0x4B400000, iy = __float_as_int(t.y) - 0x4B400000;
-        const unsigned c = min((unsigned)((ix + 1) * sx + (iy + 1) * sy), ncell_m1);
+        const unsigned c = min((unsigned)(ix * sx + iy * sy), ncell_m1);
         float4 c0, c1;
         ld_cell256(cells + 2 * c, c0, c1);
-        const float2 r = __fadd2_rn(t, make_float2(-magic, -magic));
-        const float2 d = __fadd2_rn(P0, make_float2(-r.x, -r.y));                // (u0, v0), exact
+        // the cell centre (exact) minus the anchor is exact, and it cancels
+        // px but for the offset (Sterbenz), so only ex and ey round
+        const float2 r = make_float2(__fsub_rn(t.x, magic), __fsub_rn(t.y, magic));
+        const float2 d = make_float2(__fadd_rn(__fadd_rn(__fsub_rn(vx, r.x), px), ex),
+                                     __fadd_rn(__fadd_rn(__fsub_rn(vy, r.y), py), ey));
         const float2 s = __ffma2_rn(d, ninv, hinv);                                // steps to each exit edge
         // ceil(s) as round(s + 1/2) through the float mantissa (either way at a tie)
         float m = __fadd_rn(__fadd_rn(__fadd_rn(fminf(s.x, s.y), 0.5f), magic), -magic);

@@ -60,7 +60,7 @@ struct EnergyRow {
     float sig_c1, sig_c2;       // sigma^2 = c1*s^2 + c2*sg/s^2
     float einf, Esrc1f, Esrc2f;
     float sig_c1_lo, sig_c2_lo; // low parts of c1, c2 as float pairs
-    float pad;
+    float inv_f1_lo, inv_f2_lo; // low parts of 1/ein^3, 1/KN(ein)
 };
 
 std::string fmt(const char *f, ...);
