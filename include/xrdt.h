@@ -43,7 +43,8 @@ typedef enum xrdt_status {
     XRDT_ERR_CUDA = 5,        /* a CUDA runtime call failed                    */
     XRDT_ERR_ALLOC = 6,       /* device or pinned allocation failed            */
     XRDT_ERR_UNSUPPORTED = 7, /* a flag combination that is not implemented    */
-    XRDT_ERR_TIMEOUT = 8      /* a bounded device wait gave up                 */
+    XRDT_ERR_TIMEOUT = 8,     /* a bounded device wait gave up                 */
+    XRDT_ERR_IO = 9           /* a file could not be written or read           */
 } xrdt_status;
 
 /* Bits of xrdt_problem.quirks: behaviours of the reference kernel that are
@@ -285,6 +286,18 @@ int32_t xrdt_ct_sinogram(xrdt_ctx *ctx, const xrdt_problem *p, const float *spec
 int32_t xrdt_mlem_matrix(xrdt_ctx *ctx, const float *A, int64_t rays, int32_t K,
                          const float *y, const float *c, float *x, int32_t iters,
                          uint32_t flags);
+
+/* ---- MLEM checkpoints ------------------------------------------------
+ * The state of an MLEM run is its estimate and the number of iterations done
+ * (the reference keeps both in MATLAB memory only, main.m:154-176).  write
+ * stores x [n] (host or device memory) and iteration in a file at path,
+ * replacing it only once the new file is complete; read checks the file's
+ * header, element count and checksum (XRDT_ERR_INPUT when the file is not a
+ * checkpoint of n elements or is damaged) and fills x (host or device) and
+ * *iteration.  An MLEM continued from a checkpoint gives the same estimate as
+ * the run that was not interrupted.  XRDT_ERR_IO when the file system fails. */
+int32_t xrdt_mlem_checkpoint_write(const char *path, const float *x, int64_t n, int64_t iteration);
+int32_t xrdt_mlem_checkpoint_read(const char *path, float *x, int64_t n, int64_t *iteration);
 
 /* ---- per-voxel-coefficient operator: forward, adjoint, MLEM -----------
  * The reference's unknowns are per material: Amatrix[k, m, ray] sums the

@@ -75,6 +75,9 @@ SIGNATURES = {
     "xrdt_batch_tune": (ctypes.c_int32, [_vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int64),
                                          ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
     "xrdt_op_adjoint_rays": (ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_int64, _vp, ctypes.c_uint32]),
+    "xrdt_mlem_checkpoint_write": (ctypes.c_int32, [ctypes.c_char_p, _vp, ctypes.c_int64, ctypes.c_int64]),
+    "xrdt_mlem_checkpoint_read": (ctypes.c_int32, [ctypes.c_char_p, _vp, ctypes.c_int64,
+                                                   ctypes.POINTER(ctypes.c_int64)]),
     "xrdt_debug_decisions": (ctypes.c_int32, [_vp, _P, _vp, _vp, _vp, _vp, _vp, ctypes.c_float, ctypes.c_float,
                                               ctypes.c_float, ctypes.c_float, _vp, ctypes.c_int64, _vp, _vp, _vp,
                                               _vp, _vp, ctypes.POINTER(ctypes.c_int64)]),
@@ -350,6 +353,27 @@ def mlem_matrix(A, y, c, x0, iters: int, K: int | None = None, ctx: Context | No
     rays = int(ky.numel() if hasattr(ky, "numel") else ky.size)
     _check(lib().xrdt_mlem_matrix(ctx.h, pa, rays, K, py, pc, px, iters, 0), ctx.h)
     return x
+
+
+def mlem_checkpoint_write(path: str, x, iteration: int) -> None:
+    """xrdt_mlem_checkpoint_write: the estimate x (numpy or CUDA tensor) and
+    the number of iterations done, to a file."""
+    px, kx = _ptr(x, np.float32)
+    n = int(kx.numel() if hasattr(kx, "numel") else kx.size)
+    _check(lib().xrdt_mlem_checkpoint_write(os.fsencode(path), px, n, int(iteration)))
+
+
+def mlem_checkpoint_read(path: str, x):
+    """xrdt_mlem_checkpoint_read into x (a float32 numpy array or CUDA
+    tensor of the checkpoint's size, filled in place); returns (x, iteration)."""
+    if not hasattr(x, "data_ptr"):
+        if not (isinstance(x, np.ndarray) and x.dtype == np.float32 and x.flags.c_contiguous):
+            raise ValueError("x must be a contiguous float32 array or tensor")
+    px, kx = _ptr(x, np.float32)
+    n = int(kx.numel() if hasattr(kx, "numel") else kx.size)
+    it = ctypes.c_int64()
+    _check(lib().xrdt_mlem_checkpoint_read(os.fsencode(path), px, n, ctypes.byref(it)))
+    return x, it.value
 
 
 def mlem_matrix_noalloc(A, y, c, x, iters: int, stream: int | None = None):

@@ -88,6 +88,7 @@ int get_buf(xrdt_ctx *ctx, int slot, size_t bytes, void **out)
             ctx->cap[slot] = 0;
         }
         void *p = nullptr;
+        if (test_alloc_fails()) return fail(ctx, XRDT_ERR_ALLOC, fmt("cudaMalloc(%zu bytes): failure injected", bytes));
         cudaError_t e = cudaMalloc(&p, bytes);
         if (e != cudaSuccess) {
             cudaGetLastError();
@@ -347,6 +348,7 @@ const char *xrdt_status_string(int32_t s)
     case XRDT_ERR_ALLOC: return "allocation failed";
     case XRDT_ERR_UNSUPPORTED: return "unsupported option";
     case XRDT_ERR_TIMEOUT: return "device wait timed out";
+    case XRDT_ERR_IO: return "file could not be written or read";
     default: return "unknown status";
     }
 }

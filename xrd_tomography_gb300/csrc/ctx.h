@@ -1,6 +1,7 @@
 // ctx.h -- the library context (xrdt_ctx) shared by the C ABI's source files.
 #pragma once
 
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -34,6 +35,16 @@ struct xrdt_ctx {
 };
 
 namespace xrdt {
+
+// Failure injection on the host: while the environment variable
+// XRDT_TEST_FAIL_ALLOC is "1", every device allocation the library makes
+// reports failure, as on a device that is full, so that callers can check
+// that XRDT_ERR_ALLOC comes back and that the context stays usable.
+inline bool test_alloc_fails()
+{
+    const char *e = getenv("XRDT_TEST_FAIL_ALLOC");
+    return e && e[0] == '1';
+}
 
 // Brackets one kernel group with events when profiling is on.
 struct ProfScope {

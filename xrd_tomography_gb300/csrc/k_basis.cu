@@ -20,6 +20,7 @@
 //
 // The wait on the mbarrier is bounded: on time-out the kernel raises an error
 // flag, skips the read-back and still frees its tensor memory.
+#include <cstdlib>
 #include "xrdt_device.cuh"
 
 namespace xrdt {
@@ -70,14 +71,15 @@ __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N)
 
 __global__ void __launch_bounds__(kBasisThreads)
 k_basis_expand(const float *__restrict__ C, long long M, int K, const float *__restrict__ B, int N,
-               float *__restrict__ I, unsigned *__restrict__ err)
+               float *__restrict__ I, unsigned *__restrict__ err, int test_timeout)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
     const int a_bytes = kTileM * K * 4, b_bytes = N * K * 4;
     unsigned char *a_hi = sm, *a_lo = sm + a_bytes;
     unsigned char *b_hi = sm + 2 * a_bytes, *b_lo = b_hi + b_bytes;
     uint64_t *mbar = reinterpret_cast<uint64_t *>(b_lo + b_bytes);
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 1);
+    uint64_t *idle = mbar + 1;   // a barrier nothing arrives at (the time-out test)
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 2);
     const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
     const long long m0 = (long long)blockIdx.x * kTileM;
 
@@ -90,6 +92,7 @@ k_basis_expand(const float *__restrict__ C, long long M, int K, const float *__r
     }
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(idle)));
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
     // the CTA's rows of C and the basis, split into TF32 pairs
@@ -137,20 +140,34 @@ k_basis_expand(const float *__restrict__ C, long long M, int K, const float *__r
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
             smem_u32(mbar)));
     }
-    // wait for the accumulator (bounded)
+    // wait for the accumulator (bounded).  The time-out test waits on the
+    // barrier nothing signals instead, with a short limit, so the give-up
+    // path below runs for real.
+    const uint32_t wait_bar = smem_u32(test_timeout ? idle : mbar);
+    const unsigned limit = test_timeout ? 1024u : kSpinLimit;
     uint32_t done = 0;
     for (unsigned it = 0; !done; it++) {
         asm volatile(
             "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
             "selp.u32 %0, 1, 0, p;\n\t}\n"
             : "=r"(done)
-            : "r"(smem_u32(mbar)), "r"(0u));
-        if (!done && it >= kSpinLimit) break;
+            : "r"(wait_bar), "r"(0u));
+        if (!done && it >= limit) break;
     }
     done = __all_sync(0xffffffffu, done);   // tcgen05.ld below needs the whole warp
     asm volatile("tcgen05.fence::after_thread_sync;");
     if (!done) {
         if (lane == 0) atomicOr(err, 1u);
+        // before the tensor memory is freed, let the block's own MMAs finish
+        // (again bounded): they still write the accumulator
+        uint32_t drained = 0;
+        for (unsigned it = 0; !drained && it < kSpinLimit; it++)
+            asm volatile(
+                "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                "selp.u32 %0, 1, 0, p;\n\t}\n"
+                : "=r"(drained)
+                : "r"(smem_u32(mbar)), "r"(0u));
+        if (!drained && lane == 0) atomicOr(err, 2u);
     } else {
         // warp w holds accumulator lanes 32w .. 32w+31 = rows of the tile
         const long long row = m0 + wid * 32 + lane;
@@ -175,7 +192,7 @@ k_basis_expand(const float *__restrict__ C, long long M, int K, const float *__r
 
 } // namespace
 
-size_t basis_smem(int K, int N) { return 2 * (size_t)kTileM * K * 4 + 2 * (size_t)N * K * 4 + 16; }
+size_t basis_smem(int K, int N) { return 2 * (size_t)kTileM * K * 4 + 2 * (size_t)N * K * 4 + 24; }
 
 cudaError_t launch_basis_expand(const float *C, long long M, int K, const float *B, int N, float *I, unsigned *err,
                                 cudaStream_t s, int64_t *launches)
@@ -184,7 +201,11 @@ cudaError_t launch_basis_expand(const float *C, long long M, int K, const float 
     cudaError_t e = cudaFuncSetAttribute(k_basis_expand, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const long long tiles = (M + kTileM - 1) / kTileM;
-    k_basis_expand<<<(unsigned)tiles, kBasisThreads, smem, s>>>(C, M, K, B, N, I, err);
+    // XRDT_TEST_BASIS_TIMEOUT=1 makes every block's accumulator wait run out
+    // (test of the time-out path: error flag, drain, tensor memory freed)
+    const char *tt = getenv("XRDT_TEST_BASIS_TIMEOUT");
+    const int test_timeout = (tt && tt[0] == '1') ? 1 : 0;
+    k_basis_expand<<<(unsigned)tiles, kBasisThreads, smem, s>>>(C, M, K, B, N, I, err, test_timeout);
     if (launches) (*launches)++;
     return cudaGetLastError();
 }

@@ -108,6 +108,8 @@ int fail(xrdt_ctx *c, int status, const std::string &msg)
 int op_alloc(xrdt_op *op, size_t bytes, void **out)
 {
     void *p = nullptr;
+    if (test_alloc_fails())
+        return fail(op->ctx, XRDT_ERR_ALLOC, fmt("cudaMalloc(%zu bytes): failure injected", bytes));
     cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -417,7 +419,8 @@ int plan_make_tiles(Plan *pl)
             most = std::max(most, used);
         }
     }
-    cudaError_t e = cudaMalloc((void **)&pl->walkbuf, sizeof(float2) * (size_t)std::max<int64_t>(most, 1));
+    cudaError_t e = test_alloc_fails() ? cudaErrorMemoryAllocation
+                                       : cudaMalloc((void **)&pl->walkbuf, sizeof(float2) * (size_t)std::max<int64_t>(most, 1));
     for (Plan::Tile &t : pl->tiles) {
         const size_t ns = std::max<size_t>(t.segs.size(), 1);
         if (e == cudaSuccess) e = cudaMallocHost((void **)&t.jobs_h, sizeof(VoxJob) * ns);
@@ -437,7 +440,8 @@ int plan_create(xrdt_ctx *ctx, xrdt_op *const *ops, int n, Plan **out)
     Plan *pl = new Plan();
     pl->ctx = ctx;
     pl->ops.assign(ops, ops + n);
-    cudaError_t e = cudaMallocHost((void **)&pl->jobs_h, sizeof(VoxJob) * n);
+    cudaError_t e = test_alloc_fails() ? cudaErrorMemoryAllocation
+                                       : cudaMallocHost((void **)&pl->jobs_h, sizeof(VoxJob) * n);
     if (e == cudaSuccess) e = cudaMalloc((void **)&pl->jobs_d, sizeof(VoxJob) * n);
     if (e == cudaSuccess) e = cudaMalloc((void **)&pl->off_d, sizeof(int64_t) * 5 * (n + 1));
     if (e == cudaSuccess) e = cudaMalloc((void **)&pl->counters_d, sizeof(unsigned long long) * 2);
