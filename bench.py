@@ -48,7 +48,7 @@ FLUSH_BYTES = 256 << 20
 # ncu capture of a single launch on the 128x128 workload (4096 pairs x 5009
 # voxels); the traffic is the launch's walk table plus a fixed part, so the
 # 256x256 figure below is that rate times the pair-voxels of its mean launch
-K_FWD_DRAM_BYTES_PER_PAIR_VOXEL = None
+K_FWD_DRAM_BYTES_PER_PAIR_VOXEL = (166599424 + 3529728) / (4096 * 5009)   # 8.29 B (read + write)
 # issue slots busy in k_fwd (ncu SpeedOfLight, 128x128 workload): the kernel
 # is bound by instruction issue, not by the SFU rate of the roofline below
 K_FWD_ISSUE_BUSY = 0.8338
@@ -66,8 +66,12 @@ def parse():
                     help="synthetic configuration (1 is the benchmark; 0 and 2 are small profiling cases; "
                          "3 runs batched MLEM on the 64 phantoms of the batched configuration at their stated "
                          "sizes, several minutes per iteration)")
-    ap.add_argument("--batch", type=int, default=64, help="--workload 3: number of phantoms")
-    ap.add_argument("--iters", type=int, default=1, help="--workload 3: timed MLEM iterations")
+    ap.add_argument("--batch", type=int, default=None,
+                    help="--workload 3: number of phantoms (64); --workload 4 --mlem: number of slices (16)")
+    ap.add_argument("--iters", type=int, default=1, help="--workload 3, --workload 4 --mlem: timed MLEM iterations")
+    ap.add_argument("--mlem", action="store_true",
+                    help="--workload 4: per-voxel MLEM on slices of the 384x384 stack instead of the forward "
+                         "projection")
     return ap.parse_args()
 
 
@@ -459,7 +463,8 @@ def batch_mlem_bench(xt, synth, ctx, stream, dev, n=8, iters=10):
 
 def run_batched_stated(args):
     """--workload 3: batched per-voxel MLEM on the batched configuration at its
-    stated sizes -- args.batch phantoms (64) with sides uniform in 64-384
+    stated sizes (--workload 4 --mlem: on slices of the 384x384 stack instead)
+    -- args.batch phantoms (64) with sides uniform in 64-384
     voxels, 60-360 views, 128-768 px, 64 energy bins, 32 coefficients per
     voxel -- as one xrdt_batch: every operator streams its detector-side
     table in tiles inside each iteration, one CUDA graph per iteration.  One
@@ -480,7 +485,18 @@ def run_batched_stated(args):
     torch.cuda.set_stream(stream)
     ctx = xt.Context(local, stream=stream.cuda_stream)
     t_setup = time.perf_counter()
-    inps = synth.batch_inputs(args.batch)
+    if args.workload == 4:
+        # slices of the scanner stack: 384x384 at 1.5 mm, 12 materials, 720
+        # views, 1024 px x 96 energy bins, each slice its own seeded phantom
+        n = args.batch or 16
+        inps = [synth.make_inputs(synth.config_problem(4), synth.SEED_BASE + 4 + 1000 * k) for k in range(n)]
+        what = (f"{n} slice(s) of the 384x384 stack (1.5 mm, 12 materials, 720 views, 1024 px x 96 energy "
+                f"bins), {inps[0].problem.nwt} coefficients per voxel")
+    else:
+        n = args.batch or 64
+        inps = synth.batch_inputs(n)
+        what = (f"{n} phantoms of the batched configuration at its stated sizes (sides 64-384, 60-360 views, "
+                f"128-768 px), 64 energy bins, {inps[0].problem.nwt} coefficients per voxel")
     ops = [xt.Operator(i.problem, i.spectrum, i.seg, i.a1, i.a2, ctx=ctx) for i in inps]
     gen = torch.Generator(device=dev).manual_seed(23)
     ys, cs, xs = [], [], []
@@ -533,10 +549,7 @@ def run_batched_stated(args):
             "value": 1e3 / ms_iter, "unit": "iter/s", "n_gpus": ws, "steps": args.iters, "warmup": 1,
             "ms_per_step": ms_iter, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 (FP64 geometry decisions and global sums)", "data": "synthetic (seeded)",
-            "config": {"workload": f"{args.batch} phantoms of the batched configuration at its stated sizes "
-                                   f"(sides 64-384, 60-360 views, 128-768 px), 64 energy bins, "
-                                   f"{inps[0].problem.nwt} coefficients per voxel, one xrdt_batch, detector-side "
-                                   f"tables streamed in tiles",
+            "config": {"workload": f"{what}, one xrdt_batch, detector-side tables streamed in tiles",
                        "pair_voxels_per_iter": int(sum(pv)), "rays": int(sum(i.problem.rays for i in inps)),
                        "sizes": [f"{i.problem.nx}^2/{i.problem.n_src}v/{i.problem.n_col}px" for i in inps]},
             "g_pair_voxels_per_s": sum(pv) / (ms_iter * 1e-3) / 1e9,
@@ -711,7 +724,7 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
-    elif args.workload == 3:
+    elif args.workload == 3 or (args.workload == 4 and args.mlem):
         run_batched_stated(args)
     else:
         run_ours(args)

@@ -354,6 +354,27 @@ int32_t xrdt_op_forward_rays(xrdt_op *op, const float *x, const int64_t *rays,
 int32_t xrdt_op_adjoint_rays(xrdt_op *op, const float *w, const int64_t *rays,
                              int64_t n_rays, float *g, uint32_t flags);
 
+/* ---- the per-voxel operator with a dense q basis -----------------------
+ * The reference's coarse q "basis" is point-sampled: bin k of the model row
+ * is the Gaussian at the bin centre times its width (wvt_value.cu:8-22,
+ * integrate_diffraction.cu:311-315).  With a dense basis B [J][NWT]
+ * (row-major, non-negative) the unknowns of a voxel are J coefficients c and
+ * its coarse pattern is x[k] = sum_j c[j] B[j][k]: forward(c) = Av (c B),
+ * adjoint(w) = (Av^T w) B^T, and MLEM (main.m:162-176) runs on the
+ * coefficients.  The expansion and the contraction are GEMMs on the tensor
+ * cores (tcgen05, 3xTF32, FP32 accumulation; xrdt_basis_expand).  c and g
+ * are [NX*NY*J], voxel index ix + NX*iy, coefficient fastest (0 at empty
+ * voxels); y, w, y_meas and c_bg as for the operator.  J and NWT multiples
+ * of 16 in [16, 64].  The basis operator uses its operator's buffers: the
+ * two take part in one call at a time, and the operator must outlive it. */
+typedef struct xrdt_bop xrdt_bop;
+int32_t xrdt_bop_create(xrdt_op *op, const float *B, int32_t J, xrdt_bop **bop);
+int32_t xrdt_bop_destroy(xrdt_bop *bop);
+int32_t xrdt_bop_forward(xrdt_bop *bop, const float *c, float *y, uint32_t flags);
+int32_t xrdt_bop_adjoint(xrdt_bop *bop, const float *w, float *g, uint32_t flags);
+int32_t xrdt_bop_mlem(xrdt_bop *bop, const float *y_meas, const float *c_bg, float *c, int32_t iters,
+                      uint32_t flags);
+
 /* ---- batches: many operators in one launch per kernel ------------------
  * A batch runs the forward, the adjoint and MLEM of several operators
  * (phantoms and scanners of any sizes) together: the forward and the adjoint

@@ -75,6 +75,11 @@ SIGNATURES = {
     "xrdt_batch_tune": (ctypes.c_int32, [_vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int64),
                                          ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
     "xrdt_op_adjoint_rays": (ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_int64, _vp, ctypes.c_uint32]),
+    "xrdt_bop_create": (ctypes.c_int32, [_vp, _vp, ctypes.c_int32, ctypes.POINTER(_vp)]),
+    "xrdt_bop_destroy": (ctypes.c_int32, [_vp]),
+    "xrdt_bop_forward": (ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_uint32]),
+    "xrdt_bop_adjoint": (ctypes.c_int32, [_vp, _vp, _vp, ctypes.c_uint32]),
+    "xrdt_bop_mlem": (ctypes.c_int32, [_vp, _vp, _vp, _vp, ctypes.c_int32, ctypes.c_uint32]),
     "xrdt_mlem_checkpoint_write": (ctypes.c_int32, [ctypes.c_char_p, _vp, ctypes.c_int64, ctypes.c_int64]),
     "xrdt_mlem_checkpoint_read": (ctypes.c_int32, [ctypes.c_char_p, _vp, ctypes.c_int64,
                                                    ctypes.POINTER(ctypes.c_int64)]),
@@ -487,6 +492,66 @@ class Operator:
             x = np.array(x0, dtype=np.float32, copy=True).reshape(-1)
             px = x.ctypes.data
         _check(lib().xrdt_op_mlem(self.h, py, pc, px, iters, 0), self.ctx.h)
+        return x
+
+
+class BasisOperator:
+    """xrdt_bop: an Operator whose voxels carry J coefficients of a dense q
+    basis B [J, NWT] (non-negative): forward(c) = Av (c B), adjoint(w) =
+    (Av^T w) B^T, MLEM on the coefficients; the expansion and contraction
+    run on the tensor cores.  Coefficient arrays have NX*NY*J entries."""
+
+    def __init__(self, op: "Operator", B):
+        self.op = op
+        self.ctx = op.ctx
+        pb, kb = _ptr(B, np.float32)
+        self.J = int(kb.shape[0])
+        h = _vp()
+        _check(lib().xrdt_bop_create(op.h, pb, self.J, ctypes.byref(h)), self.ctx.h)
+        self.h = h
+        self.ctx._operators.add(self)
+
+    @property
+    def unknowns(self) -> int:
+        return self.op.p.nx * self.op.p.ny * self.J
+
+    def close(self):
+        if getattr(self, "h", None) and self.ctx.h:
+            lib().xrdt_bop_destroy(self.h)
+        self.h = None
+
+    def __del__(self):  # pragma: no cover - interpreter shutdown order
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def forward(self, c, y=None):
+        pc, kc = _ptr(c, np.float32)
+        if y is None:
+            y = np.empty(self.op.p.rays, np.float32)
+        py, ky = _ptr(y, np.float32)
+        _check(lib().xrdt_bop_forward(self.h, pc, py, 0), self.ctx.h)
+        return ky
+
+    def adjoint(self, w, g=None):
+        pw, kw = _ptr(w, np.float32)
+        if g is None:
+            g = np.empty(self.unknowns, np.float32)
+        pg, kg = _ptr(g, np.float32)
+        _check(lib().xrdt_bop_adjoint(self.h, pw, pg, 0), self.ctx.h)
+        return kg
+
+    def mlem(self, y, c, x0, iters: int):
+        py, ky = _ptr(y, np.float32)
+        pc, kc = _ptr(c, np.float32)
+        if hasattr(x0, "data_ptr"):
+            x = x0
+            px = x.data_ptr()
+        else:
+            x = np.array(x0, dtype=np.float32, copy=True).reshape(-1)
+            px = x.ctypes.data
+        _check(lib().xrdt_bop_mlem(self.h, py, pc, px, iters, 0), self.ctx.h)
         return x
 
 

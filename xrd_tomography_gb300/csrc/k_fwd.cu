@@ -59,7 +59,7 @@ __host__ __device__ inline Layout fwd_layout(const DevProblem &P, int E, int SL,
     L.winlo = o; o = align16(o + sizeof(int) * P.nrg_det);
     L.wn = o; o = align16(o + sizeof(int) * 2 * E);
     L.cs = o; o = align16(o + sizeof(float) * kWarps * E * SL);
-    L.ifine = o; if (with_n) o = align16(o + sizeof(float) * P.n_mat * (P.nqf + 1));
+    L.ifine = o; if (with_n) o = align16(o + sizeof(float) * P.n_mat * (P.nqf + 3));
     L.fq = o; if (with_n) o = align16(o + sizeof(float2) * P.nqf);
     L.cq = o; if (with_a) o = align16(o + sizeof(float4) * P.nwt);
     L.s2 = o; o = align16(o + sizeof(float) * (size_t)P.nq * P.na);
@@ -161,9 +161,9 @@ k_fwd(const FwdArgs args)
     for (int i = tid; i < P.nrg_det; i += kThreads) winlo[i] = args.T.win_lo[i];
     for (int i = tid; i < kWarps * P.nrg_det; i += kThreads) Ck[i] = make_float2(0.f, 0.f);
     if (WITH_N) {
-        // rows of nqf + 1: each material's pattern and a zero pad
-        for (int i = tid; i < P.n_mat * (P.nqf + 1); i += kThreads) {
-            const int mm = i / (P.nqf + 1), j = i - mm * (P.nqf + 1);
+        // rows of nqf + 3: each material's pattern and three zero pads
+        for (int i = tid; i < P.n_mat * (P.nqf + 3); i += kThreads) {
+            const int mm = i / (P.nqf + 3), j = i - mm * (P.nqf + 3);
             Is[i] = j < P.nqf ? __ldg(args.Ifine + mm * P.nqf + j) : 0.f;
         }
         for (int i = tid; i < P.nqf; i += kThreads) fq[i] = args.T.fine_q[i];
@@ -265,26 +265,41 @@ k_fwd(const FwdArgs args)
                         float acc = 0.f;
                         // pref == 0: the attenuation factor underflowed, every term is 0
                         if (jlo <= jhi && pref != 0.f) {
-                            // an even number of bins, so the pair loop has no tail: an
-                            // odd window takes one more bin (an exact term of the full
-                            // sum, or the zero pad after the last bin).  A tail would make
-                            // the compiler rebuild the float counter from the trip count
-                            // through an int-to-float conversion, which this GPU issues
-                            // on its FP64 pipe.
-                            jhi += (jhi - jlo + 1) & 1;
+                            // a multiple of four bins, so the loop has no tail: the
+                            // extra bins are exact terms of the full sum or the zero
+                            // pads after the last bin.  (A tail would make the
+                            // compiler rebuild the float counter from the trip count
+                            // through an int-to-float conversion, which this GPU
+                            // issues on its FP64 pipe.)
+                            jhi += (4 - ((jhi - jlo + 1) & 3)) & 3;
                             nexp += (unsigned)(jhi - jlo + 1);
+                            // The exponent c (w - q_j)^2 as a quadratic in u = j - jc
+                            // about the bin jc nearest the centre: with
+                            // delta = w - q_jc (|delta| <= dq/2),
+                            //   c (delta - u dq)^2 = A + B u + C u^2,
+                            // A = c delta^2, B = -2 c delta dq, C = c dq^2 (dq^2
+                            // with the grid step's low part).  Near the
+                            // peak the sum is A alone; far out C u^2 dominates, so
+                            // the exponent keeps the relative accuracy of the direct
+                            // form in two FMAs per bin.
                             const float2 q0 = fq[jlo];
                             const float d0 = (w_hi - q0.x) + (w_lo - q0.y);
-                            const float *Ir = Is + m * (P.nqf + 1) + jlo;
+                            const float tc = rintf(d0 * inv_dqf);
+                            const float delta = fmaf(-tc, dqf_lo, fmaf(-tc, dqf_hi, d0));
+                            const float cd = cexp * delta;
+                            const float Aq = cd * delta;
+                            const float Bq = -2.f * cd * dqf_hi;
+                            const float Cq = cexp * fmaf(dqf_hi, dqf_hi, 2.f * dqf_hi * dqf_lo);
+                            const float *Ir = Is + m * (P.nqf + 3) + jlo;
                             const float *Iend = Ir + (jhi - jlo + 1);
                             float acc2 = 0.f;
-                            float t0 = 0.f;   // bin offset as a float: no conversion in the loop
-                            for (; Ir < Iend; Ir += 2, t0 += 2.f) {
-                                const float t1 = t0 + 1.f;
-                                const float da = fmaf(-t0, dqf_lo, fmaf(-t0, dqf_hi, d0));
-                                const float db = fmaf(-t1, dqf_lo, fmaf(-t1, dqf_hi, d0));
-                                acc = fmaf(ex2_approx(cexp * da * da), Ir[0], acc);
-                                acc2 = fmaf(ex2_approx(cexp * db * db), Ir[1], acc2);
+                            float u = -tc;   // bin offset from jc as a float: no conversion in the loop
+                            for (; Ir < Iend; Ir += 4, u += 4.f) {
+                                const float u1 = u + 1.f, u2 = u + 2.f, u3 = u + 3.f;
+                                acc = fmaf(ex2_approx(fmaf(fmaf(Cq, u, Bq), u, Aq)), Ir[0], acc);
+                                acc2 = fmaf(ex2_approx(fmaf(fmaf(Cq, u1, Bq), u1, Aq)), Ir[1], acc2);
+                                acc = fmaf(ex2_approx(fmaf(fmaf(Cq, u2, Bq), u2, Aq)), Ir[2], acc);
+                                acc2 = fmaf(ex2_approx(fmaf(fmaf(Cq, u3, Bq), u3, Aq)), Ir[3], acc2);
                             }
                             acc += acc2;
                         }

@@ -515,6 +515,7 @@ __global__ void k_vox_wtab(const VoxBatch B, int ones)
 //   mode 1: the MLEM update x <- x * sum / (sens + 1e-7), non-finite -> 0,
 //           negative -> 0 (main.m:162-176), and xd = x dq
 //   mode 2: g[voxel] = sum in the full-grid layout (nx + ny*NX)*nwt + k
+//   mode 3: g = sum in the compact voxel order [nv][nwt]
 __global__ void k_vox_reduce(const VoxBatch B, int mode)
 {
     const int64_t *off = B.off + 2 * (B.n + 1);
@@ -536,10 +537,12 @@ __global__ void k_vox_reduce(const VoxBatch B, int mode)
             if (v < 0.f) v = 0.f;
             J.xc[loc] = v;
             J.xd[loc] = v * J.op.coarse_q[loc % K].z;
-        } else {
+        } else if (mode == 2) {
             const int64_t vi = loc / K;
             const int xy = J.op.vox_xy[vi];
             J.g[((int64_t)(xy & 0xffff) + (int64_t)(xy >> 16) * J.op.P.nx) * K + (loc - vi * K)] = (float)s;
+        } else {
+            J.g[loc] = (float)s;   // compact voxel order [nv][NWT]
         }
     }
 }

@@ -689,20 +689,21 @@ int op_plan(xrdt_op *op, Plan **pl)
     return XRDT_OK;
 }
 
-// y[i] = Av_i x[i] for every problem (device arrays, full-grid x).
+// y[i] = Av_i x[i] for every problem (device arrays, full-grid x; x == NULL:
+// the compact xd = x dq of every problem is already in place).
 int plan_forward(Plan *pl, const float *const *x, float *const *y)
 {
     xrdt_ctx *ctx = pl->ctx;
     cudaStream_t st = ctx->stream;
     const int n = (int)pl->ops.size();
     for (int i = 0; i < n; i++) {
-        pl->jobs_h[i].xfull = x[i];
+        pl->jobs_h[i].xfull = x ? x[i] : nullptr;
         pl->jobs_h[i].y = y[i];
     }
     int rc = plan_upload(pl);
     if (rc) return rc;
     const VoxBatch B = plan_batch(pl);
-    if (plan_total(pl, 2) > 0) {
+    if (x && plan_total(pl, 2) > 0) {
         ProfScope ps(ctx, XRDT_KERNEL_VOX_UPDATE);
         CK(launch_vox_gather(B, plan_total(pl, 2), false, st, &ctx->launches));
     }
@@ -718,8 +719,9 @@ int plan_forward(Plan *pl, const float *const *x, float *const *y)
     return XRDT_OK;
 }
 
-// g[i] = Av_i^T w[i] for every problem (device arrays, full-grid g).
-int plan_adjoint(Plan *pl, const float *const *w, float *const *g)
+// g[i] = Av_i^T w[i] for every problem (device arrays, full-grid g; compact:
+// g[i] in the compact voxel order [nv][NWT]).
+int plan_adjoint(Plan *pl, const float *const *w, float *const *g, bool compact = false)
 {
     xrdt_ctx *ctx = pl->ctx;
     cudaStream_t st = ctx->stream;
@@ -728,7 +730,7 @@ int plan_adjoint(Plan *pl, const float *const *w, float *const *g)
         const xrdt_op *op = pl->ops[i];
         pl->jobs_h[i].w = w[i];
         pl->jobs_h[i].g = g[i];
-        CK(cudaMemsetAsync(g[i], 0, sizeof(float) * (size_t)op->p.nx * op->p.ny * op->p.nwt, st));
+        if (!compact) CK(cudaMemsetAsync(g[i], 0, sizeof(float) * (size_t)op->p.nx * op->p.ny * op->p.nwt, st));
     }
     if (plan_total(pl, 2) == 0) return XRDT_OK;
     int rc = plan_upload(pl);
@@ -744,7 +746,31 @@ int plan_adjoint(Plan *pl, const float *const *w, float *const *g)
         else CK(launch_vox_adjoint(B, pl->adj_grid, pl->adj_smem, st, &ctx->launches));
     }
     ProfScope ps(ctx, XRDT_KERNEL_VOX_UPDATE);
-    CK(launch_vox_reduce(B, plan_total(pl, 2), 2, st, &ctx->launches));
+    CK(launch_vox_reduce(B, plan_total(pl, 2), compact ? 3 : 2, st, &ctx->launches));
+    return XRDT_OK;
+}
+
+// One MLEM pass of every problem without the update: the forward with the
+// ratios y / (Av x + c) (xd in place, ymeas and cbg in the descriptors), the
+// adjoint of the ratios, and their sums into g in the compact voxel order.
+int plan_ratio_backprojection(Plan *pl)
+{
+    xrdt_ctx *ctx = pl->ctx;
+    cudaStream_t st = ctx->stream;
+    const VoxBatch B = plan_batch(pl);
+    if (pl->streamed) {
+        ProfScope ps(ctx, XRDT_KERNEL_VOX_FORWARD);
+        CK(stream_forward(pl, true, st, &ctx->launches));
+    } else {
+        {
+            ProfScope ps(ctx, XRDT_KERNEL_VOX_FORWARD);
+            CK(launch_vox_forward(B, true, pl->fwd_grid, pl->fwd_smem, st, &ctx->launches));
+        }
+        ProfScope ps(ctx, XRDT_KERNEL_VOX_ADJOINT);
+        CK(launch_vox_adjoint(B, pl->adj_grid, pl->adj_smem, st, &ctx->launches));
+    }
+    ProfScope ps(ctx, XRDT_KERNEL_VOX_UPDATE);
+    CK(launch_vox_reduce(B, plan_total(pl, 2), 3, st, &ctx->launches));
     return XRDT_OK;
 }
 
@@ -1329,6 +1355,276 @@ int32_t xrdt_batch_tune(xrdt_batch *b, int32_t *adj_warps, int64_t *adj_tiles, i
     if (fwd_grid) *fwd_grid = b->plan->fwd_grid;
     if (adj_grid) *adj_grid = b->plan->adj_grid;
     return XRDT_OK;
+}
+
+} // extern "C"
+
+// ---- the operator with a dense q basis -------------------------------------
+// The unknowns of a voxel are J coefficients c[v, j] of a fixed basis
+// B[j, k] over the NWT coarse q bins: x[v, k] = sum_j c[v, j] B[j, k].  The
+// forward expands the coefficients on the tensor cores (tcgen05, 3xTF32,
+// k_basis.cu) straight into x dq, the input of the per-voxel forward; the
+// adjoint contracts the per-voxel back-projection with B^T on the tensor
+// cores.  MLEM runs on the coefficients (main.m:162-176 with the operator
+// A B^T), which keeps them non-negative for a non-negative basis.
+
+struct xrdt_bop {
+    xrdt_op *op = nullptr;
+    int J = 0;
+    std::vector<void *> allocs;
+    float *Bdq = nullptr;    // [J][NWT]  B[j][k] dq_k: expands into x dq
+    float *Bt = nullptr;     // [NWT][J]  B^T: contracts the back-projection
+    float *coef = nullptr;   // [nv][J]
+    float *gx = nullptr;     // [nv][NWT] back-projection of the coarse bins
+    float *gc = nullptr;     // [nv][J]
+    float *sc = nullptr;     // [nv][J] coefficient sensitivity B A^T 1
+    float *full = nullptr;   // [NX*NY*J] staging of full-grid coefficient arrays
+    unsigned *err = nullptr; // tensor-core wait flag
+    bool sc_ready = false;
+};
+
+namespace {
+
+void bop_free(xrdt_bop *b)
+{
+    for (void *p : b->allocs) cudaFree(p);
+    b->allocs.clear();
+}
+
+int bop_alloc(xrdt_bop *b, size_t bytes, void **out)
+{
+    xrdt_ctx *ctx = b->op->ctx;
+    void *p = nullptr;
+    if (test_alloc_fails()) return fail(ctx, XRDT_ERR_ALLOC, fmt("cudaMalloc(%zu bytes): failure injected", bytes));
+    cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, XRDT_ERR_ALLOC, fmt("cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e)));
+    }
+    b->allocs.push_back(p);
+    *out = p;
+    return XRDT_OK;
+}
+
+// coef [nv][J] -> x dq [nv][NWT] of the operator
+int bop_expand(xrdt_bop *b)
+{
+    xrdt_op *op = b->op;
+    xrdt_ctx *ctx = op->ctx;
+    if (op->v.nv == 0) return XRDT_OK;
+    ProfScope ps(ctx, XRDT_KERNEL_BASIS);
+    CK(launch_basis_expand(b->coef, op->v.nv, b->J, b->Bdq, op->p.nwt, op->xd, b->err, ctx->stream, &ctx->launches));
+    return XRDT_OK;
+}
+
+// gx [nv][NWT] -> gc [nv][J]
+int bop_contract(xrdt_bop *b, const float *gx, float *gc)
+{
+    xrdt_op *op = b->op;
+    xrdt_ctx *ctx = op->ctx;
+    if (op->v.nv == 0) return XRDT_OK;
+    ProfScope ps(ctx, XRDT_KERNEL_BASIS);
+    CK(launch_basis_expand(gx, op->v.nv, op->p.nwt, b->Bt, b->J, gc, b->err, ctx->stream, &ctx->launches));
+    return XRDT_OK;
+}
+
+// full-grid [NX*NY*J] device array -> coef
+int bop_gather(xrdt_bop *b, const float *full)
+{
+    xrdt_op *op = b->op;
+    xrdt_ctx *ctx = op->ctx;
+    CK(launch_rows_gather(full, op->v.vox_xy, op->p.nx, op->v.nv, b->J, b->coef, ctx->stream, &ctx->launches));
+    return XRDT_OK;
+}
+
+// compact [nv][J] -> full-grid [NX*NY*J] device array, zeros at empty voxels
+int bop_scatter(xrdt_bop *b, const float *compact, float *full)
+{
+    xrdt_op *op = b->op;
+    xrdt_ctx *ctx = op->ctx;
+    CK(cudaMemsetAsync(full, 0, sizeof(float) * (size_t)op->p.nx * op->p.ny * b->J, ctx->stream));
+    CK(launch_rows_scatter(compact, op->v.vox_xy, op->p.nx, op->v.nv, b->J, full, ctx->stream, &ctx->launches));
+    return XRDT_OK;
+}
+
+// the tensor-core waits of the calls since the flag was cleared
+int bop_check(xrdt_bop *b)
+{
+    xrdt_ctx *ctx = b->op->ctx;
+    CK(cudaMemcpyAsync(ctx->h_counters + 2, b->err, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->h_counters[2]) return fail(ctx, XRDT_ERR_TIMEOUT, "the tensor-core accumulator never completed");
+    return XRDT_OK;
+}
+
+int bop_begin(xrdt_bop *b)
+{
+    if (!b || !b->op) return XRDT_ERR_NULL;
+    int rc = begin(b->op);
+    if (rc) return rc;
+    xrdt_ctx *ctx = b->op->ctx;
+    CK(cudaMemsetAsync(b->err, 0, sizeof(unsigned), ctx->stream));
+    return XRDT_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int32_t xrdt_bop_create(xrdt_op *op, const float *B, int32_t J, xrdt_bop **out)
+{
+    if (!op || !out) return XRDT_ERR_NULL;
+    *out = nullptr;
+    int rc = begin(op);
+    if (rc) return rc;
+    xrdt_ctx *ctx = op->ctx;
+    if (!B) return fail(ctx, XRDT_ERR_NULL, "the basis is required");
+    const int K = op->p.nwt;
+    if (J < 16 || J > 64 || (J & 15) || K < 16 || K > 64 || (K & 15))
+        return fail(ctx, XRDT_ERR_DIMS, "need J and NWT multiples of 16 in [16, 64]");
+    std::vector<float> hB((size_t)J * K);
+    CK(cudaMemcpy(hB.data(), B, sizeof(float) * hB.size(), cudaMemcpyDefault));
+    for (float v : hB)
+        if (!(v >= 0.f) || !std::isfinite(v)) return fail(ctx, XRDT_ERR_INPUT, "basis entries must be finite and >= 0");
+    std::vector<float4> cq(K);
+    CK(cudaMemcpy(cq.data(), op->v.coarse_q, sizeof(float4) * K, cudaMemcpyDeviceToHost));
+    std::vector<float> hBdq((size_t)J * K), hBt((size_t)K * J);
+    for (int j = 0; j < J; j++)
+        for (int k = 0; k < K; k++) {
+            hBdq[(size_t)j * K + k] = hB[(size_t)j * K + k] * cq[k].z;   // as the forward forms x dq
+            hBt[(size_t)k * J + j] = hB[(size_t)j * K + k];
+        }
+    xrdt_bop *b = new xrdt_bop();
+    b->op = op;
+    b->J = J;
+    const size_t nv = (size_t)std::max(op->v.nv, 1);
+    void *p;
+    auto alloc = [&](size_t bytes, void **dst) { return bop_alloc(b, bytes, dst); };
+    if ((rc = alloc(sizeof(float) * hBdq.size(), &p)) == 0) b->Bdq = (float *)p;
+    if (!rc && (rc = alloc(sizeof(float) * hBt.size(), &p)) == 0) b->Bt = (float *)p;
+    if (!rc && (rc = alloc(sizeof(float) * nv * J, &p)) == 0) b->coef = (float *)p;
+    if (!rc && (rc = alloc(sizeof(float) * nv * K, &p)) == 0) b->gx = (float *)p;
+    if (!rc && (rc = alloc(sizeof(float) * nv * J, &p)) == 0) b->gc = (float *)p;
+    if (!rc && (rc = alloc(sizeof(float) * nv * J, &p)) == 0) b->sc = (float *)p;
+    if (!rc && (rc = alloc(sizeof(float) * (size_t)op->p.nx * op->p.ny * J, &p)) == 0) b->full = (float *)p;
+    if (!rc && (rc = alloc(sizeof(unsigned), &p)) == 0) b->err = (unsigned *)p;
+    cudaError_t e = cudaSuccess;
+    if (!rc) e = cudaMemcpy(b->Bdq, hBdq.data(), sizeof(float) * hBdq.size(), cudaMemcpyHostToDevice);
+    if (!rc && e == cudaSuccess) e = cudaMemcpy(b->Bt, hBt.data(), sizeof(float) * hBt.size(), cudaMemcpyHostToDevice);
+    if (!rc && e != cudaSuccess) {
+        cudaGetLastError();
+        rc = fail(ctx, XRDT_ERR_CUDA, fmt("basis upload: %s", cudaGetErrorString(e)));
+    }
+    if (rc) {
+        bop_free(b);
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return XRDT_OK;
+}
+
+int32_t xrdt_bop_destroy(xrdt_bop *b)
+{
+    if (!b) return XRDT_ERR_NULL;
+    if (b->op && b->op->ctx) {
+        cudaSetDevice(b->op->ctx->device);
+        cudaStreamSynchronize(b->op->ctx->stream);
+    }
+    bop_free(b);
+    delete b;
+    return XRDT_OK;
+}
+
+int32_t xrdt_bop_forward(xrdt_bop *b, const float *c, float *y, uint32_t flags)
+{
+    int rc = bop_begin(b);
+    if (rc) return rc;
+    xrdt_op *op = b->op;
+    xrdt_ctx *ctx = op->ctx;
+    if (!c || !y) return fail(ctx, XRDT_ERR_NULL, "c and y are required");
+    if (flags) return fail(ctx, XRDT_ERR_UNSUPPORTED, "unknown flag bits");
+    cudaStream_t st = ctx->stream;
+    const size_t nfull = (size_t)op->p.nx * op->p.ny * b->J;
+    const float *dc;
+    if ((rc = view_in(op, c, nfull, b->full, &dc))) return rc;
+    const bool hostY = !is_device_ptr(y);
+    float *dy = hostY ? op->ray_a : y;
+    Plan *pl;
+    if ((rc = op_plan(op, &pl)) || (rc = bop_gather(b, dc)) || (rc = bop_expand(b))) return rc;
+    if ((rc = plan_forward(pl, nullptr, &dy))) return rc;
+    if (hostY) CK(cudaMemcpyAsync(y, dy, sizeof(float) * op->rays, cudaMemcpyDeviceToHost, st));
+    return bop_check(b);
+}
+
+int32_t xrdt_bop_adjoint(xrdt_bop *b, const float *w, float *g, uint32_t flags)
+{
+    int rc = bop_begin(b);
+    if (rc) return rc;
+    xrdt_op *op = b->op;
+    xrdt_ctx *ctx = op->ctx;
+    if (!w || !g) return fail(ctx, XRDT_ERR_NULL, "w and g are required");
+    if (flags) return fail(ctx, XRDT_ERR_UNSUPPORTED, "unknown flag bits");
+    cudaStream_t st = ctx->stream;
+    const size_t nfull = (size_t)op->p.nx * op->p.ny * b->J;
+    const float *dw;
+    Plan *pl;
+    if ((rc = view_in(op, w, op->rays, op->ray_a, &dw)) || (rc = op_plan(op, &pl))) return rc;
+    float *gx = b->gx;
+    if ((rc = plan_adjoint(pl, &dw, &gx, true)) || (rc = bop_contract(b, b->gx, b->gc))) return rc;
+    const bool hostG = !is_device_ptr(g);
+    float *dg = hostG ? b->full : g;
+    if ((rc = bop_scatter(b, b->gc, dg))) return rc;
+    if (hostG) CK(cudaMemcpyAsync(g, dg, sizeof(float) * nfull, cudaMemcpyDeviceToHost, st));
+    return bop_check(b);
+}
+
+int32_t xrdt_bop_mlem(xrdt_bop *b, const float *y, const float *c, float *x, int32_t iters, uint32_t flags)
+{
+    int rc = bop_begin(b);
+    if (rc) return rc;
+    xrdt_op *op = b->op;
+    xrdt_ctx *ctx = op->ctx;
+    if (!y || !c || !x) return fail(ctx, XRDT_ERR_NULL, "y, c and x are required");
+    if (iters < 0) return fail(ctx, XRDT_ERR_DIMS, "iters must be >= 0");
+    if (flags) return fail(ctx, XRDT_ERR_UNSUPPORTED, "unknown flag bits");
+    cudaStream_t st = ctx->stream;
+    const size_t nfull = (size_t)op->p.nx * op->p.ny * b->J;
+    const int64_t ncoef = (int64_t)op->v.nv * b->J;
+    const float *dy, *dc, *dx0;
+    Plan *pl;
+    if ((rc = view_in(op, y, op->rays, op->ray_a, &dy)) || (rc = view_in(op, c, op->rays, op->ray_b, &dc)) ||
+        (rc = view_in(op, x, nfull, b->full, &dx0)) || (rc = op_plan(op, &pl)))
+        return rc;
+    if ((rc = bop_gather(b, dx0))) return rc;
+    if (op->v.nv > 0 && iters > 0) {
+        if ((rc = plan_tune(pl)) || (rc = plan_sens(pl))) return rc;
+        if (!b->sc_ready) {
+            // the coefficient sensitivity B (A^T 1), from the operator's FP64 one
+            CK(launch_to_float(op->sens, (int64_t)op->v.nv * op->p.nwt, b->gx, st, &ctx->launches));
+            if ((rc = bop_contract(b, b->gx, b->sc))) return rc;
+            b->sc_ready = true;
+        }
+        pl->jobs_h[0].ymeas = dy;
+        pl->jobs_h[0].cbg = dc;
+        pl->jobs_h[0].g = b->gx;
+        if ((rc = plan_upload(pl))) return rc;
+        for (int it = 0; it < iters; it++) {
+            if ((rc = bop_expand(b)) || (rc = plan_ratio_backprojection(pl)) || (rc = bop_contract(b, b->gx, b->gc)))
+                return rc;
+            ProfScope ps(ctx, XRDT_KERNEL_VOX_UPDATE);
+            CK(launch_bop_update(b->coef, b->gc, b->sc, ncoef, st, &ctx->launches));
+        }
+    }
+    const bool hostX = !is_device_ptr(x);
+    float *dxo = hostX ? b->full : x;
+    if (iters > 0) {
+        if ((rc = bop_scatter(b, b->coef, dxo))) return rc;
+    } else if (hostX) {
+        CK(cudaMemcpyAsync(dxo, dx0, sizeof(float) * nfull, cudaMemcpyDeviceToDevice, st));
+    }
+    if (hostX) CK(cudaMemcpyAsync(x, dxo, sizeof(float) * nfull, cudaMemcpyDeviceToHost, st));
+    return bop_check(b);
 }
 
 } // extern "C"

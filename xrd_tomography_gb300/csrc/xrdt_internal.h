@@ -173,6 +173,16 @@ cudaError_t launch_spectrum(const SpecFineBin *fb, const SpecCoarseBin *sb, int 
 cudaError_t launch_det_walk(const DevProblem &P, const SrcGeom *sg, const int2 *pairs, long long p0,
                             long long n_items, const int *vox_xy, int nv, const float4 *cells, float2 *tab,
                             cudaStream_t s, int64_t *launches);
+// k_bop.cu: rows of R values per non-empty voxel between the full grid
+// [NX*NY][R] and the compact voxel order [nv][R]; the coefficient-space MLEM
+// update c <- c g / (s + 1e-7) with the fix-ups of main.m:163,176.
+cudaError_t launch_rows_gather(const float *full, const int *vox_xy, int nx, int64_t nv, int R, float *compact,
+                               cudaStream_t s, int64_t *launches);
+cudaError_t launch_rows_scatter(const float *compact, const int *vox_xy, int nx, int64_t nv, int R, float *full,
+                                cudaStream_t s, int64_t *launches);
+cudaError_t launch_bop_update(float *c, const float *g, const float *s, int64_t n, cudaStream_t st,
+                              int64_t *launches);
+cudaError_t launch_to_float(const double *a, int64_t n, float *b, cudaStream_t s, int64_t *launches);
 // k_decisions.cu: the integer decisions of the fast path for listed rays
 // (test export): walk[i][v] = (detector-side sample count, its ROI edge,
 // source-side sample count, its ROI edge); nq[i][v][j] = Compton table bin of
