@@ -242,6 +242,10 @@ __device__ __forceinline__ float2 walk_cells(const float4 *__restrict__ cells, i
     // exit edge offset h = +-0.5 (towards the step) times the inverse step
     const float2 hinv = make_float2(L.x < 0.f ? 0.5f * ilx : -0.5f * ilx, L.y < 0.f ? 0.5f * ily : -0.5f * ily);
     const float lxly = L.x * L.y;
+    const float2 uhi = make_float2(w.ux.hi, w.uy.hi), ulo = make_float2(w.ux.lo, w.uy.lo), v2 = make_float2(vx, vy);
+    // the distance of the voxel's nearest sample is below one step unless the
+    // sample count was capped: then a two-sum that needs no ordering
+    const bool small_dlt = w.dlt.hi <= DQ;
     float2 acc = make_float2(0.f, 0.f), comp = make_float2(0.f, 0.f);
     for (float k0 = 0.f; k0 < nf;) {
         // distance s = dlt + k0 DQ and displacement t = s u as float pairs
@@ -249,29 +253,34 @@ __device__ __forceinline__ float2 walk_cells(const float4 *__restrict__ cells, i
         // centre is then good to about 1e-7 voxel, where a position formed
         // at a magnitude of hundreds of voxels in FP32 would be off by 1e-5
         // and shift the interpolant by as much at material edges
-        // (explicitly rounded operations: a contracted multiply-add would
-        // count a product's error twice)
+        // (explicitly rounded operations, x and y packed in one instruction:
+        // a contracted multiply-add would count a product's error twice)
         const float kq = __fmul_rn(k0, DQ);
         const float kqe = fmaf(k0, DQ, -kq);
         const float sh = __fadd_rn(w.dlt.hi, kq);
-        const float bb = __fsub_rn(sh, w.dlt.hi);
-        const float sl = __fadd_rn(__fadd_rn(__fsub_rn(w.dlt.hi, __fsub_rn(sh, bb)), __fsub_rn(kq, bb)),
-                                   __fadd_rn(kqe, w.dlt.lo));
-        const float px = __fmul_rn(sh, w.ux.hi), py = __fmul_rn(sh, w.uy.hi);
-        const float ex = __fadd_rn(fmaf(sh, w.ux.hi, -px), fmaf(sh, w.ux.lo, __fmul_rn(sl, w.ux.hi)));
-        const float ey = __fadd_rn(fmaf(sh, w.uy.hi, -py), fmaf(sh, w.uy.lo, __fmul_rn(sl, w.uy.hi)));
+        float sl;
+        if (small_dlt) {
+            sl = __fadd_rn(__fsub_rn(w.dlt.hi, __fsub_rn(sh, kq)), __fadd_rn(kqe, w.dlt.lo));   // |kq| >= dlt
+        } else {
+            const float bb = __fsub_rn(sh, w.dlt.hi);
+            sl = __fadd_rn(__fadd_rn(__fsub_rn(w.dlt.hi, __fsub_rn(sh, bb)), __fsub_rn(kq, bb)),
+                           __fadd_rn(kqe, w.dlt.lo));
+        }
+        const float2 s2 = make_float2(sh, sh);
+        const float2 p = __fmul2_rn(s2, uhi);
+        const float2 e = __fadd2_rn(__ffma2_rn(s2, uhi, make_float2(-p.x, -p.y)),
+                                    __ffma2_rn(s2, ulo, __fmul2_rn(make_float2(sl, sl), uhi)));
         // the cell whose centre is nearest (any cell holding the point gives
         // the same value: the interpolant is continuous), then the offset
-        const float2 t = make_float2(__fadd_rn(__fadd_rn(vx, px), magic), __fadd_rn(__fadd_rn(vy, py), magic));
+        const float2 t = __fadd2_rn(__fadd2_rn(v2, p), make_float2(magic, magic));
         const int ix = __float_as_int(t.x) - 0x4B400000, iy = __float_as_int(t.y) - 0x4B400000;
         const unsigned c = min((unsigned)(ix * sx + iy * sy), ncell_m1);
         float4 c0, c1;
         ld_cell256(cells + 2 * c, c0, c1);
         // the cell centre (exact) minus the anchor is exact, and it cancels
-        // px but for the offset (Sterbenz), so only ex and ey round
-        const float2 r = make_float2(__fsub_rn(t.x, magic), __fsub_rn(t.y, magic));
-        const float2 d = make_float2(__fadd_rn(__fadd_rn(__fsub_rn(vx, r.x), px), ex),
-                                     __fadd_rn(__fadd_rn(__fsub_rn(vy, r.y), py), ey));
+        // p but for the offset (Sterbenz), so only e rounds
+        const float2 r = __fadd2_rn(t, make_float2(-magic, -magic));
+        const float2 d = __fadd2_rn(__fadd2_rn(__fadd2_rn(v2, make_float2(-r.x, -r.y)), p), e);
         const float2 s = __ffma2_rn(d, ninv, hinv);                                // steps to each exit edge
         // ceil(s) as round(s + 1/2) through the float mantissa (either way at a tie)
         float m = __fadd_rn(__fadd_rn(__fadd_rn(fminf(s.x, s.y), 0.5f), magic), -magic);
