@@ -237,12 +237,18 @@ def test_tiny_mlem_matches_dense_restatement(ctx, oracle_lib):
     op = make_op(inp, ctx)
     y32, c32 = y.astype(np.float32), c.astype(np.float32)
     # Through 20 iterations every estimate is within MLEM_RTOL of FP64.  At 50
-    # the largest element error is 1.3e-5: the FP32 operator's entries are off
-    # by 2e-7 (median) to 2e-6 (99th percentile), and with those entries in
-    # FP64 the iterate is within 5.6e-6 after 50 updates; the FP32 iteration's
-    # own rounding (per-energy weights, the estimate stored as float) adds
-    # the rest in the slowly converging elements.  That bound is asserted
-    # separately below.
+    # the largest element error is 1.26e-5.  The FP32 operator's entries are
+    # off by 2e-7 (median) to 2e-6 (99th percentile); with those entries and
+    # the iteration in FP64 the iterate is within 5.6e-6 after 50 updates.
+    # The rest comes from the FP32 adjoint itself: its update factor g/s of
+    # one iteration differs from the FP64 one by about one float rounding
+    # (5e-8 standard deviation, 3e-7 at most), the same pattern in every
+    # iteration since the weights change slowly, and an element that decays
+    # towards 0 is multiplied by that factor 50 times (the deviation after 50
+    # updates is 35 to 280 times the first one for the largest errors).
+    # Keeping the estimate in FP64 between updates, the partial sums as
+    # float pairs and the sensitivity's weights unrounded changed the
+    # largest error at 50 from 1.32e-5 to 1.26e-5 only.
     for iters, tol in ((1, MLEM_RTOL), (5, MLEM_RTOL), (20, MLEM_RTOL), (50, 2 * MLEM_RTOL)):
         x = op.mlem(y32, c32, x0.astype(np.float32), iters)
         xr = mlem_dense(A, y32.astype(np.float64), c32.astype(np.float64), x0, iters)

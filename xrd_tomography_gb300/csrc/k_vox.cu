@@ -163,7 +163,7 @@ __host__ __device__ inline FwdLayout vox_fwd_layout(const DevProblem &P, int E)
     L.winlo = o; o = al16(o + sizeof(int) * P.nrg_det);
     L.wn = o; o = al16(o + sizeof(int) * 2 * E);
     L.cq = o; o = al16(o + sizeof(float4) * P.nwt);
-    L.ratio = o; o = al16(o + sizeof(float) * P.nrg_det);
+    L.ratio = o; o = al16(o + sizeof(double) * P.nrg_det);
     L.total = o;
     return L;
 }
@@ -183,7 +183,7 @@ __device__ __forceinline__ void vox_fwd_pair(const VoxJob &J, int64_t pidx, unsi
     int *winlo = (int *)(sm + L.winlo);
     int *wn = (int *)(sm + L.wn);
     float4 *cq = (float4 *)(sm + L.cq);
-    float *ratio = (float *)(sm + L.ratio);
+    double *ratio = (double *)(sm + L.ratio);   // kept in FP64: see the weights below
 
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int64_t npairs = (int64_t)P.n_src * P.n_det;
@@ -257,7 +257,7 @@ __device__ __forceinline__ void vox_fwd_pair(const VoxJob &J, int64_t pidx, unsi
         double acc = 0.0;
         for (int j = 0; j < W; j++) acc += (double)rf[n * W + j] * TN[winlo[n] + j - lo_e];
         const int64_t ray = pidx + (int64_t)n * npairs;
-        if (MLEM) ratio[n] = (float)((double)J.ymeas[ray] / (acc + (double)J.cbg[ray] + 1e-20));   // main.m:162
+        if (MLEM) ratio[n] = (double)J.ymeas[ray] / (acc + (double)J.cbg[ray] + 1e-20);   // main.m:162
         else J.y[ray] = (float)acc;
     }
     if (MLEM) {
@@ -268,7 +268,7 @@ __device__ __forceinline__ void vox_fwd_pair(const VoxJob &J, int64_t pidx, unsi
             double s = 0.0;
             for (int n = wn[2 * el]; n <= wn[2 * el + 1]; n++) {
                 const int j = e - winlo[n];
-                if (j >= 0 && j < W) s += (double)rf[n * W + j] * (double)ratio[n];
+                if (j >= 0 && j < W) s += (double)rf[n * W + j] * ratio[n];
             }
             J.what[pidx * E + el] = (float)s;
         }
@@ -474,18 +474,34 @@ k_vox_adj(const VoxBatch B)
                 __syncwarp();
             }
         }
-        // a job that is one tile of a problem adds to the partial rows the
-        // earlier tiles left (tiles run in a fixed order on one stream)
-        float *out = J.part + ((int64_t)by * nv + (int64_t)chunk * 32) * K;
+        // The partial rows keep the compensated sums as pairs (sum, minus
+        // the compensation): rounded to one float, each row would carry the
+        // same relative error into every MLEM iteration, where the update
+        // multiplies it in again and again.  A job that is one tile of a
+        // problem adds to the rows the earlier tiles left (tiles run in a
+        // fixed order on one stream), with a two-sum.
+        float2 *out = J.part + ((int64_t)by * nv + (int64_t)chunk * 32) * K;
         if (J.accumulate)
-            for (int i = lane; i < nin * K; i += 32) out[i] += gw[i].x - gw[i].y;
+            for (int i = lane; i < nin * K; i += 32) {
+                const float2 o = out[i];
+                const float s = o.x + gw[i].x;
+                const float bb = s - o.x;
+                const float err = (o.x - (s - bb)) + (gw[i].x - bb);
+                out[i] = make_float2(s, o.y + (err - gw[i].y));
+            }
         else
-            for (int i = lane; i < nin * K; i += 32) out[i] = gw[i].x - gw[i].y;
+            for (int i = lane; i < nin * K; i += 32) out[i] = make_float2(gw[i].x, -gw[i].y);
     }
 }
 
-// what[p, e] = sum_nrg RF[e, nrg] w[p + nrg * npairs] (ones: every w = 1).
-__global__ void k_vox_wtab(const VoxBatch B, int ones)
+// what[p, e] = sum_nrg RF[e, nrg] w[p + nrg * npairs].  mode 0: the weights
+// w; mode 1: every w = 1, the sum rounded to float; mode 2: every w = 1, the
+// part of the sum that rounding to float dropped.  The sensitivity is the
+// adjoint of mode 1 plus that of mode 2: with one float per energy shared by
+// every pair, its rounding would be the same relative error in every term of
+// an energy, which no sum over pairs averages out, and MLEM multiplies each
+// unknown by (1 + that error) again in every iteration.
+__global__ void k_vox_wtab(const VoxBatch B, int mode)
 {
     const int64_t *off = B.off + 4 * (B.n + 1);
     const int64_t total = off[B.n];
@@ -503,15 +519,16 @@ __global__ void k_vox_wtab(const VoxBatch B, int ones)
         for (int n = J.op.win_n[2 * e]; n <= J.op.win_n[2 * e + 1]; n++) {
             const int j = e - J.op.win_lo[n];
             if (j < 0 || j >= W) continue;
-            const double wv = ones ? 1.0 : (double)J.w[p + (int64_t)n * npairs];
+            const double wv = mode ? 1.0 : (double)J.w[p + (int64_t)n * npairs];
             s += (double)J.op.rf_win[n * W + j] * wv;
         }
-        J.what[loc] = (float)s;
+        J.what[loc] = mode == 2 ? (float)(s - (double)(float)s) : (float)s;
     }
 }
 
 // Sum of the adjoint's partial rows in FP64 and what follows from it:
 //   mode 0: sens = sum (the sensitivity, Av^T 1)
+//   mode 4: sens += sum (its second part, k_vox_wtab)
 //   mode 1: the MLEM update x <- x * sum / (sens + 1e-7), non-finite -> 0,
 //           negative -> 0 (main.m:162-176), and xd = x dq
 //   mode 2: g[voxel] = sum in the full-grid layout (nx + ny*NX)*nwt + k
@@ -528,9 +545,14 @@ __global__ void k_vox_reduce(const VoxBatch B, int mode)
         const int64_t loc = t - off[pj];
         const int64_t n = (int64_t)J.op.nv * K;
         double s = 0.0;
-        for (int gi = 0; gi < J.groups; gi++) s += (double)J.part[(int64_t)gi * n + loc];
+        for (int gi = 0; gi < J.groups; gi++) {
+            const float2 pv = J.part[(int64_t)gi * n + loc];
+            s += (double)pv.x + (double)pv.y;
+        }
         if (mode == 0) {
             J.sens[loc] = s;
+        } else if (mode == 4) {
+            J.sens[loc] += s;
         } else if (mode == 1) {
             float v = (float)((double)J.xc[loc] * s / (J.sens[loc] + 1e-7));
             if (!isfinite(v)) v = 0.f;
@@ -700,9 +722,9 @@ cudaError_t launch_vox_adjoint(const VoxBatch &B, int grid, size_t smem, cudaStr
     return cudaGetLastError();
 }
 
-cudaError_t launch_vox_wtab(const VoxBatch &B, int64_t total, bool ones, cudaStream_t s, int64_t *launches)
+cudaError_t launch_vox_wtab(const VoxBatch &B, int64_t total, int mode, cudaStream_t s, int64_t *launches)
 {
-    k_vox_wtab<<<grid_for(total, 256), 256, 0, s>>>(B, ones ? 1 : 0);
+    k_vox_wtab<<<grid_for(total, 256), 256, 0, s>>>(B, mode);
     if (launches) (*launches)++;
     return cudaGetLastError();
 }

@@ -83,6 +83,9 @@ k_det_walk(DevProblem P, F32Consts c, const SrcGeom *__restrict__ sg, const int2
             det_position(P, gs.sphi, gs.cphi, det, &ex, &ey, &ez);
         }
         const float exf = (float)ex, eyf = (float)ey;
+        // the endpoint as float pairs, once per ray group (conversions from
+        // double issue on the FP64 pipe)
+        const ff exff = ff_from_double(ex), eyff = ff_from_double(ey);
         float2 *out = tab + (valid ? row : 0) * nv;
         const int v1 = min(nv, (strip + 1) * kVoxPerStrip);
         for (int v = strip * kVoxPerStrip; v < v1; v++) {
@@ -97,7 +100,7 @@ k_det_walk(DevProblem P, F32Consts c, const SrcGeom *__restrict__ sg, const int2
                 // decided in FP32 (guard bands) or FP64; the anchor of an FP32
                 // decision comes from the endpoint as a float pair
                 if (walk_setup_f32(P, c, exf, eyf, vx, vy, &ws))
-                    walk_anchor_ff(c, ff_from_double(ex), ff_from_double(ey), vx, vy, &ws);
+                    walk_anchor_ff(c, exff, eyff, vx, vy, &ws);
                 else
                     walk_setup_f64(P, ex, ey, (double)vx, (double)vy, &ws);
             }

@@ -33,7 +33,7 @@ struct xrdt_op {
     float *a1 = nullptr, *a2 = nullptr;
     float *xc = nullptr, *xd = nullptr;   // unknowns, compact; xd = x * dq
     float *what = nullptr;                // [pairs][E]
-    float *part = nullptr;                // [groups][nv][NWT]
+    float2 *part = nullptr;               // [groups][nv][NWT] as float pairs
     double *sens = nullptr;               // [nv][NWT]
     float *xfull = nullptr;               // staging of the full-grid layout
     float *ray_a = nullptr, *ray_b = nullptr;   // staging of ray vectors
@@ -317,7 +317,7 @@ cudaError_t zero_rows(const Plan *pl, cudaStream_t st)
     for (size_t i = 0; i < pl->ops.size(); i++) {
         const xrdt_op *op = pl->ops[i];
         if (op->v.nv == 0) continue;
-        cudaError_t e = cudaMemsetAsync(op->part, 0, sizeof(float) * (size_t)pl->rows[i] * op->v.nv * op->p.nwt, st);
+        cudaError_t e = cudaMemsetAsync(op->part, 0, sizeof(float2) * (size_t)pl->rows[i] * op->v.nv * op->p.nwt, st);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
@@ -505,20 +505,24 @@ int plan_sens(Plan *pl)
     if (rc) return rc;
     const VoxBatch B = plan_batch(pl);
     cudaStream_t st = ctx->stream;
-    {
-        ProfScope ps(ctx, XRDT_KERNEL_VOX_UPDATE);
-        CK(launch_vox_wtab(B, plan_total(pl, 4), true, st, &ctx->launches));
-    }
-    if (pl->streamed) {
-        ProfScope ps(ctx, XRDT_KERNEL_VOX_ADJOINT);
-        CK(stream_adjoint(pl, st, &ctx->launches));
-    } else {
-        ProfScope ps(ctx, XRDT_KERNEL_VOX_ADJOINT);
-        CK(launch_vox_adjoint(B, pl->adj_grid, pl->adj_smem, st, &ctx->launches));
-    }
-    {
-        ProfScope ps(ctx, XRDT_KERNEL_VOX_UPDATE);
-        CK(launch_vox_reduce(B, plan_total(pl, 2), 0, st, &ctx->launches));
+    // Av^T 1 in two parts: the weights of ones rounded to float, then what
+    // that rounding dropped (k_vox_wtab), added in FP64
+    for (int part = 0; part < 2; part++) {
+        {
+            ProfScope ps(ctx, XRDT_KERNEL_VOX_UPDATE);
+            CK(launch_vox_wtab(B, plan_total(pl, 4), 1 + part, st, &ctx->launches));
+        }
+        if (pl->streamed) {
+            ProfScope ps(ctx, XRDT_KERNEL_VOX_ADJOINT);
+            CK(stream_adjoint(pl, st, &ctx->launches));
+        } else {
+            ProfScope ps(ctx, XRDT_KERNEL_VOX_ADJOINT);
+            CK(launch_vox_adjoint(B, pl->adj_grid, pl->adj_smem, st, &ctx->launches));
+        }
+        {
+            ProfScope ps(ctx, XRDT_KERNEL_VOX_UPDATE);
+            CK(launch_vox_reduce(B, plan_total(pl, 2), part ? 4 : 0, st, &ctx->launches));
+        }
     }
     for (xrdt_op *op : pl->ops) op->sens_ready = true;
     return XRDT_OK;
@@ -622,7 +626,7 @@ int plan_tune(Plan *pl)
     }
     int rc = plan_upload(pl);
     if (rc) return rc;
-    CK(launch_vox_wtab(plan_batch(pl), plan_total(pl, 4), true, st, &ctx->launches));
+    CK(launch_vox_wtab(plan_batch(pl), plan_total(pl, 4), 1, st, &ctx->launches));
     // streamed: the candidates are timed on the first tile, walked once here
     // (they add into partial rows that every real call clears first)
     if (pl->streamed) CK(tile_walks(pl, pl->tiles.front(), st, &ctx->launches));
@@ -738,7 +742,7 @@ int plan_adjoint(Plan *pl, const float *const *w, float *const *g, bool compact 
     const VoxBatch B = plan_batch(pl);
     {
         ProfScope ps(ctx, XRDT_KERNEL_VOX_UPDATE);
-        CK(launch_vox_wtab(B, plan_total(pl, 4), false, st, &ctx->launches));
+        CK(launch_vox_wtab(B, plan_total(pl, 4), 0, st, &ctx->launches));
     }
     {
         ProfScope ps(ctx, XRDT_KERNEL_VOX_ADJOINT);

@@ -238,7 +238,7 @@ struct VoxJob {
     float *y;                  // [rays] forward output
     const float *ymeas, *cbg;  // [rays] MLEM counts and background
     float *what;               // [pairs][E] per-energy weights
-    float *part;               // [groups][nv][nwt] adjoint partial sums
+    float2 *part;              // [groups][nv][nwt] adjoint partial sums, each as a float pair
     double *sens;              // [nv][nwt] sensitivity
     float *g;                  // [nx*ny*nwt] adjoint output
     const float *w;            // [rays] adjoint weights
@@ -274,7 +274,7 @@ cudaError_t launch_vox_forward(const VoxBatch &B, bool mlem, int grid, size_t sm
                                int64_t *launches);
 cudaError_t launch_vox_adjoint(const VoxBatch &B, int grid, size_t smem, cudaStream_t s, int64_t *launches);
 // Element-wise kernels over the concatenated ranges (total = the last offset).
-cudaError_t launch_vox_wtab(const VoxBatch &B, int64_t total, bool ones, cudaStream_t s, int64_t *launches);
+cudaError_t launch_vox_wtab(const VoxBatch &B, int64_t total, int mode, cudaStream_t s, int64_t *launches);
 cudaError_t launch_vox_reduce(const VoxBatch &B, int64_t total, int mode, cudaStream_t s, int64_t *launches);
 cudaError_t launch_vox_gather(const VoxBatch &B, int64_t total, bool with_xc, cudaStream_t s, int64_t *launches);
 cudaError_t launch_vox_scatter(const VoxBatch &B, int64_t total, cudaStream_t s, int64_t *launches);
