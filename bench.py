@@ -72,6 +72,8 @@ def parse():
     ap.add_argument("--mlem", action="store_true",
                     help="--workload 4: per-voxel MLEM on slices of the 384x384 stack instead of the forward "
                          "projection")
+    ap.add_argument("--basis", action="store_true",
+                    help="time only the tensor-core basis expansion (the default run includes it)")
     return ap.parse_args()
 
 
@@ -308,6 +310,44 @@ def mlem_stored_bench(xt, synth, ctx, stream, dev, iters=200):
                          "traffic": None, "algorithmic_bytes_per_iter": traffic, "peak_source": src}}
 
 
+def basis_bench(xt, ctx, dev, launches=20):
+    """xrdt_basis_expand (I = C B, 3xTF32 on tcgen05) on inputs larger than
+    L2, for two shapes: K = N = 32 (a dense basis of 32 coefficients onto 32
+    coarse bins, as the basis operator expands per voxel) and K = 64, N = 256.
+    Kernel time from CUDA events on the library's stream, mean over
+    `launches` launches; bytes are the algorithmic ones (C and B read, I
+    written once); flops count the three TF32 products."""
+    import torch
+    peak, src = hbm_peak_gbs()
+    out = {}
+    for K, N, M in ((32, 32, 152 * 128 * 64), (64, 256, 152 * 128 * 8)):
+        g = torch.Generator(device="cpu").manual_seed(K * 1000 + N)
+        C = torch.rand(M, K, generator=g).to(dev)
+        B = torch.rand(K, N, generator=g).to(dev)
+        I = torch.empty(M, N, device=dev)
+        xt.basis_expand(C, B, I, ctx=ctx)
+        ctx.set_profiling(True)
+        for _ in range(launches):
+            xt.basis_expand(C, B, I, ctx=ctx)
+        n, ms, _ = ctx.kernel_stats(xt.api.KERNEL_BASIS)
+        ctx.set_profiling(False)
+        torch.cuda.synchronize(dev)
+        t = ms / max(1, n) * 1e-3
+        byts = 4.0 * (M * K + K * N + M * N)
+        gbs = byts / t / 1e9
+        # spot check against FP64 on a few rows
+        rows = torch.arange(0, M, max(1, M // 64), device=dev)
+        ref = (C[rows].double() @ B.double())
+        err = float(((I[rows].double() - ref).abs() / ref.abs().clamp_min(1e-30)).max())
+        out[f"M{M}_K{K}_N{N}"] = {
+            "ms_per_launch": t * 1e3, "launches": int(n), "tflops_3xtf32": 6.0 * M * N * K / t / 1e12,
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                         "traffic": None, "algorithmic_bytes_per_launch": byts, "peak_source": src},
+            "max_rel_err_vs_fp64": err}
+        del C, B, I
+    return out
+
+
 def vox_mlem_bench(xt, synth, ctx, stream, dev, iters=50):
     """Per-voxel-coefficient MLEM (main.m:162-176 with one coarse-q pattern per
     voxel) on the 128x128 workload: counts drawn from a seeded ground truth
@@ -394,15 +434,15 @@ def vox_err_vs_oracle(inp, x_host, y_gpu, n, seed):
     return err_summary(np.asarray(y_gpu)[rays], y_ref)
 
 
-def batch_mlem_bench(xt, synth, ctx, stream, dev, n=8, iters=10):
+def batch_mlem_bench(xt, synth, ctx, stream, dev, n=8, iters=10, side=(64, 160), views=(24, 64), px=(64, 160)):
     """Batched MLEM over phantoms of uneven size (the batched configuration's
     generator with its ranges scaled down so that the section takes seconds:
-    sides 64-160 voxels, 24-64 views, 64-160 px, 64 energy bins, 128 fine q
-    bins, 32 coefficients per voxel): one persistent launch per kernel and
-    one CUDA graph per iteration for the whole batch, against the same
-    operators run one after another and the plain FP64 kernel."""
+    by default sides 64-160 voxels, 24-64 views, 64-160 px, 64 energy bins,
+    128 fine q bins, 32 coefficients per voxel): one persistent launch per
+    kernel and one CUDA graph per iteration for the whole batch, against the
+    same operators run one after another and the plain FP64 kernel."""
     import torch
-    inps = synth.batch_inputs(n, side=(64, 160), views=(24, 64), px=(64, 160))
+    inps = synth.batch_inputs(n, side=side, views=views, px=px)
     ops = [xt.Operator(i.problem, i.spectrum, i.seg, i.a1, i.a2, ctx=ctx) for i in inps]
     ys, cs, x0 = [], [], []
     for k, (inp, op) in enumerate(zip(inps, ops)):
@@ -668,6 +708,10 @@ def run_ours(args):
         line["mlem"] = mlem_stored_bench(xt, synth, ctx, stream, dev)
         line["vox_mlem"] = vox_mlem_bench(xt, synth, ctx, stream, dev)
         line["batch_mlem"] = batch_mlem_bench(xt, synth, ctx, stream, dev)
+        # many small problems, each of which alone leaves most of the GPU idle
+        line["batch_mlem_small"] = batch_mlem_bench(xt, synth, ctx, stream, dev, n=48, side=(24, 48),
+                                                    views=(8, 16), px=(16, 32))
+        line["basis"] = basis_bench(xt, ctx, dev)
     if rank == 0:
         # roofline of the dominant kernel: the forward kernel's exponentials
         # (Gaussian q terms, attenuation and Compton factors) on the SFU
@@ -690,6 +734,9 @@ def run_ours(args):
             "issue_slots_busy": K_FWD_ISSUE_BUSY,
             "issue_source": "ncu Issue Slots Busy of k_fwd on the 128x128 workload",
             "kernel": "k_fwd (factored forward projector)",
+            "work": "exp2 evaluations the kernel performs (q bins inside its 7.5-sigma windows, one attenuation "
+                    "and one Compton factor per (voxel, source energy)), counted by the kernel itself: the "
+                    "implemented algorithm's count, not the dense reference-equivalent one of the metric",
             "work_per_launch": work, "launch_ms": per_launch_ms,
             "peak_source": "measured on this GPU by xrdt_probe_peak (ex2.approx, all SMs)",
         }
@@ -720,10 +767,26 @@ def run_ours(args):
     ctx.close()
 
 
+def run_basis_only(args):
+    import torch
+    import xrd_tomography_gb300 as xt
+    from xrd_tomography_gb300 import build as lib_build
+    lib_build.build()
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    ctx = xt.Context(0, stream=stream.cuda_stream)
+    print(json.dumps({"metric": "basis expansion (3xTF32 on tcgen05)", "basis": basis_bench(xt, ctx, dev)}),
+          flush=True)
+    ctx.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.basis:
+        run_basis_only(args)
     elif args.workload == 3 or (args.workload == 4 and args.mlem):
         run_batched_stated(args)
     else:

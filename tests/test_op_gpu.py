@@ -246,9 +246,11 @@ def test_tiny_mlem_matches_dense_restatement(ctx, oracle_lib):
     # iteration since the weights change slowly, and an element that decays
     # towards 0 is multiplied by that factor 50 times (the deviation after 50
     # updates is 35 to 280 times the first one for the largest errors).
-    # Keeping the estimate in FP64 between updates, the partial sums as
-    # float pairs and the sensitivity's weights unrounded changed the
-    # largest error at 50 from 1.32e-5 to 1.26e-5 only.
+    # Keeping the partial sums as float pairs and the sensitivity's weights
+    # unrounded changed the largest error at 50 from 1.32e-5 to 1.26e-5 only;
+    # an estimate carried in FP64 between updates changed nothing (it is not
+    # kept: a checkpoint holds the float estimate, and a resumed run must
+    # equal the uninterrupted one).
     for iters, tol in ((1, MLEM_RTOL), (5, MLEM_RTOL), (20, MLEM_RTOL), (50, 2 * MLEM_RTOL)):
         x = op.mlem(y32, c32, x0.astype(np.float32), iters)
         xr = mlem_dense(A, y32.astype(np.float64), c32.astype(np.float64), x0, iters)
