@@ -202,6 +202,29 @@ int32_t xrdt_forward_rays(xrdt_ctx *ctx, const xrdt_problem *p,
                           float *Nphotons, float *Cphotons, float *A_rows,
                           uint32_t flags);
 
+/* The cross-section table path: the forward model with the coherent
+ * (Rayleigh) term read from a tabulated cross-section S1 [NQ, NA] instead of
+ * the materials' fine-q patterns -- the form the reference keeps commented
+ * out after its kernel (integrate_diffraction.cu:416-418, 479-494, 703-719;
+ * tables from XSection_builder.m:93-128):
+ *   Nphotons[ray] = sum_v sum_{e in window} RF[e,nrg] Pin Pout geom
+ *                   Rayleigh(theta) a2(v) S1[nq, na]
+ * with nq the bin of log2(ein sin(theta/2)) on [q_min, q_max) (NQ bins),
+ * na the Compton table's column, S1 quantised to u8 by floor and clamp as S2
+ * is; Cphotons exactly as xrdt_forward.  XRDT_TAB_BILINEAR reads both tables
+ * bilinearly instead, between the grid points q_min + i (q_max - q_min)/(NQ-1)
+ * and a_min + j (a_max - a_min)/(NA-1) of XSection_builder.m:121-125
+ * (clamped at the ends).  Arguments and layouts as xrdt_forward, with S1 in
+ * place of Ifine; the caller scales Nphotons by S1_max/255 as main.m:68
+ * scales Cphotons.  Every ray; no model matrix; flags: XRDT_TAB_BILINEAR,
+ * XRDT_FWD_NO_SYNC. */
+#define XRDT_TAB_BILINEAR 0x4u
+int32_t xrdt_forward_tables(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum,
+                            const int32_t *seg, const float *a1, const float *a2,
+                            const float *S1, const float *S2,
+                            float q_min, float q_max, float a_min, float a_max,
+                            float *Nphotons, float *Cphotons, uint32_t flags);
+
 /* The integer decisions of the fast forward path, for bit-exact comparison
  * with an FP64 restatement (a test export: the float outputs of
  * xrdt_forward would hide a one-bin flip under their tolerance).  For the

@@ -49,6 +49,7 @@ def lib():
         _lib.xrdt_oracle_vox_rays.restype = ctypes.c_int32
         _lib.xrdt_oracle_ct_rays.restype = ctypes.c_int32
         _lib.xrdt_oracle_decisions.restype = ctypes.c_int32
+        _lib.xrdt_oracle_forward_tables.restype = ctypes.c_int32
         _lib.xrdt_oracle_attenuator.restype = ctypes.c_int64
         _lib.xrdt_oracle_get_intersection.restype = ctypes.c_int32
     return _lib
@@ -93,6 +94,28 @@ def forward_rays(inp, rays, want_a=False, want_av=False, threads=0):
     if rc != 0:
         raise ValueError("oracle rejected the input (material id above n_mat)")
     return N, C, A, Av
+
+
+def forward_tables(inp, S1, rays, bilinear=False, threads=0):
+    """Oracle Nphotons (coherent term from the S1 table) and Cphotons of the
+    cross-section table path for the listed rays, in FP64; nearest-bin
+    lookups, or bilinear ones."""
+    p = inp.problem
+    rays = np.ascontiguousarray(rays, np.int64)
+    n = rays.size
+    N = np.zeros(n)
+    C = np.zeros(n)
+    keep = [np.ascontiguousarray(x, np.float32) for x in (inp.spectrum, inp.a1, inp.a2, S1, inp.S2)]
+    seg = np.ascontiguousarray(inp.seg, np.int32)
+    rc = lib().xrdt_oracle_forward_tables(
+        ctypes.byref(p), keep[0].ctypes.data_as(_f), seg.ctypes.data_as(_i32), keep[1].ctypes.data_as(_f),
+        keep[2].ctypes.data_as(_f), keep[3].ctypes.data_as(_f), keep[4].ctypes.data_as(_f),
+        ctypes.c_float(inp.q_min), ctypes.c_float(inp.q_max), ctypes.c_float(inp.a_min), ctypes.c_float(inp.a_max),
+        ctypes.c_int32(1 if bilinear else 0), rays.ctypes.data_as(_i64), ctypes.c_int64(n),
+        N.ctypes.data_as(_d), C.ctypes.data_as(_d), ctypes.c_int32(threads))
+    if rc != 0:
+        raise ValueError("oracle rejected the input")
+    return N, C
 
 
 def decisions(inp, rays, threads=0):

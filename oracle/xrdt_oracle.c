@@ -198,6 +198,35 @@ typedef struct {
     double qnow, dqnow;
 } coarse_bin;
 
+/* The cross-section table path (xrdt_oracle_forward_tables): the coherent
+ * term from the u8 table S1 instead of the fine-q pattern sum, and the
+ * lookups of both tables by nearest bin or bilinear. */
+typedef struct {
+    const unsigned char *S1u8;
+    int bilinear;
+} oracle_tables;
+
+/* Bilinear value of a u8 table [nq, na] (index q + a*nq) at grid coordinates
+ * (tq, ta), the grid points being the table's entries
+ * (XSection_builder.m:121-125: q_min + i (q_max - q_min)/(NQ - 1)); clamped
+ * to the table. */
+static double table_bilinear(const unsigned char *S, int nq, int na, double tq, double ta)
+{
+    if (!(tq > 0.0)) tq = 0.0;
+    if (tq > (double)(nq - 1)) tq = (double)(nq - 1);
+    if (!(ta > 0.0)) ta = 0.0;
+    if (ta > (double)(na - 1)) ta = (double)(na - 1);
+    int i = (int)floor(tq), j = (int)floor(ta);
+    if (i > nq - 2) i = nq - 2;
+    if (j > na - 2) j = na - 2;
+    if (i < 0) i = 0;
+    if (j < 0) j = 0;
+    const double f = tq - (double)i, g = ta - (double)j;
+    const double s00 = S[i + j * nq], s10 = S[(i + 1) + j * nq];
+    const double s01 = S[i + (j + 1) * nq], s11 = S[(i + 1) + (j + 1) * nq];
+    return (1.0 - g) * ((1.0 - f) * s00 + f * s10) + g * ((1.0 - f) * s01 + f * s11);
+}
+
 /* One block of integrate_diffraction.cu:9-409 in FP64. */
 static void forward_one_ray(const xrdt_problem *p, const float *spectrum, const float *Ifine,
                             const int32_t *seg, const float *a1, const float *a2,
@@ -205,7 +234,7 @@ static void forward_one_ray(const xrdt_problem *p, const float *spectrum, const 
                             double q_min, double q_max, double a_min, double a_max,
                             int64_t ray, double *N_out, double *C_out, double *A_row,
                             double *Av_row, const double *xv, double *yv, double *gv, double wgt,
-                            int32_t *dec_walk, int32_t *dec_nq, int32_t *dec_na)
+                            int32_t *dec_walk, int32_t *dec_nq, int32_t *dec_na, const oracle_tables *tab)
 {
     /* dec_*: where set, the integer decisions of every non-empty voxel in loop
      * order: walk[v] = (detector-side samples, its edge, source-side samples,
@@ -252,6 +281,8 @@ static void forward_one_ray(const xrdt_problem *p, const float *spectrum, const 
 
     double da = (a_max - a_min) / (double)NA; /* :167-168 */
     double dq = (q_max - q_min) / (double)NQ;
+    double dq_grid = (q_max - q_min) / (double)(NQ - 1);  /* the tables' grid points */
+    double da_grid = (a_max - a_min) / (double)(NA - 1);
     double dq_fine = (p->q_hi - p->q_lo) / (double)NQF; /* Forward_XRD.cu:42 */
     const int quirk_stale = (p->quirks & XRDT_QUIRK_STALE_VOXEL_A) != 0;
 
@@ -275,6 +306,7 @@ static void forward_one_ray(const xrdt_problem *p, const float *spectrum, const 
             int na = cuda_floor_int((log2aratio - a_min) / da);
             if (na < 0) na = 0;
             else if (na >= NA) na = NA - 1;
+            const double ta = (log2aratio - a_min) / da_grid;   /* bilinear lookups */
 
             Rvox_x = cur_x;
             Rvox_y = cur_y;
@@ -339,9 +371,26 @@ static void forward_one_ray(const xrdt_problem *p, const float *spectrum, const 
                 double Pin = exp(-(As2v_x / f1 + As2v_y / f2));  /* :295-296 */
                 double Pout = exp(-(Av2d_x / f1 + Av2d_y / f2));
 
+                /* Coherent term from the S1 table instead (the reference's
+                 * commented-out kernel, integrate_diffraction.cu:716-719 with
+                 * the bin of :703-707): wvt = ein sin(theta/2) on the log2
+                 * axis of the tables (XSection_builder.m:106). */
+                if (want_nc && tab) {
+                    double wc = ein * sinthetahalf;
+                    double s1;
+                    if (tab->bilinear) {
+                        s1 = table_bilinear(tab->S1u8, NQ, NA, (log2(wc) - q_min) / dq_grid, ta);
+                    } else {
+                        int nqc = cuda_floor_int((log2(wc) - q_min) / dq);
+                        if (nqc < 0) nqc = 0;
+                        else if (nqc >= NQ) nqc = NQ - 1;
+                        s1 = (double)tab->S1u8[nqc + na * NQ];
+                    }
+                    Nnow += Pin * Pout * RF * geomproduct * Rayleigh_factor * a2now * s1;
+                }
                 /* Fine-q Rayleigh sum, :299-308 (all NQF bins). */
-                const float *Im = want_nc ? Ifine + (int64_t)matID * NQF : NULL;
-                for (int qf = 0; want_nc && qf < NQF; qf++) {
+                const float *Im = (want_nc && !tab) ? Ifine + (int64_t)matID * NQF : NULL;
+                for (int qf = 0; Im && qf < NQF; qf++) {
                     double qaxis_fine = p->q_lo + dq_fine * (0.5 + (double)qf);
                     double Rq = RF * exp(-(wvt - qaxis_fine) * (wvt - qaxis_fine) / (2.0 * sigma_wvt2)) *
                                 p->rsqrt2pi / sqrt(sigma_wvt2) * dq_fine;
@@ -377,8 +426,10 @@ static void forward_one_ray(const xrdt_problem *p, const float *spectrum, const 
                 f2 = p->kn0 + p->kn1 * eout + p->kn2 * eout * eout;
                 double Pout_c = exp(-(Av2d_x / f1 + Av2d_y / f2));
                 double Compton_factor = eratio * eratio * (eratio + 1.0 / eratio - 1.0 + costheta * costheta) / 2.0;
-                Cnow += channel_match * Pin * Pout_c * RF * geomproduct * Compton_factor * a2now *
-                        (double)S2u8[nq + na * NQ];
+                const double s2 = (tab && tab->bilinear)
+                                      ? table_bilinear(S2u8, NQ, NA, (log2wvt - q_min) / dq_grid, ta)
+                                      : (double)S2u8[nq + na * NQ];
+                Cnow += channel_match * Pin * Pout_c * RF * geomproduct * Compton_factor * a2now * s2;
             }
             dec_v++;
         }
@@ -425,10 +476,44 @@ int32_t xrdt_oracle_forward_rays(const xrdt_problem *p,
         if (Av_row) memset(Av_row, 0, sizeof(double) * (size_t)avrow);
         forward_one_ray(p, spectrum, Ifine, seg, a1, a2, S2u8, cb,
                         (double)q_min, (double)q_max, (double)a_min, (double)a_max,
-                        rays[i], &N_out[i], &C_out[i], A_row, Av_row, NULL, NULL, NULL, 0.0, NULL, NULL, NULL);
+                        rays[i], &N_out[i], &C_out[i], A_row, Av_row, NULL, NULL, NULL, 0.0, NULL, NULL, NULL, NULL);
     }
     free(cb);
     free(S2u8);
+    return 0;
+}
+
+/* The cross-section table path for the listed rays: Nphotons with the
+ * coherent term of the S1 table (nearest bin, or bilinear when bilinear != 0),
+ * Cphotons as xrdt_oracle_forward_rays (bilinear S2 lookups when bilinear). */
+int32_t xrdt_oracle_forward_tables(const xrdt_problem *p, const float *spectrum, const int32_t *seg,
+                                   const float *a1, const float *a2, const float *S1, const float *S2,
+                                   float q_min, float q_max, float a_min, float a_max, int32_t bilinear,
+                                   const int64_t *rays, int64_t n_rays, double *N_out, double *C_out,
+                                   int32_t n_threads)
+{
+    const int64_t nvox = (int64_t)p->nx * p->ny;
+    for (int64_t i = 0; i < nvox; i++)
+        if (seg[i] > p->n_mat) return -1;
+    if (p->nq < 2 || p->na < 2) return -2;
+    const int64_t nS = (int64_t)p->nq * p->na;
+    unsigned char *u8 = (unsigned char *)malloc(2 * (size_t)nS);
+    for (int64_t i = 0; i < 2 * nS; i++) {
+        int s = cuda_floor_int((double)(i < nS ? S1[i] : S2[i - nS]));
+        if (s < 0) s = 0;
+        else if (s > 255) s = 255;
+        u8[i] = (unsigned char)s;
+    }
+    oracle_tables tab = {u8, bilinear ? 1 : 0};
+#ifdef _OPENMP
+    if (n_threads > 0) omp_set_num_threads(n_threads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+    for (int64_t i = 0; i < n_rays; i++)
+        forward_one_ray(p, spectrum, NULL, seg, a1, a2, u8 + nS, NULL, (double)q_min, (double)q_max,
+                        (double)a_min, (double)a_max, rays[i], &N_out[i], &C_out[i], NULL, NULL, NULL, NULL,
+                        NULL, 0.0, NULL, NULL, NULL, &tab);
+    free(u8);
     return 0;
 }
 
@@ -472,7 +557,7 @@ int32_t xrdt_oracle_decisions(const xrdt_problem *p, const float *spectrum, cons
         double nn, cc;
         forward_one_ray(p, spectrum, Ifine, seg, a1, a2, s2u8, cb, (double)q_min, (double)q_max,
                         (double)a_min, (double)a_max, rays[i], &nn, &cc, NULL, NULL, NULL, NULL, NULL, 0.0,
-                        walk + i * nv * 4, nq + i * nv * W, i == 0 ? na : NULL);
+                        walk + i * nv * 4, nq + i * nv * W, i == 0 ? na : NULL, NULL);
     }
     free(cb);
     return 0;
@@ -513,7 +598,7 @@ int32_t xrdt_oracle_vox_rays(const xrdt_problem *p, const float *spectrum, const
         /* one pass per ray: the forward sum and the adjoint accumulation */
         forward_one_ray(p, spectrum, NULL, seg, a1, a2, NULL, cb, 0.0, 1.0, 0.0, 1.0, rays[i], &nn, &cc,
                         NULL, NULL, x, &yy, gpriv ? gpriv + (size_t)t * (size_t)ng : NULL, w ? w[i] : 0.0,
-                        NULL, NULL, NULL);
+                        NULL, NULL, NULL, NULL);
         if (y_out) y_out[i] = yy;
     }
     if (g_out) {

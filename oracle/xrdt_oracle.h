@@ -61,6 +61,16 @@ int32_t xrdt_oracle_forward_rays(const xrdt_problem *p,
  * (voxel index nx+ny*NX) it writes y_out[i] = sum_{v,k} Av[rays[i]][v][k] x[v][k];
  * with w [n_rays] it writes g_out[v][k] = sum_i w[i] Av[rays[i]][v][k].  Either
  * pair may be NULL.  Returns 0, or a negative value for invalid input. */
+/* The cross-section table path: the coherent term from the table S1
+ * (integrate_diffraction.cu:703-719, code the reference keeps commented out)
+ * instead of the fine-q pattern sum, and both tables read by nearest bin or,
+ * with bilinear != 0, bilinearly between the grid points of
+ * XSection_builder.m:121-125. */
+int32_t xrdt_oracle_forward_tables(const xrdt_problem *p, const float *spectrum, const int32_t *seg,
+                                   const float *a1, const float *a2, const float *S1, const float *S2,
+                                   float q_min, float q_max, float a_min, float a_max, int32_t bilinear,
+                                   const int64_t *rays, int64_t n_rays, double *N_out, double *C_out,
+                                   int32_t n_threads);
 int32_t xrdt_oracle_vox_rays(const xrdt_problem *p, const float *spectrum, const int32_t *seg,
                              const float *a1, const float *a2, const double *x, const double *w,
                              const int64_t *rays, int64_t n_rays, double *y_out, double *g_out,

@@ -184,3 +184,31 @@ def test_oracle_ct_limits(oracle_lib):
     T2, _ = oracle_lib.ct_rays(d, rays)
     hit = T < G
     assert hit.any() and np.all(T2[hit] < T[hit]) and np.all(T2[~hit] == T[~hit])
+
+
+def test_table_path_restatement(oracle_lib):
+    """The oracle's cross-section table path (integrate_diffraction.cu:703-719,
+    commented out in the reference): with nearest lookups its Compton counts
+    are the forward's; a constant coherent table gives the same coherent
+    counts by nearest and bilinear lookup; and a coherent table that is
+    linear along the wavevector axis is read exactly by the bilinear lookup,
+    so the counts are linear in the table."""
+    inp = synth.make_inputs(synth.tiny_problem(), 7)
+    p = inp.problem
+    rays = np.arange(p.rays)
+    S1 = synth.coherent_table(inp)
+    _, C_tab = oracle_lib.forward_tables(inp, S1, rays)
+    _, C_fwd, _, _ = oracle_lib.forward_rays(inp, rays)
+    assert np.array_equal(C_tab, C_fwd)
+    Sc = np.full(p.nq * p.na, 99.0, np.float32)
+    Nn, _ = oracle_lib.forward_tables(inp, Sc, rays)
+    Nb, _ = oracle_lib.forward_tables(inp, Sc, rays, bilinear=True)
+    assert np.allclose(Nn, Nb, rtol=1e-13, atol=0)
+    # integer-valued tables a + b*i along q (no u8 rounding): bilinear counts
+    # are affine in (a, b)
+    iq = np.tile(np.arange(p.nq, dtype=np.float32), p.na)
+    N1, _ = oracle_lib.forward_tables(inp, 10.0 + 2.0 * iq, rays, bilinear=True)
+    N2, _ = oracle_lib.forward_tables(inp, 30.0 + 6.0 * iq, rays, bilinear=True)
+    N0, _ = oracle_lib.forward_tables(inp, np.full(p.nq * p.na, 10.0, np.float32), rays, bilinear=True)
+    assert np.allclose(N2, 3.0 * N1, rtol=1e-12, atol=0)
+    assert np.all(N1 >= N0)

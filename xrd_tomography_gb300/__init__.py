@@ -5,6 +5,6 @@ include/xrdt.h; this package is its Python front end.
 """
 from .problem import Problem, QUIRK_STALE_VOXEL_A, reference_problem  # noqa: F401
 from .api import (Batch, BasisOperator, Context, Forward_XRD, Operator, XrdtError, basis_expand, ct_sinogram, forward,  # noqa: F401
-                  forward_rays, lib, mlem_matrix, spectrum_build, debug_decisions,
+                  forward_rays, forward_tables, lib, mlem_matrix, spectrum_build, debug_decisions,
                   mlem_matrix_noalloc, mlem_checkpoint_write, mlem_checkpoint_read, validate,
-                  c_reference_problem, FWD_PLAIN_FP64, FWD_NO_SYNC)
+                  c_reference_problem, FWD_PLAIN_FP64, FWD_NO_SYNC, TAB_BILINEAR)

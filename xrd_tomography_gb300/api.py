@@ -25,6 +25,7 @@ LIB_PATH = os.path.join(HERE, "libxrdt.so")
 
 FWD_PLAIN_FP64 = 0x1
 FWD_NO_SYNC = 0x2
+TAB_BILINEAR = 0x4
 OP_PLAIN_FP64 = 0x1
 (KERNEL_PREP_MAP, KERNEL_PREP_VOXELS, KERNEL_SRC_ATTEN, KERNEL_FORWARD, KERNEL_PLAIN, KERNEL_GATHER,
  KERNEL_MLEM, KERNEL_VOX_FORWARD, KERNEL_VOX_ADJOINT, KERNEL_VOX_UPDATE, KERNEL_CT, KERNEL_BASIS, KERNEL_WALK, KERNEL_SPECTRUM) = range(14)
@@ -50,6 +51,8 @@ SIGNATURES = {
                                                ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)]),
     "xrdt_forward": (ctypes.c_int32, [_vp, _P, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_float, ctypes.c_float,
                                       ctypes.c_float, ctypes.c_float, _vp, _vp, _vp, ctypes.c_uint32]),
+    "xrdt_forward_tables": (ctypes.c_int32, [_vp, _P, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_float, ctypes.c_float,
+                                             ctypes.c_float, ctypes.c_float, _vp, _vp, ctypes.c_uint32]),
     "xrdt_mlem_matrix": (ctypes.c_int32, [_vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp, _vp, ctypes.c_int32,
                                           ctypes.c_uint32]),
     "xrdt_mlem_matrix_noalloc": (ctypes.c_int32, [_vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp, _vp, ctypes.c_int32,
@@ -230,6 +233,33 @@ def forward(p: Problem, spectrum, Ifine, seg, a1, a2, S2, q_min, q_max, a_min, a
                             ptrs[6], ptrs[7], ptrs[8], fl)
     _check(rc, ctx.h)
     return keep[6], keep[7], keep[8]
+
+
+def forward_tables(p: Problem, spectrum, seg, a1, a2, S1, S2, q_min, q_max, a_min, a_max,
+                   Nphotons=None, Cphotons=None, bilinear: bool = False, ctx: Context | None = None,
+                   flags: int = 0):
+    """xrdt_forward_tables: the forward model with the coherent term read
+    from the cross-section table S1 [NQ*NA] (nearest bins, or both tables
+    bilinearly).  Returns (Nphotons, Cphotons) as flat arrays (numpy unless
+    torch CUDA tensors are passed)."""
+    ctx = ctx or default_context()
+    rays = p.rays
+    if Nphotons is None:
+        Nphotons = np.empty(rays, np.float32)
+    if Cphotons is None:
+        Cphotons = np.empty(rays, np.float32)
+    keep = []
+    ptrs = []
+    for a, dt in ((spectrum, np.float32), (seg, np.int32), (a1, np.float32), (a2, np.float32),
+                  (S1, np.float32), (S2, np.float32), (Nphotons, np.float32), (Cphotons, np.float32)):
+        pt, k = _ptr(a, dt)
+        ptrs.append(pt)
+        keep.append(k)
+    fl = flags | (TAB_BILINEAR if bilinear else 0)
+    rc = lib().xrdt_forward_tables(ctx.h, ctypes.byref(p), ptrs[0], ptrs[1], ptrs[2], ptrs[3], ptrs[4], ptrs[5],
+                                   float(q_min), float(q_max), float(a_min), float(a_max), ptrs[6], ptrs[7], fl)
+    _check(rc, ctx.h)
+    return keep[6], keep[7]
 
 
 def forward_rays(p: Problem, rays, spectrum, Ifine, seg, a1, a2, S2, q_min, q_max, a_min, a_max,

@@ -41,6 +41,7 @@ enum Slot {
     S_RAYS, S_PAIRS, S_NC, S_CC, S_AC,
     S_MA, S_MY, S_MC, S_MX, S_MPART, S_MSENS, S_BC, S_BB, S_BI, S_ERR, S_WALK,
     S_SPFINE, S_SPSRC, S_SPDET, S_SPOUT, S_DWALK, S_DNQ,
+    S_S1, S_S1U8, S_VTA,
     S_COUNT
 };
 
@@ -201,6 +202,8 @@ int build_dev_problem(const xrdt_problem *p, float q_min, float q_max, float a_m
     d->a_max = a_max;
     d->dq_tab = ((double)q_max - (double)q_min) / (double)p->nq;
     d->da_tab = ((double)a_max - (double)a_min) / (double)p->na;
+    d->dq_grid = p->nq > 1 ? ((double)q_max - (double)q_min) / (double)(p->nq - 1) : 0.0;
+    d->da_grid = p->na > 1 ? ((double)a_max - (double)a_min) / (double)(p->na - 1) : 0.0;
     // maxBatch of integrate_diffraction.cu:160-161, times the block size
     const double diag = sqrt((double)((int64_t)p->nx * p->nx + (int64_t)p->ny * p->ny));
     d->kmax = (long long)ceil(diag / (p->dq_step * (double)p->nwt)) * (long long)p->nwt;
@@ -241,6 +244,7 @@ F32Consts make_f32_consts(const DevProblem &P)
     c.dEs = (float)P.dEs;
     c.qmin_t = (float)P.q_min;
     c.inv_dqt = P.dq_tab > 0 ? (float)(1.0 / P.dq_tab) : 0.f;
+    c.inv_dqg = P.dq_grid > 0 ? (float)(1.0 / P.dq_grid) : 0.f;
     const double NWT = (double)P.nwt;
     c.qpar_b = (float)P.dq0;
     c.qpar_a = (float)((P.q_hi - P.q_lo - P.dq0 * NWT) / (NWT * NWT));
@@ -555,15 +559,22 @@ constexpr int64_t kWalkTableBytes = (int64_t)4 << 30;
 
 // Shared body of xrdt_forward (rays == NULL: every ray, the Forward_XRD
 // layout) and xrdt_forward_rays (outputs per listed ray).
+// tab (the cross-section table path, xrdt_forward_tables): 0 = the fine-q
+// patterns Ifine; 1 = the coherent table S1, nearest bins; 2 = both tables
+// read bilinearly.
 int forward_impl(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, const float *Ifine,
                  const int32_t *seg, const float *a1, const float *a2, const float *S2, float q_min,
                  float q_max, float a_min, float a_max, const int64_t *ray_list, int64_t n_list,
-                 float *Nphotons, float *Cphotons, float *Amatrix, uint32_t flags)
+                 float *Nphotons, float *Cphotons, float *Amatrix, uint32_t flags, const float *S1 = nullptr,
+                 int tab = 0)
 {
     if (!ctx) return XRDT_ERR_NULL;
     ctx->err.clear();
-    if (!p || !spectrum || !Ifine || !seg || !a1 || !a2 || !S2 || !Nphotons || !Cphotons)
+    if (!p || !spectrum || (!Ifine && !tab) || (!S1 && tab) || !seg || !a1 || !a2 || !S2 || !Nphotons || !Cphotons)
         return fail(ctx, XRDT_ERR_NULL, "a required array pointer is NULL");
+    if (tab && (Amatrix || ray_list || (flags & XRDT_FWD_PLAIN_FP64)))
+        return fail(ctx, XRDT_ERR_UNSUPPORTED, "the table path computes Nphotons and Cphotons of every ray");
+    if (tab && (p->nq < 2 || p->na < 2)) return fail(ctx, XRDT_ERR_DIMS, "the table path needs NQ, NA >= 2");
     int rc = xrdt_problem_validate(p);
     if (rc) return fail(ctx, rc, fmt("problem rejected: %s", xrdt_status_string(rc)));
     if (flags & ~(XRDT_FWD_PLAIN_FP64 | XRDT_FWD_NO_SYNC))
@@ -598,7 +609,10 @@ int forward_impl(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, co
     // ---- inputs ----
     const void *d_spec, *d_ifine, *d_seg, *d_a1, *d_a2, *d_S2;
     if ((rc = stage_in(ctx, S_SPEC, spectrum, sizeof(float) * p->nrg_src * p->nrg_det, &d_spec))) return rc;
-    if ((rc = stage_in(ctx, S_IFINE, Ifine, sizeof(float) * (size_t)p->nqf * p->n_mat, &d_ifine))) return rc;
+    d_ifine = nullptr;
+    if (!tab && (rc = stage_in(ctx, S_IFINE, Ifine, sizeof(float) * (size_t)p->nqf * p->n_mat, &d_ifine))) return rc;
+    const void *d_S1 = nullptr;
+    if (tab && (rc = stage_in(ctx, S_S1, S1, sizeof(float) * (size_t)p->nq * p->na, &d_S1))) return rc;
     if ((rc = stage_in(ctx, S_SEG, seg, sizeof(int32_t) * nvox, &d_seg))) return rc;
     if ((rc = stage_in(ctx, S_A1, a1, sizeof(float) * nvox, &d_a1))) return rc;
     if ((rc = stage_in(ctx, S_A2, a2, sizeof(float) * nvox, &d_a2))) return rc;
@@ -635,6 +649,14 @@ int forward_impl(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, co
     if ((rc = get_buf(ctx, S_S2U8, (size_t)p->nq * p->na, &tmp))) return rc;
     B.s2u8 = (unsigned char *)tmp;
     B.atten_src = nullptr;
+    if (tab) {
+        if ((rc = get_buf(ctx, S_S1U8, (size_t)p->nq * p->na, &tmp))) return rc;
+        B.s1u8 = (unsigned char *)tmp;
+    }
+    if (tab == 2) {
+        if ((rc = get_buf(ctx, S_VTA, sizeof(float) * nvox, &tmp))) return rc;
+        B.vox_ta = (float *)tmp;
+    }
 
     { ProfScope ps(ctx, XRDT_KERNEL_PREP_VOXELS);
     CK(launch_prep_voxels(P, (const int32_t *)d_seg, (const float *)d_a1, (const float *)d_a2, B, st,
@@ -719,7 +741,8 @@ int forward_impl(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, co
         if ((rc = get_buf(ctx, S_ASRC, sizeof(float2) * (size_t)p->n_src * nv, &tmp))) return rc;
         B.atten_src = (float2 *)tmp;
         { ProfScope ps(ctx, XRDT_KERNEL_PREP_MAP);
-          CK(launch_prep_map(P, (const float *)d_a1, (const float *)d_a2, (const float *)d_S2, B, st, &ctx->launches)); }
+          CK(launch_prep_map(P, (const float *)d_a1, (const float *)d_a2, (const float *)d_S2, B, st, &ctx->launches,
+                             (const float *)d_S1)); }
         { ProfScope ps(ctx, XRDT_KERNEL_SRC_ATTEN);
           CK(launch_src_atten(P, (const SrcGeom *)d_srcg, nv, B, st, &ctx->launches)); }
         T.work = ctx->profiling ? ctx->d_work : nullptr;
@@ -743,7 +766,7 @@ int forward_impl(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, co
                 }
                 ProfScope ps(ctx, XRDT_KERNEL_FORWARD);
                 CK(launch_fast_forward(P, (const SrcGeom *)d_srcg, T, B, nv, (const float *)d_ifine, list, n_total,
-                                       p0, (int)n, (const float2 *)dtab, oN, oC, oA, st, &ctx->launches));
+                                       p0, (int)n, (const float2 *)dtab, oN, oC, oA, st, &ctx->launches, tab));
             }
             return XRDT_OK;
         };
@@ -802,6 +825,18 @@ int32_t xrdt_forward(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum
 {
     return forward_impl(ctx, p, spectrum, Ifine, seg, a1, a2, S2, q_min, q_max, a_min, a_max, nullptr, 0,
                         Nphotons, Cphotons, Amatrix, flags);
+}
+
+int32_t xrdt_forward_tables(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, const int32_t *seg,
+                            const float *a1, const float *a2, const float *S1, const float *S2, float q_min,
+                            float q_max, float a_min, float a_max, float *Nphotons, float *Cphotons,
+                            uint32_t flags)
+{
+    if (!ctx) return XRDT_ERR_NULL;
+    if (flags & ~(XRDT_TAB_BILINEAR | XRDT_FWD_NO_SYNC)) return fail(ctx, XRDT_ERR_UNSUPPORTED, "unknown flag bits");
+    const int tab = (flags & XRDT_TAB_BILINEAR) ? 2 : 1;
+    return forward_impl(ctx, p, spectrum, nullptr, seg, a1, a2, S2, q_min, q_max, a_min, a_max, nullptr, 0,
+                        Nphotons, Cphotons, nullptr, flags & XRDT_FWD_NO_SYNC, S1, tab);
 }
 
 int32_t xrdt_forward_rays(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum, const float *Ifine,

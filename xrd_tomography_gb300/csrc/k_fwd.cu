@@ -38,14 +38,14 @@ constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 
 struct Layout {
-    size_t en, rf, offse, winlo, wn, ifine, fq, cq, s2, tn, tns, cs, ck, ta, total;
+    size_t en, rf, offse, winlo, wn, ifine, fq, cq, s2, s1, tn, tns, cs, ck, ta, total;
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
 // Shared-memory layout; identical on host and device.
 __host__ __device__ inline Layout fwd_layout(const DevProblem &P, int E, int SL, int e_pass, bool with_n,
-                                             bool with_a)
+                                             bool with_a, int tab)
 {
     Layout L;
     const int W = 2 * P.dnrg + 1;
@@ -59,10 +59,11 @@ __host__ __device__ inline Layout fwd_layout(const DevProblem &P, int E, int SL,
     L.winlo = o; o = align16(o + sizeof(int) * P.nrg_det);
     L.wn = o; o = align16(o + sizeof(int) * 2 * E);
     L.cs = o; o = align16(o + sizeof(float) * kWarps * E * SL);
-    L.ifine = o; if (with_n) o = align16(o + sizeof(float) * P.n_mat * (P.nqf + 3));
-    L.fq = o; if (with_n) o = align16(o + sizeof(float2) * P.nqf);
+    L.ifine = o; if (with_n && !tab) o = align16(o + sizeof(float) * P.n_mat * (P.nqf + 3));
+    L.fq = o; if (with_n && !tab) o = align16(o + sizeof(float2) * P.nqf);
     L.cq = o; if (with_a) o = align16(o + sizeof(float4) * P.nwt);
     L.s2 = o; o = align16(o + sizeof(float) * (size_t)P.nq * P.na);
+    L.s1 = o; if (tab) o = align16(o + sizeof(float) * (size_t)P.nq * P.na);
     L.ta = o; if (with_a) o = align16(o + sizeof(float) * (size_t)e_pass * P.n_mat * P.nwt);
     L.total = o;
     return L;
@@ -77,6 +78,8 @@ struct FwdArgs {
     const float4 *cells;
     const float2 *atten_src;
     const unsigned char *s2u8;
+    const unsigned char *s1u8;   // the table path: the coherent table
+    const float *vox_ta;         // the table path, bilinear: the Compton column as a grid coordinate
     const float *Ifine;
     float *N, *C, *A;
     const int2 *pairs;         // a list of pairs, or NULL: the linear pairs src + det*SRC
@@ -88,7 +91,10 @@ struct FwdArgs {
     F32Consts c;
 };
 
-template <bool WITH_N, bool WITH_A>
+// TAB: 0 the coherent term from the materials' fine-q patterns
+// (integrate_diffraction.cu:299-308); 1 from the coherent table S1 by nearest
+// bin, 2 with both tables read bilinearly (the cross-section table path).
+template <bool WITH_N, bool WITH_A, int TAB>
 __global__ void __launch_bounds__(kThreads, 3)
 k_fwd(const FwdArgs args)
 {
@@ -99,7 +105,7 @@ k_fwd(const FwdArgs args)
     const int E = args.E;
     const int W = 2 * P.dnrg + 1;
     const int SL = args.sl;
-    const Layout L = fwd_layout(P, E, SL, args.e_pass, WITH_N, WITH_A);
+    const Layout L = fwd_layout(P, E, SL, args.e_pass, WITH_N, WITH_A, TAB);
     double *TN = (double *)(sm + L.tn);
     float2 *TNs = (float2 *)(sm + L.tns);
     float2 *Ck = (float2 *)(sm + L.ck);
@@ -117,6 +123,7 @@ k_fwd(const FwdArgs args)
     float2 *fq = (float2 *)(sm + L.fq);
     float4 *cq = (float4 *)(sm + L.cq);
     float *S2 = (float *)(sm + L.s2);   // quantised table as floats (no u8 conversion in the loop)
+    float *S1 = (float *)(sm + L.s1);   // the table path's coherent table, the same way
     float *TA = (float *)(sm + L.ta);
 
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -160,7 +167,7 @@ k_fwd(const FwdArgs args)
     for (int i = tid; i < kWarps * E * SL; i += kThreads) CS[i] = 0.f;
     for (int i = tid; i < P.nrg_det; i += kThreads) winlo[i] = args.T.win_lo[i];
     for (int i = tid; i < kWarps * P.nrg_det; i += kThreads) Ck[i] = make_float2(0.f, 0.f);
-    if (WITH_N) {
+    if (WITH_N && !TAB) {
         // rows of nqf + 3: each material's pattern and three zero pads
         for (int i = tid; i < P.n_mat * (P.nqf + 3); i += kThreads) {
             const int mm = i / (P.nqf + 3), j = i - mm * (P.nqf + 3);
@@ -171,12 +178,13 @@ k_fwd(const FwdArgs args)
     if (WITH_A)
         for (int i = tid; i < P.nwt; i += kThreads) cq[i] = args.T.coarse_q[i];
     for (int i = tid; i < P.nq * P.na; i += kThreads) S2[i] = (float)args.s2u8[i];
+    if (TAB)
+        for (int i = tid; i < P.nq * P.na; i += kThreads) S1[i] = (float)args.s1u8[i];
 
     // ---- per-(source, pixel) geometry, integrate_diffraction.cu:81-128 ----
     if (tid == 0) pair_geom(P, args.sg[src], det, &pair.G, &pair.Rdx, &pair.Rdy);
     const PairGeom &G = pair.G;
     const float rsqrt2pi = c.rsqrt2pi;
-    const float DQf = c.DQ;
     const float dqf_hi = c.dqf_hi, dqf_lo = c.dqf_lo;
     const float inv_dqf = c.inv_dqf, qlo_f = c.q_lo;
     const float kn0 = c.kn0, kn1 = c.kn1, kn2 = c.kn2;
@@ -209,6 +217,7 @@ k_fwd(const FwdArgs args)
             const float a2v = args.vox_a2[v];
             const float2 Asv = args.atten_src[(int64_t)src * nv + v];
             const float2 Adv = walk[v];
+            const float tav = TAB == 2 ? args.vox_ta[v] : 0.f;
 
             const int nin = min(32, nv - chunk * 32);
             for (int i = 0; i < nin; i++) {
@@ -228,6 +237,7 @@ k_fwd(const FwdArgs args)
                 const float a2now = __shfl_sync(0xffffffffu, a2v, i);
                 const float Asx = __shfl_sync(0xffffffffu, Asv.x, i);
                 const float Asy = __shfl_sync(0xffffffffu, Asv.y, i);
+                const float ta = TAB == 2 ? __shfl_sync(0xffffffffu, tav, i) : 0.f;
                 const float s2f = sh * sh;
                 const float sg_s2 = __fdividef(sg, s2f);
 #pragma unroll 1
@@ -256,7 +266,24 @@ k_fwd(const FwdArgs args)
                     nexp += 1;
                     const float pref = PP * Wg * rsqrt2pi * rs;
                     const float half = kSig * sig2 * rs;
-                    if (WITH_N) {
+                    if (WITH_N && TAB) {
+                        // the coherent term from the table S1 (the reference's
+                        // commented-out kernel, integrate_diffraction.cu:703-719):
+                        // Pin Pout geom Rayleigh a2 S1[wvt bin, a-ratio bin] with
+                        // wvt = ein sin(theta/2) on the tables' log2 axis
+                        const float ein = en_ein[el];
+                        float s1v;
+                        if (TAB == 1) {
+                            s1v = S1[coherent_bin(P, ein, sh, oh, ol, args.T.energy[lo_e + el].ein, qmin_t, inv_dqt) +
+                                     na * P.nq];
+                        } else {
+                            s1v = table_bilinear(S1, P.nq, P.na, (lg2_approx(ein * sh) - qmin_t) * c.inv_dqg, ta);
+                        }
+                        float2 k = TNw[el];
+                        kahan_add(k.x, k.y, PP * Wg * a2now * s1v);
+                        TNw[el] = k;
+                    }
+                    if (WITH_N && !TAB) {
                         const float jc = (w_hi - qlo_f) * inv_dqf - 0.5f;
                         // bounded floors: the indices are clamped to the grid and an
                         // empty window is skipped
@@ -341,8 +368,18 @@ k_fwd(const FwdArgs args)
                         }
                         const int n1 = min(wn[2 * el + 1], floor_bounded(((Eo_lo + dEsf) * inv_er - edmin) * inv_dEd));
                         if (n0 <= n1) {
-                            const int nq = compton_bin(P, ein, eratio, inv_er, sh, oh, ol, args.T.energy[eg].ein,
-                                                       qmin_t, inv_dqt);
+                            // the table's value: nearest bin, or bilinear in the table path
+                            float s2v;
+                            if (TAB == 2) {
+                                const float wC = ein * sh;
+                                const float arg = eratio + wC * wC;
+                                const float l2 = lg2_approx(wC * arg * rsqrt_approx(arg) * inv_er);
+                                s2v = table_bilinear(S2, P.nq, P.na, (l2 - qmin_t) * c.inv_dqg, ta);
+                            } else {
+                                s2v = S2[compton_bin(P, ein, eratio, inv_er, sh, oh, ol, args.T.energy[eg].ein, qmin_t,
+                                                     inv_dqt) +
+                                         na * P.nq];
+                            }
                             // Pc = exp(-(Xin + Xc)) with Xc the source-side exponent at
                             // the outgoing energy eout = ein / eratio, formed as the
                             // Rayleigh one plus the small Compton change, so that Pc
@@ -359,7 +396,7 @@ k_fwd(const FwdArgs args)
                             nexp += 1;
                             // an underflowed Pc adds exact zeros below: no branch
                             const float Cf = eratio * eratio * (eratio + inv_er - 1.f + cos2) * 0.5f;
-                            const float base = Pc * gp * Cf * a2now * S2[nq + na * P.nq];
+                            const float base = Pc * gp * Cf * a2now * s2v;
                             const float span = dEsf * inv_er;   // Eout2 - Eout1
                             const float inv_span = rcp_approx(span);
                             // this lane's (warp, energy) row of chunk sums, indexed by n;
@@ -467,12 +504,12 @@ k_fwd(const FwdArgs args)
     }
 }
 
-template <bool WN, bool WA>
+template <bool WN, bool WA, int TAB>
 cudaError_t launch_variant(const FwdArgs &a, size_t smem, cudaStream_t s)
 {
-    cudaError_t e = cudaFuncSetAttribute(k_fwd<WN, WA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_fwd<WN, WA, TAB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_fwd<WN, WA><<<(unsigned)a.n_pairs, kThreads, smem, s>>>(a);
+    k_fwd<WN, WA, TAB><<<(unsigned)a.n_pairs, kThreads, smem, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -502,17 +539,19 @@ cudaError_t launch_gather_rays(const int64_t *idx, int64_t n, const float *Nc, c
     return cudaGetLastError();
 }
 
-size_t fast_forward_smem(const DevProblem &P, int sl, int e_pass, bool with_n, bool with_a)
+size_t fast_forward_smem(const DevProblem &P, int sl, int e_pass, bool with_n, bool with_a, int tab)
 {
     const int E = P.e_hi - P.e_lo + 1;
-    return fwd_layout(P, E, sl, e_pass, with_n, with_a).total;
+    return fwd_layout(P, E, sl, e_pass, with_n, with_a, tab).total;
 }
 
 cudaError_t launch_fast_forward(const DevProblem &P, const SrcGeom *d_src, const FwdTables &T,
                                 const PrepBuffers &B, int nv, const float *Ifine, const int2 *pairs,
                                 long long n_list, long long p0, int n_pairs, const float2 *walk, float *N,
-                                float *C, float *A, cudaStream_t s, int64_t *launches)
+                                float *C, float *A, cudaStream_t s, int64_t *launches, int tab)
 {
+    // the table path computes Nphotons and Cphotons only
+    if (tab && (A || !N || tab > 2 || !B.s1u8 || (tab == 2 && !B.vox_ta))) return cudaErrorInvalidValue;
     FwdArgs a;
     a.pairs = pairs;
     a.p0 = p0;
@@ -529,6 +568,8 @@ cudaError_t launch_fast_forward(const DevProblem &P, const SrcGeom *d_src, const
     a.cells = B.cells;
     a.atten_src = B.atten_src;
     a.s2u8 = B.s2u8;
+    a.s1u8 = B.s1u8;
+    a.vox_ta = B.vox_ta;
     a.Ifine = Ifine;
     a.N = N;
     a.C = C;
@@ -543,10 +584,10 @@ cudaError_t launch_fast_forward(const DevProblem &P, const SrcGeom *d_src, const
     // would push the block past ~110 KB of shared memory
     int e_pass = a.E;
     if (with_a) {
-        while (e_pass > 1 && fwd_layout(P, a.E, a.sl, e_pass, with_n, true).total > 110 * 1024) e_pass = (e_pass + 1) / 2;
+        while (e_pass > 1 && fwd_layout(P, a.E, a.sl, e_pass, with_n, true, 0).total > 110 * 1024) e_pass = (e_pass + 1) / 2;
     }
     a.e_pass = e_pass;
-    const size_t smem = fwd_layout(P, a.E, a.sl, e_pass, with_n, with_a).total;
+    const size_t smem = fwd_layout(P, a.E, a.sl, e_pass, with_n, with_a, tab).total;
     if (smem + sizeof(PairRec) > 227 * 1024) return cudaErrorInvalidConfiguration;   // dynamic + static
     if (launches) (*launches)++;
     if (nv == 0) {
@@ -554,10 +595,12 @@ cudaError_t launch_fast_forward(const DevProblem &P, const SrcGeom *d_src, const
         cudaError_t e = cudaSuccess;
         return e;
     }
-    if (with_n && with_a) return launch_variant<true, true>(a, smem, s);
-    if (with_n) return launch_variant<true, false>(a, smem, s);
-    if (with_a) return launch_variant<false, true>(a, smem, s);
-    return launch_variant<false, false>(a, smem, s);
+    if (tab == 1) return launch_variant<true, false, 1>(a, smem, s);
+    if (tab == 2) return launch_variant<true, false, 2>(a, smem, s);
+    if (with_n && with_a) return launch_variant<true, true, 0>(a, smem, s);
+    if (with_n) return launch_variant<true, false, 0>(a, smem, s);
+    if (with_a) return launch_variant<false, true, 0>(a, smem, s);
+    return launch_variant<false, false, 0>(a, smem, s);
 }
 
 } // namespace xrdt

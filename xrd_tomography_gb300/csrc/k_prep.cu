@@ -26,7 +26,8 @@ namespace {
 
 __global__ void k_build_cells(int nx, int ny, const float *__restrict__ a1, const float *__restrict__ a2,
                               float4 *__restrict__ cells, const float *__restrict__ S2,
-                              unsigned char *__restrict__ s2u8, int ns2)
+                              unsigned char *__restrict__ s2u8, int ns2, const float *__restrict__ S1,
+                              unsigned char *__restrict__ s1u8)
 {
     const int64_t ncell = (int64_t)(nx + 1) * (ny + 1);
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -64,6 +65,10 @@ __global__ void k_build_cells(int nx, int ny, const float *__restrict__ a1, cons
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ns2; i += stride) {
         const int q = floor_to_int((double)S2[i]);
         s2u8[i] = (unsigned char)(q < 0 ? 0 : (q > 255 ? 255 : q));
+        if (S1) {
+            const int q1 = floor_to_int((double)S1[i]);
+            s1u8[i] = (unsigned char)(q1 < 0 ? 0 : (q1 > 255 ? 255 : q1));
+        }
     }
 }
 
@@ -116,7 +121,7 @@ k_compact_voxels(int nx, int ny, int n_mat, const int32_t *__restrict__ seg, int
 
 __global__ void k_voxel_compton(DevProblem P, const float *__restrict__ a1, const float *__restrict__ a2,
                                 const int *__restrict__ vox_xy, const int *__restrict__ counters,
-                                int *__restrict__ vox_na, float *__restrict__ vox_a2)
+                                int *__restrict__ vox_na, float *__restrict__ vox_a2, float *__restrict__ vox_ta)
 {
     const int nv = counters[0];
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
@@ -129,9 +134,11 @@ __global__ void k_voxel_compton(DevProblem P, const float *__restrict__ a1, cons
         }
         double a1now, a2now;
         bilinear_f64(a1, a2, P.nx, P.ny, sx, sy, &a1now, &a2now);
-        int na = floor_to_int((log2(fabs(a1now / a2now)) - P.a_min) / P.da_tab);
+        const double l2a = log2(fabs(a1now / a2now));
+        int na = floor_to_int((l2a - P.a_min) / P.da_tab);
         vox_na[v] = na < 0 ? 0 : (na >= P.na ? P.na - 1 : na);
         vox_a2[v] = (float)a2now;
+        if (vox_ta) vox_ta[v] = (float)((l2a - P.a_min) / P.da_grid);   // clamped where it is used
     }
 }
 
@@ -158,12 +165,13 @@ __global__ void k_src_atten(DevProblem P, const SrcGeom *__restrict__ sg, const 
 } // namespace
 
 cudaError_t launch_prep_map(const DevProblem &P, const float *a1, const float *a2, const float *S2,
-                            PrepBuffers &B, cudaStream_t s, int64_t *launches)
+                            PrepBuffers &B, cudaStream_t s, int64_t *launches, const float *S1)
 {
     const int64_t ncell = (int64_t)(P.nx + 1) * (P.ny + 1);
     int blocks = (int)((ncell + 255) / 256);
     if (blocks > 4096) blocks = 4096;
-    k_build_cells<<<blocks, 256, 0, s>>>(P.nx, P.ny, a1, a2, B.cells, S2, B.s2u8, P.nq * P.na);
+    k_build_cells<<<blocks, 256, 0, s>>>(P.nx, P.ny, a1, a2, B.cells, S2, B.s2u8, S2 ? P.nq * P.na : 0,
+                                         B.s1u8 ? S1 : nullptr, B.s1u8);
     if (launches) (*launches)++;
     return cudaGetLastError();
 }
@@ -175,7 +183,7 @@ cudaError_t launch_prep_voxels(const DevProblem &P, const int32_t *seg, const fl
     const int64_t nvox = (int64_t)P.nx * P.ny;
     int blocks = (int)((nvox + 255) / 256);
     if (blocks > 2048) blocks = 2048;
-    k_voxel_compton<<<blocks, 256, 0, s>>>(P, a1, a2, B.vox_xy, B.counters, B.vox_na, B.vox_a2);
+    k_voxel_compton<<<blocks, 256, 0, s>>>(P, a1, a2, B.vox_xy, B.counters, B.vox_na, B.vox_a2, B.vox_ta);
     if (launches) (*launches) += 2;
     return cudaGetLastError();
 }

@@ -183,6 +183,45 @@ __device__ __forceinline__ int compton_bin(const DevProblem &P, float ein, float
     return nq < 0 ? 0 : (nq >= P.nq ? P.nq - 1 : nq);
 }
 
+// The cross-section table path (code the reference keeps commented out,
+// integrate_diffraction.cu:703-719): the coherent table's wavevector bin
+// nq = floor((log2(w) - q_min) / dq) with w = ein sin(theta/2), clamped to
+// [0, NQ), decided in FP32 from the hi part of sin(theta/2); within 2e-4 of a
+// bin edge again in FP64 from 1 - cos(theta) (pair (oh, ol)).
+__device__ __noinline__ int coherent_bin_f64(const DevProblem &P, double ein, float omc_hi, float omc_lo)
+{
+    const double omcd = (double)omc_hi + (double)omc_lo;
+    const double sd = sqrt(fabs(omcd) / 2.0);
+    return floor_to_int((log2(ein * sd) - P.q_min) / P.dq_tab);
+}
+
+__device__ __forceinline__ int coherent_bin(const DevProblem &P, float ein, float sh, float oh, float ol,
+                                            double ein_d, float qmin_t, float inv_dqt)
+{
+    const float tq = (lg2_approx(ein * sh) - qmin_t) * inv_dqt;
+    float ftq;
+    int nq = floor_bounded(tq, &ftq);   // clamped to the table below
+    const float fr = tq - ftq;
+    if (!(fr > 2e-4f && fr < 1.f - 2e-4f)) nq = coherent_bin_f64(P, ein_d, oh, ol);
+    return nq < 0 ? 0 : (nq >= P.nq ? P.nq - 1 : nq);
+}
+
+// Bilinear value of a table [nq, na] (index q + a*nq, values as floats) at
+// grid coordinates (tq, ta): the grid points are the table's entries,
+// q_min + i (q_max - q_min)/(NQ - 1) (XSection_builder.m:121-125); clamped to
+// the table (a NaN coordinate reads the first row or column).
+__device__ __forceinline__ float table_bilinear(const float *S, int nq, int na, float tq, float ta)
+{
+    tq = fminf(fmaxf(tq, 0.f), (float)(nq - 1));
+    ta = fminf(fmaxf(ta, 0.f), (float)(na - 1));
+    const int i = min((int)tq, nq - 2), j = min((int)ta, na - 2);
+    const float f = tq - (float)i, g = ta - (float)j;
+    const float *r0 = S + i + j * nq, *r1 = r0 + nq;
+    const float lo = fmaf(f, r0[1] - r0[0], r0[0]);
+    const float hi = fmaf(f, r1[1] - r1[0], r1[0]);
+    return fmaf(g, hi - lo, lo);
+}
+
 // FP64 walk set-up out of line: the rare fallback of walk_setup_f32 stays a
 // real branch instead of being predicated into the caller's loop.
 __device__ __noinline__ void walk_setup_f64(const DevProblem &P, double ex, double ey, double vx, double vy,

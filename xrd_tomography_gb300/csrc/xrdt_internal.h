@@ -28,6 +28,7 @@ struct DevProblem {
     double cx, cy, r_src, r_det, col_pitch, row_pitch, z0, focal, geomAdet, vox;
     double tan_half, tan_full, sta, cta;
     double q_min, q_max, a_min, a_max, dq_tab, da_tab;
+    double dq_grid, da_grid;   // spacing of the tables' grid points (bilinear lookups)
 };
 
 // FP32 copies of the problem constants that the FP32 kernels use inside
@@ -41,7 +42,7 @@ struct F32Consts {
     float dqf_hi, dqf_lo, inv_dqf, q_lo, q_hi;
     float kn0, kn1, kn2;
     float edmin, inv_dEd, dEd, dEs;
-    float qmin_t, inv_dqt;
+    float qmin_t, inv_dqt, inv_dqg;
     float qpar_a, qpar_b;   // coarse bin edges: edge(n) = q_lo + qpar_b n + qpar_a n^2
 };
 F32Consts make_f32_consts(const DevProblem &P);
@@ -113,17 +114,21 @@ cudaError_t launch_basis_expand(const float *C, long long M, int K, const float 
 
 // k_prep.cu
 struct PrepBuffers {
-    float4 *cells;          // [2][(ny+1)*(nx+1)*2] bilinear cells, row- then column-major
-    int *vox_xy;            // [nx*ny] packed x | y << 16 of non-empty voxels
-    int *vox_mat;           // [nx*ny]
-    int *vox_na;            // [nx*ny] Compton table column per voxel
-    float *vox_a2;          // [nx*ny] a2 used by the Compton term
-    int *counters;          // [0] = number of non-empty voxels, [1] = bad material flag
-    float2 *atten_src;      // [n_src * nv] source-side line integrals
-    unsigned char *s2u8;    // [nq*na]
+    float4 *cells = nullptr;          // [2][(ny+1)*(nx+1)*2] bilinear cells, row- then column-major
+    int *vox_xy = nullptr;            // [nx*ny] packed x | y << 16 of non-empty voxels
+    int *vox_mat = nullptr;           // [nx*ny]
+    int *vox_na = nullptr;            // [nx*ny] Compton table column per voxel
+    float *vox_a2 = nullptr;          // [nx*ny] a2 used by the Compton term
+    float *vox_ta = nullptr;          // [nx*ny] the same column as a grid coordinate (bilinear lookups), or NULL
+    int *counters = nullptr;          // [0] = number of non-empty voxels, [1] = bad material flag
+    float2 *atten_src = nullptr;      // [n_src * nv] source-side line integrals
+    unsigned char *s2u8 = nullptr;    // [nq*na]
+    unsigned char *s1u8 = nullptr;    // [nq*na] the coherent table of the table path, or NULL
 };
+// S1 (with B.s1u8): the coherent table, quantised like S2.
 cudaError_t launch_prep_map(const DevProblem &P, const float *a1, const float *a2,
-                            const float *S2, PrepBuffers &B, cudaStream_t s, int64_t *launches);
+                            const float *S2, PrepBuffers &B, cudaStream_t s, int64_t *launches,
+                            const float *S1 = nullptr);
 cudaError_t launch_prep_voxels(const DevProblem &P, const int32_t *seg, const float *a1,
                                const float *a2, PrepBuffers &B, cudaStream_t s, int64_t *launches);
 cudaError_t launch_src_atten(const DevProblem &P, const SrcGeom *d_src, int nv, PrepBuffers &B,
@@ -142,7 +147,7 @@ struct FwdTables {
     const float4 *coarse_q;    // [nwt] (q_hi, q_lo, dq, 0)
     unsigned long long *work;  // nullable: counts the exp2 evaluations
 };
-size_t fast_forward_smem(const DevProblem &P, int sl, int e_pass, bool with_n, bool with_a);
+size_t fast_forward_smem(const DevProblem &P, int sl, int e_pass, bool with_n, bool with_a, int tab = 0);
 // n_pairs blocks, block b on pair p0 + b: of the list pairs[0 .. n_list)
 // when it is given (outputs then go to the compact layout [nrg_det][n_list],
 // and [nrg_det][n_list][n_mat*nwt] for A), else of the linear index
@@ -152,7 +157,7 @@ cudaError_t launch_fast_forward(const DevProblem &P, const SrcGeom *d_src, const
                                 const PrepBuffers &B, int nv, const float *Ifine,
                                 const int2 *pairs, long long n_list, long long p0, int n_pairs,
                                 const float2 *walk, float *N, float *C, float *A, cudaStream_t s,
-                                int64_t *launches);
+                                int64_t *launches, int tab = 0);
 // k_spectrum.cu: the spectrum-response matrix (spectrum_builder.m:64-95).
 // A fine bin: edges, centre, 1/(2 sigma^2) and n/(sqrt(2 pi) sigma); a coarse
 // bin: edges and the range [h0, h1) of fine bins that overlap it.

@@ -135,6 +135,24 @@ def hd_spectrum(kvp=80.0, e_min=8.0, de=0.05, n=1440, lines=((59.3, 0.35), (67.2
     return edges.astype(np.float32), N.astype(np.float32)
 
 
+def coherent_table(inp: "Inputs", seed: int = 0) -> np.ndarray:
+    """A synthetic coherent cross-section table S1 [NQ, NA] (index q + a*NQ)
+    on the 0..255 scale of XSection_builder.m:113-119: the form-factor-like
+    fall with the wavevector transfer of coherent scattering, modulated along
+    the a-ratio axis, with a little noise and one entry below and one above
+    the u8 range."""
+    p = inp.problem
+    rng = np.random.default_rng(SEED_BASE + 500 + seed)
+    qq = np.linspace(0.0, 1.0, p.nq)[:, None]
+    aa = np.linspace(0.0, 1.0, p.na)[None, :]
+    ph = rng.uniform(0, 2 * math.pi, 2)
+    t = np.exp(-2.5 * qq) * (0.75 + 0.2 * np.cos(2.7 * aa + ph[0])) + 0.05 * np.sin(7.0 * qq + ph[1]) * aa
+    S = 255.0 * np.clip(t, 0.0, None) + rng.uniform(-0.5, 0.5, (p.nq, p.na))
+    S[1, 0] = -2.0
+    S[0, -1] = 258.5
+    return S.astype(np.float32).flatten(order="F")
+
+
 def _s2_table(rng, nq, na):
     qq = np.linspace(0.0, 1.0, nq)[:, None]
     aa = np.linspace(0.0, 1.0, na)[None, :]
