@@ -1,6 +1,8 @@
 """The spectrum-response builder (spectrum_builder.m:64-95): the oracle's
 matrix form against the reference's literal double loop, a conservation
 property (CPU), and the CUDA builder against the oracle (GPU)."""
+import os
+
 import numpy as np
 import pytest
 
@@ -68,10 +70,18 @@ def ctx():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("grids", ["reference", "rectangular", "irregular"])
+@pytest.mark.parametrize("grids", ["reference", "rectangular", "irregular", "measured"])
 def test_spectrum_build_matches_oracle(ctx, grids):
     rng = np.random.default_rng(3)
-    if grids == "reference":
+    if grids == "measured":
+        # the reference's measured 80 kVp spectrum (Spectrum_80kVp/spectral_data_HD.mat,
+        # read by xrd_tomography_gb300.matfile into tests/golden/real_inputs.npz): its
+        # 1441 edges and the counts of the 1440 bins (spectrum_builder.m:26-30)
+        fx = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "real_inputs.npz"))
+        e = fx["spectrum_energy"].astype(np.float32)
+        n = fx["spectrum_counts"][:-1].astype(np.float32)
+        src = det = np.linspace(8.0, 80.0, 65).astype(np.float32)
+    elif grids == "reference":
         # the reference's grid: 1440 bins of 0.05 keV, 64 coarse bins over 8-80 keV
         e, n = synth.hd_spectrum()
         src = det = np.linspace(8.0, 80.0, 65).astype(np.float32)
