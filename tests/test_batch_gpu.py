@@ -62,11 +62,25 @@ def test_batch_matches_single_operators_and_oracle(ctx, torch_cuda, oracle_lib):
         assert torch.equal(ys[k], y1), k
         # the adjoint's pair groups differ: the partial sums add in another order
         assert max_rel_err(gs[k].cpu().numpy(), g1.cpu().numpy()) < FAST_RTOL, k
-    inp = inps[0]
-    rays = np.arange(inp.problem.rays)
-    y_ref, g_ref = oracle_lib.vox_rays(inp, rays, x=xs[0].cpu().numpy(), w=ws[0].cpu().numpy())
-    assert max_rel_err(ys[0].cpu().numpy(), y_ref) < FAST_RTOL
-    assert max_rel_err(gs[0].cpu().numpy(), g_ref.reshape(-1)) < FAST_RTOL
+    # every problem of the batch against the oracle: the batch forward on
+    # sampled rays (all of the tiny problem's), and the batch adjoint of
+    # weights that are zero off those rays
+    sel = [np.arange(inps[0].problem.rays)]
+    sel += [np.sort(np.random.default_rng(40 + k).choice(inp.problem.rays, 48, replace=False))
+            for k, inp in enumerate(inps[1:], 1)]
+    wsp = []
+    for k, inp in enumerate(inps):
+        idx = torch.from_numpy(sel[k]).cuda()
+        w = torch.zeros(inp.problem.rays, device="cuda")
+        w[idx] = ws[k][idx]
+        wsp.append(w)
+    gsp = [torch.empty(op.unknowns, device="cuda") for op in ops]
+    batch.adjoint(wsp, gsp)
+    torch.cuda.synchronize()
+    for k, inp in enumerate(inps):
+        y_ref, g_ref = oracle_lib.vox_rays(inp, sel[k], x=xs[k].cpu().numpy(), w=wsp[k].cpu().numpy()[sel[k]])
+        assert max_rel_err(ys[k].cpu().numpy()[sel[k]], y_ref) < FAST_RTOL, k
+        assert max_rel_err(gsp[k].cpu().numpy(), g_ref.reshape(-1)) < FAST_RTOL, k
     warps, tiles, fgrid, agrid = batch.tune()
     assert warps in (1, 2, 4) and tiles >= 1 and fgrid >= 1 and agrid >= 1
     # a second batch of the same shapes reads the choice from the cache file
