@@ -205,7 +205,7 @@ int32_t xrdt_forward_rays(xrdt_ctx *ctx, const xrdt_problem *p,
 /* The cross-section table path: the forward model with the coherent
  * (Rayleigh) term read from a tabulated cross-section S1 [NQ, NA] instead of
  * the materials' fine-q patterns -- the form the reference keeps commented
- * out after its kernel (integrate_diffraction.cu:416-418, 479-494, 703-719;
+ * out after its kernel (integrate_diffraction.cu:416-418, 479-494, 701-719;
  * tables from XSection_builder.m:93-128):
  *   Nphotons[ray] = sum_v sum_{e in window} RF[e,nrg] Pin Pout geom
  *                   Rayleigh(theta) a2(v) S1[nq, na]

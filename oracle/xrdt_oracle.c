@@ -373,7 +373,7 @@ static void forward_one_ray(const xrdt_problem *p, const float *spectrum, const 
 
                 /* Coherent term from the S1 table instead (the reference's
                  * commented-out kernel, integrate_diffraction.cu:716-719 with
-                 * the bin of :703-707): wvt = ein sin(theta/2) on the log2
+                 * the bin of :701-707): wvt = ein sin(theta/2) on the log2
                  * axis of the tables (XSection_builder.m:106). */
                 if (want_nc && tab) {
                     double wc = ein * sinthetahalf;

@@ -62,7 +62,7 @@ int32_t xrdt_oracle_forward_rays(const xrdt_problem *p,
  * with w [n_rays] it writes g_out[v][k] = sum_i w[i] Av[rays[i]][v][k].  Either
  * pair may be NULL.  Returns 0, or a negative value for invalid input. */
 /* The cross-section table path: the coherent term from the table S1
- * (integrate_diffraction.cu:703-719, code the reference keeps commented out)
+ * (integrate_diffraction.cu:701-719, code the reference keeps commented out)
  * instead of the fine-q pattern sum, and both tables read by nearest bin or,
  * with bilinear != 0, bilinearly between the grid points of
  * XSection_builder.m:121-125. */

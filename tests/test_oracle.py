@@ -187,7 +187,7 @@ def test_oracle_ct_limits(oracle_lib):
 
 
 def test_table_path_restatement(oracle_lib):
-    """The oracle's cross-section table path (integrate_diffraction.cu:703-719,
+    """The oracle's cross-section table path (integrate_diffraction.cu:701-719,
     commented out in the reference): with nearest lookups its Compton counts
     are the forward's; a constant coherent table gives the same coherent
     counts by nearest and bilinear lookup; and a coherent table that is

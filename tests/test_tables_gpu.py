@@ -1,7 +1,7 @@
 """The cross-section table path (xrdt_forward_tables): the coherent term read
 from the tabulated cross-section S1 instead of the materials' fine-q patterns,
 the form the reference keeps commented out after its kernel
-(integrate_diffraction.cu:416-418, 479-494, 703-719), with nearest-bin or
+(integrate_diffraction.cu:416-418, 479-494, 701-719), with nearest-bin or
 bilinear lookups of both tables, against the FP64 oracle's restatement of the
 same lines (the commented-out code itself does not compile: it names an
 energy_channel function and NPSI spectra the reference does not define)."""

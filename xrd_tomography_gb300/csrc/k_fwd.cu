@@ -268,7 +268,7 @@ k_fwd(const FwdArgs args)
                     const float half = kSig * sig2 * rs;
                     if (WITH_N && TAB) {
                         // the coherent term from the table S1 (the reference's
-                        // commented-out kernel, integrate_diffraction.cu:703-719):
+                        // commented-out kernel, integrate_diffraction.cu:701-719):
                         // Pin Pout geom Rayleigh a2 S1[wvt bin, a-ratio bin] with
                         // wvt = ein sin(theta/2) on the tables' log2 axis
                         const float ein = en_ein[el];

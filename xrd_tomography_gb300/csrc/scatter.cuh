@@ -184,7 +184,7 @@ __device__ __forceinline__ int compton_bin(const DevProblem &P, float ein, float
 }
 
 // The cross-section table path (code the reference keeps commented out,
-// integrate_diffraction.cu:703-719): the coherent table's wavevector bin
+// integrate_diffraction.cu:701-719): the coherent table's wavevector bin
 // nq = floor((log2(w) - q_min) / dq) with w = ein sin(theta/2), clamped to
 // [0, NQ), decided in FP32 from the hi part of sin(theta/2); within 2e-4 of a
 // bin edge again in FP64 from 1 - cos(theta) (pair (oh, ol)).
