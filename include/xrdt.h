@@ -342,7 +342,10 @@ int32_t xrdt_mlem_checkpoint_read(const char *path, float *x, int64_t n, int64_t
  * calls synchronise the context's stream before they return.  The context
  * must outlive the operator. */
 typedef struct xrdt_op xrdt_op;
-/* Requires NWT <= 1024 and at most 128 source bins in the spectrum windows. */
+/* Requires NWT <= 1024, at most 128 source bins in the spectrum windows, and
+ * the adjoint's compensated sums of 32 voxels (256 NWT bytes) within one
+ * block's shared memory, i.e. NWT up to about 840 on this GPU; otherwise
+ * XRDT_ERR_UNSUPPORTED. */
 int32_t xrdt_op_create(xrdt_ctx *ctx, const xrdt_problem *p, const float *spectrum,
                        const int32_t *seg, const float *a1, const float *a2,
                        xrdt_op **op);

@@ -308,3 +308,36 @@ def test_launches_are_counted(ctx):
     before = ctx.launches
     xt.forward(inp.problem, *inp.args(), ctx=ctx)
     assert ctx.launches - before >= 4
+
+
+def wide_window_problem(n_src_bins):
+    """The tiny problem's phantom and scanner with n_src_bins source energy
+    bins over 16 detector bins (windows of 11 source bins 8 apart): the
+    detector windows together span all source bins."""
+    p = synth._base(12, 12, 4, 8, 1, n_src_bins, 16, (20.0, 80.0), (20.0, 80.0), 5,
+                    32, 64, 3, 16, 16, (0.5, 4.0), 0.03)
+    return synth.scanner(p, vox_mm=4.0, r_src_mm=150.0, r_det_mm=120.0, col_mm=4.0, row_mm=2.0,
+                         z0_mm=12.0, focal_mm=1.0)
+
+
+def test_widest_energy_windows(ctx, oracle_lib):
+    """128 source bins inside the detector windows, the most the projector
+    and the per-voxel operator take (one shared-memory row per bin): every
+    ray against the oracle; 130 bins are rejected."""
+    inp = synth.make_inputs(wide_window_problem(128), 13)
+    p = inp.problem
+    N, C, A = xt.forward(p, *inp.args(), ctx=ctx)
+    rays = np.arange(p.rays)
+    No, Co, Ao, _ = oracle_lib.forward_rays(inp, rays, want_a=True)
+    assert max_rel_err(N, No) < FAST_RTOL
+    assert max_rel_err(C, Co) < FAST_RTOL
+    assert max_rel_err(np.asarray(A).reshape(Ao.shape), Ao) < FAST_RTOL
+    op = xt.Operator(p, inp.spectrum, inp.seg, inp.a1, inp.a2, ctx=ctx)
+    x = np.random.default_rng(5).uniform(0.0, 1.0, (p.nx * p.ny, p.nwt)).astype(np.float32)
+    x[np.asarray(inp.seg).reshape(-1) == 0] = 0.0
+    y_ref, _ = oracle_lib.vox_rays(inp, rays, x=x.reshape(-1))
+    assert max_rel_err(op.forward(x.reshape(-1)), y_ref) < FAST_RTOL
+    op.close()
+    wide = synth.make_inputs(wide_window_problem(130), 13)
+    with pytest.raises(xt.XrdtError):
+        xt.forward(wide.problem, *wide.args(), want_amatrix=False, ctx=ctx)

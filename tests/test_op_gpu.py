@@ -405,3 +405,28 @@ def test_reference_configuration_operator(ctx, oracle_lib):
     yv = op.forward(xv.reshape(-1))
     assert max_rel_err(yv[gold_rays], np.einsum("rmk,mk->r", A_gold, xm)) < FAST_RTOL
     op.close()
+
+
+def test_widest_coarse_grid(ctx, oracle_lib):
+    """768 coarse q bins: the adjoint then fits one warp per block (its
+    compensated sums take 192 KB of shared memory); forward and adjoint of
+    every ray against the oracle.  1024 bins exceed a block and are
+    rejected."""
+    def problem(nwt):
+        p = synth._base(12, 12, 4, 8, 1, 12, 12, (20.0, 80.0), (20.0, 80.0), 2,
+                        nwt, 64, 3, 16, 16, (0.5, 4.0), 0.001)
+        return synth.scanner(p, vox_mm=4.0, r_src_mm=150.0, r_det_mm=120.0, col_mm=4.0, row_mm=2.0,
+                             z0_mm=12.0, focal_mm=1.0)
+    inp = synth.make_inputs(problem(768), 7)
+    p = inp.problem
+    op = make_op(inp, ctx)
+    x = rand_x(inp, 1)
+    rays = np.arange(p.rays)
+    w = np.random.default_rng(2).uniform(0.0, 2.0, p.rays).astype(np.float32)
+    y_ref, g_ref = oracle_lib.vox_rays(inp, rays, x=x, w=w)
+    assert max_rel_err(op.forward(x), y_ref) < FAST_RTOL
+    assert max_rel_err(op.adjoint(w), g_ref.reshape(-1)) < FAST_RTOL
+    op.close()
+    big = synth.make_inputs(problem(1024), 7)
+    with pytest.raises(xt.XrdtError):
+        make_op(big, ctx)
