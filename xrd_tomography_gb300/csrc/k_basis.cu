@@ -112,17 +112,29 @@ __device__ __forceinline__ ChunkPos chunk_pos(int j, int wid, int lane, int K)
     return p;
 }
 
+// BULK: the tiles of C come through the bulk-copy engine into a ring of
+// `stages` shared-memory stages (a tile's rows are contiguous in C: one
+// cp.async.bulk per tile, completing on the stage's mbarrier), so that
+// several tiles are in flight per CTA without holding them in registers; C
+// must be 16-byte aligned.  Otherwise each thread loads its chunks of the
+// next tile into registers.
+template <bool BULK>
 __global__ void __launch_bounds__(kBasisThreads)
 k_basis_expand(const float *__restrict__ C, long long M, int K, const float *__restrict__ B, int N,
-               float *__restrict__ I, unsigned *__restrict__ err, int aligned, int aligned_b, int test_timeout)
+               float *__restrict__ I, unsigned *__restrict__ err, int aligned, int aligned_b, int test_timeout,
+               int stages)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
     const int a_bytes = kTileM * K * 4, b_bytes = N * K * 4;
+    const int rs = K * 4;                        // a stage row: the tile as it lies in C
+    const int nst = BULK ? stages : 0;
     unsigned char *a_hi = sm, *a_lo = sm + a_bytes;
     unsigned char *b_hi = sm + 2 * a_bytes, *b_lo = b_hi + b_bytes;
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(b_lo + b_bytes);   // [2]: one per accumulator
+    unsigned char *raw = b_lo + b_bytes;         // [stages][128][rs] (BULK)
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(raw + (size_t)nst * kTileM * rs);   // [2]: one per accumulator
     uint64_t *idle = mbar + 2;   // a barrier nothing arrives at (the time-out test)
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 3);
+    uint64_t *full = mbar + 3;   // [stages]: a stage's copies have landed (BULK)
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(full + nst);
     const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
     const long long tiles = (M + kTileM - 1) / kTileM;
     const int nitems = 16 * ((K + 15) >> 4);   // warp instructions per tile, all warps
@@ -139,6 +151,7 @@ k_basis_expand(const float *__restrict__ C, long long M, int K, const float *__r
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)));
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar + 1)));
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(idle)));
+        for (int st = 0; st < nst; st++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(full + st)));
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
     // the basis, split into TF32 pairs, once: B[k][n .. n+3] per load (N is
@@ -166,12 +179,51 @@ k_basis_expand(const float *__restrict__ C, long long M, int K, const float *__r
         }
     }
 
+    // BULK: one thread copies tile t's rows (contiguous in C, 16-byte
+    // aligned, a multiple of 32 bytes) into stage st with one bulk copy that
+    // completes on the stage's barrier
+    auto issue_bulk = [&](long long t, int st) {
+        const long long m0 = t * kTileM;
+        const int rows = (int)(M - m0 < kTileM ? M - m0 : kTileM);
+        const uint32_t fb = smem_u32(full + st);
+        const uint32_t bytes = (uint32_t)(rows * K * 4);
+        // the split's reads of this stage (generic proxy) before the copy's writes (async proxy)
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(bytes) : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         smem_u32(raw + (size_t)st * kTileM * rs)),
+                     "l"(C + m0 * K), "r"(bytes), "r"(fb)
+                     : "memory");
+    };
+    // BULK: stage st, split, into the K-major A buffers (rows past the end of
+    // C hold stale words; their accumulator rows are never stored)
+    auto split_stage = [&](int st) {
+        const unsigned char *src = raw + (size_t)st * kTileM * rs;
+#pragma unroll
+        for (int j = 0; j < kMaxK / 4; j++) {
+            if (j < per_warp) {
+                const ChunkPos p = chunk_pos(j, wid, lane, K);
+                if (p.ok) {
+                    const float4 x = *reinterpret_cast<const float4 *>(src + p.r * rs + 16 * p.c4);
+                    float4 h, l;
+                    h.x = tf32_rna(x.x); l.x = tf32_rna(x.x - h.x);
+                    h.y = tf32_rna(x.y); l.y = tf32_rna(x.y - h.y);
+                    h.z = tf32_rna(x.z); l.z = tf32_rna(x.z - h.z);
+                    h.w = tf32_rna(x.w); l.w = tf32_rna(x.w - h.w);
+                    const int o = kmajor_offset(p.r, 4 * p.c4, K);
+                    *reinterpret_cast<float4 *>(a_hi + o) = h;
+                    *reinterpret_cast<float4 *>(a_lo + o) = l;
+                }
+            }
+        }
+    };
+
     // this thread's chunks of a tile of C, loaded into registers ahead of use
-    float4 ra[kMaxK / 4];
+    float4 ra[BULK ? 1 : kMaxK / 4];
     auto load_tile = [&](long long tile) {
         const long long m0 = tile * kTileM;
 #pragma unroll
-        for (int j = 0; j < kMaxK / 4; j++) {
+        for (int j = 0; j < (BULK ? 0 : kMaxK / 4); j++) {
             ra[j] = make_float4(0.f, 0.f, 0.f, 0.f);
             if (j < per_warp) {
                 const ChunkPos p = chunk_pos(j, wid, lane, K);
@@ -190,7 +242,7 @@ k_basis_expand(const float *__restrict__ C, long long M, int K, const float *__r
     // the registers, split, into the K-major A buffers
     auto store_tile = [&]() {
 #pragma unroll
-        for (int j = 0; j < kMaxK / 4; j++) {
+        for (int j = 0; j < (BULK ? 0 : kMaxK / 4); j++) {
             if (j < per_warp) {
                 const ChunkPos p = chunk_pos(j, wid, lane, K);
                 if (p.ok) {
@@ -229,13 +281,27 @@ k_basis_expand(const float *__restrict__ C, long long M, int K, const float *__r
     };
 
     long long tile = blockIdx.x;
-    if (tile < tiles) load_tile(tile);
+    if (!BULK && tile < tiles) load_tile(tile);
     // make the barrier initialisation, the basis and the tensor-memory
     // address visible to every thread
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = *tmem_slot;
+    // BULK: the first `stages` tiles of this CTA in flight
+    long long issued = -1;   // the last tile index g (in this CTA's order) whose copies were issued
+    if (BULK && tid == 0) {
+        for (int st = 0; st < nst; st++) {
+            const long long t = tile + (long long)st * gridDim.x;
+            if (t < tiles) issue_bulk(t, st);
+        }
+    }
+    if (BULK) {
+        const long long mine = tile < tiles ? (tiles - 1 - tile) / gridDim.x : -1;   // this CTA's last g
+        issued = mine < nst - 1 ? mine : nst - 1;
+    }
+    uint32_t full_phase = 0u;   // bit st: the next phase of stage st's barrier
+    long long consumed = -1;    // the last tile index g whose stage has landed
 
     // accumulator acc_i (tile ptile) back to HBM: warp w holds lanes
     // 32w .. 32w+31 = rows of the tile; 32 columns per wait
@@ -284,8 +350,17 @@ k_basis_expand(const float *__restrict__ C, long long M, int K, const float *__r
     uint32_t phase[2] = {0u, 0u};   // the next phase each accumulator's barrier completes
     int pending = -1;               // accumulator whose MMAs are committed and not yet read back
     long long pending_tile = -1;
-    for (int g = 0; tile < tiles; g++, tile += gridDim.x) {
+    int g = 0;
+    for (; tile < tiles; g++, tile += gridDim.x) {
         const int b = g & 1;
+        const int st = BULK ? g % nst : 0;
+        if (BULK) {
+            // this tile's stage has landed
+            ok = __syncthreads_and(mbar_wait(smem_u32(full + st), (full_phase >> st) & 1u, kSpinLimit)) != 0;
+            if (!ok) break;
+            full_phase ^= 1u << st;
+            consumed = g;
+        }
         // the A buffers are free once the previous tile's MMAs are done
         if (pending >= 0) {
             const uint32_t bar = smem_u32(test_timeout ? idle : mbar + pending);
@@ -294,15 +369,26 @@ k_basis_expand(const float *__restrict__ C, long long M, int K, const float *__r
             if (!ok) break;   // the drain below still waits for the committed MMAs
             asm volatile("tcgen05.fence::after_thread_sync;");
         }
-        store_tile();
+        if (BULK) split_stage(st);
+        else store_tile();
         asm volatile("fence.proxy.async.shared::cta;");   // generic-proxy stores -> tensor core
         asm volatile("tcgen05.fence::before_thread_sync;");
         __syncthreads();
         asm volatile("tcgen05.fence::after_thread_sync;");
         if (tid == 0) issue_mma(tmem + (uint32_t)b * ncols, b);
-        // next tile's rows into registers while the MMAs run
-        const long long next = tile + gridDim.x;
-        if (next < tiles) load_tile(next);
+        if (BULK) {
+            // the stage is free again (every thread has split it): the tile
+            // `stages` ahead goes into it
+            const long long nt = tile + (long long)nst * gridDim.x;
+            if (nt < tiles) {
+                if (tid == 0) issue_bulk(nt, st);
+                issued = g + nst;
+            }
+        } else {
+            // next tile's rows into registers while the MMAs run
+            const long long next = tile + gridDim.x;
+            if (next < tiles) load_tile(next);
+        }
         // the previous tile's accumulator back to HBM
         if (pending >= 0) {
             read_back(pending, pending_tile);
@@ -328,6 +414,18 @@ k_basis_expand(const float *__restrict__ C, long long M, int K, const float *__r
             read_back(pending, pending_tile);
         }
     }
+    if (BULK && !ok) {
+        // after a time-out: let the copies still in flight land before the
+        // block exits (tiles consumed+1 .. issued; a stage holds one copy at
+        // a time)
+        bool landed = true;
+        for (long long gg = consumed + 1; gg <= issued; gg++) {
+            const int st = (int)(gg % (nst > 0 ? nst : 1));
+            landed = mbar_wait(smem_u32(full + st), (full_phase >> st) & 1u, kSpinLimit) && landed;
+            full_phase ^= 1u << st;
+        }
+        if (!__syncthreads_and(landed) && tid == 0) atomicOr(err, 4u);
+    }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     if (wid == 0)
@@ -336,21 +434,24 @@ k_basis_expand(const float *__restrict__ C, long long M, int K, const float *__r
 
 } // namespace
 
+// Shared memory of the register path (the bound xrdt_basis_expand checks);
+// the bulk path adds its stages of padded rows and their barriers.
 size_t basis_smem(int K, int N) { return 2 * (size_t)kTileM * K * 4 + 2 * (size_t)N * K * 4 + 32; }
 
-cudaError_t launch_basis_expand(const float *C, long long M, int K, const float *B, int N, float *I, unsigned *err,
-                                cudaStream_t s, int64_t *launches)
+namespace {
+
+size_t basis_smem_bulk(int K, int N, int stages)
 {
-    if (M <= 0) return cudaSuccess;
-    size_t smem = basis_smem(K, N);
-    int dev = 0, sms = 0, smem_sm = 0, optin = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_basis_expand, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    return basis_smem(K, N) + (size_t)stages * kTileM * K * 4 + 8 * (size_t)stages;
+}
+
+template <bool BULK>
+cudaError_t launch_basis_variant(const float *C, long long M, int K, const float *B, int N, float *I, unsigned *err,
+                                 cudaStream_t s, size_t smem, int stages, int aligned, int aligned_b, int sms,
+                                 int smem_sm, int optin)
+{
+    cudaError_t e = cudaFuncSetAttribute(k_basis_expand<BULK>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     if (e != cudaSuccess) return e;
-    if (smem > (size_t)optin) return cudaErrorInvalidConfiguration;
     // CTAs per SM: as many as registers and shared memory allow, but no more
     // than the 512 tensor-memory columns hold (two accumulators each, and an
     // allocation that does not fit would wait for another CTA to finish all
@@ -360,7 +461,7 @@ cudaError_t launch_basis_expand(const float *C, long long M, int K, const float 
     while (ncols < N) ncols <<= 1;
     const int tmem_ctas = 512 / (2 * ncols);
     cudaFuncAttributes fa;
-    e = cudaFuncGetAttributes(&fa, k_basis_expand);
+    e = cudaFuncGetAttributes(&fa, k_basis_expand<BULK>);
     if (e != cudaSuccess) return e;
     // registers are allocated per warp in units of 256
     const int regs_warp = ((fa.numRegs * 32 + 255) / 256) * 256;
@@ -376,20 +477,55 @@ cudaError_t launch_basis_expand(const float *C, long long M, int K, const float 
         const size_t padded = (size_t)smem_sm / (tmem_ctas + 1) + 1 - fa.sharedSizeBytes - 1024;
         if (padded > smem && padded <= (size_t)optin) smem = padded;
     }
-    const long long tiles = (M + 127) / 128;
+    const long long tiles = (M + kTileM - 1) / kTileM;
     long long grid = (long long)sms * ctas;
     if (grid > tiles) grid = tiles;
-    const int aligned = (((uintptr_t)C | (uintptr_t)I) & 15) == 0 ? 1 : 0;
-    const int aligned_b = ((uintptr_t)B & 15) == 0 ? 1 : 0;
     // XRDT_TEST_BASIS_TIMEOUT=1 makes every block's first accumulator wait
     // run out (test of the time-out path: error flag, drain, tensor memory
     // freed)
     const char *tt = getenv("XRDT_TEST_BASIS_TIMEOUT");
     const int test_timeout = (tt && tt[0] == '1') ? 1 : 0;
-    k_basis_expand<<<(unsigned)grid, kBasisThreads, smem, s>>>(C, M, K, B, N, I, err, aligned, aligned_b,
-                                                                 test_timeout);
-    if (launches) (*launches)++;
+    k_basis_expand<BULK><<<(unsigned)grid, kBasisThreads, smem, s>>>(C, M, K, B, N, I, err, aligned, aligned_b,
+                                                                       test_timeout, stages);
     return cudaGetLastError();
+}
+
+} // namespace
+
+cudaError_t launch_basis_expand(const float *C, long long M, int K, const float *B, int N, float *I, unsigned *err,
+                                cudaStream_t s, int64_t *launches)
+{
+    if (M <= 0) return cudaSuccess;
+    int dev = 0, sms = 0, smem_sm = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e != cudaSuccess) return e;
+    if (basis_smem(K, N) > (size_t)optin) return cudaErrorInvalidConfiguration;
+    const int aligned = (((uintptr_t)C | (uintptr_t)I) & 15) == 0 ? 1 : 0;
+    const int aligned_b = ((uintptr_t)B & 15) == 0 ? 1 : 0;
+    if (launches) (*launches)++;
+    // the bulk-copy ring when C allows it: two or three stages, whichever
+    // leaves more CTAs on an SM (the per-tile work is latency-bound, so CTAs
+    // count for more than a third stage), three on a tie
+    if (((uintptr_t)C & 15) == 0) {
+        int best = 0, best_ctas = 0;
+        for (int stages = 3; stages >= 2; stages--) {
+            const size_t sm_b = basis_smem_bulk(K, N, stages);
+            if (sm_b > (size_t)optin) continue;
+            const int c = (int)((size_t)smem_sm / (sm_b + 1024));
+            if (c > best_ctas) {
+                best = stages;
+                best_ctas = c;
+            }
+        }
+        if (best)
+            return launch_basis_variant<true>(C, M, K, B, N, I, err, s, basis_smem_bulk(K, N, best), best, aligned,
+                                              aligned_b, sms, smem_sm, optin);
+    }
+    return launch_basis_variant<false>(C, M, K, B, N, I, err, s, basis_smem(K, N), 0, aligned, aligned_b, sms,
+                                       smem_sm, optin);
 }
 
 } // namespace xrdt
