@@ -17,10 +17,13 @@
 //    memory (the dropped A_lo B_lo term is below 2^-22 of the product);
 //  * two accumulators in tensor memory: while the MMAs of tile g run, the
 //    four warps read tile g-1's accumulator back (tcgen05.ld) and store its
-//    rows, and the loads of tile g+1's rows of C are already in flight in
-//    registers (16-byte loads, 8 rows x 64 bytes per warp instruction, which
-//    also makes the shared-memory stores of the split free of bank
-//    conflicts);
+//    rows;
+//  * the tiles of C arrive ahead of use: through the bulk-copy engine into a
+//    ring of shared-memory stages (one cp.async.bulk per tile, completing on
+//    the stage's mbarrier) when C is 16-byte aligned and two stages fit,
+//    else as 16-byte loads into registers during the MMAs; either way a warp
+//    instruction covers 8 rows x 64 bytes, which keeps the shared-memory
+//    stores of the split free of bank conflicts;
 //  * one thread issues the MMAs (K = 8 each) and commits each tile's to the
 //    mbarrier of its accumulator.
 //
