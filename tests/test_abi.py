@@ -87,3 +87,22 @@ def test_no_silent_cpu_path_without_gpu():
     # the Python front end raises rather than computing anything on the CPU
     with pytest.raises(xt.XrdtError):
         xt.Context(0)
+
+
+def test_python_boundary_checks_types_and_sizes():
+    """The Python front end converts numpy arrays but never reinterprets a
+    tensor of another element type, and rejects arrays shorter than the
+    library will read."""
+    torch = pytest.importorskip("torch")
+    from xrd_tomography_gb300.api import _ptr
+    p, k = _ptr(np.zeros(4, np.float64), np.float32, 4)
+    assert k.dtype == np.float32 and p == k.ctypes.data
+    with pytest.raises(ValueError):
+        _ptr(np.zeros(3, np.float32), np.float32, 4)
+    with pytest.raises(ValueError):
+        _ptr(torch.zeros(4, dtype=torch.float16), np.float32)
+    with pytest.raises(ValueError):
+        _ptr(torch.zeros(4, dtype=torch.int64), np.int32)
+    with pytest.raises(ValueError):
+        _ptr(torch.zeros(3), np.float32, 4)
+    assert _ptr(torch.zeros(4), np.float32, 4)[0] != 0

@@ -193,15 +193,29 @@ def default_context() -> Context:
     return _default_ctx
 
 
-def _ptr(a, dtype):
-    """Device or host address of a torch tensor / numpy array (kept alive by caller)."""
+_TORCH_DTYPE = {np.dtype(np.float32): "torch.float32", np.dtype(np.int32): "torch.int32",
+                np.dtype(np.int64): "torch.int64", np.dtype(np.float64): "torch.float64"}
+
+
+def _ptr(a, dtype, n=None):
+    """Device or host address of a torch tensor / numpy array (kept alive by
+    caller).  A numpy array is converted to dtype; a torch tensor must have
+    that element type already (the library reads the words as they are).  n:
+    the number of elements the library will touch, checked when given."""
     if a is None:
         return None, None
     if hasattr(a, "data_ptr"):  # torch tensor
         if not a.is_contiguous():
             raise ValueError("tensors must be contiguous")
+        want = _TORCH_DTYPE.get(np.dtype(dtype))
+        if want and str(a.dtype) != want:
+            raise ValueError(f"a tensor of {a.dtype} where {want} is needed")
+        if n is not None and a.numel() < n:
+            raise ValueError(f"a tensor of {a.numel()} elements where {n} are needed")
         return a.data_ptr(), a
     arr = np.ascontiguousarray(a, dtype=dtype)
+    if n is not None and arr.size < n:
+        raise ValueError(f"an array of {arr.size} elements where {n} are needed")
     return arr.ctypes.data, arr
 
 
@@ -221,10 +235,12 @@ def forward(p: Problem, spectrum, Ifine, seg, a1, a2, S2, q_min, q_max, a_min, a
         Amatrix = np.empty(p.amatrix_elems, np.float32)
     keep = []
     ptrs = []
-    for a, dt in ((spectrum, np.float32), (Ifine, np.float32), (seg, np.int32), (a1, np.float32),
-                  (a2, np.float32), (S2, np.float32), (Nphotons, np.float32), (Cphotons, np.float32),
-                  (Amatrix, np.float32)):
-        pt, k = _ptr(a, dt)
+    nvox, ntab = p.nx * p.ny, p.nq * p.na
+    for a, dt, n in ((spectrum, np.float32, p.nrg_src * p.nrg_det), (Ifine, np.float32, p.nqf * p.n_mat),
+                     (seg, np.int32, nvox), (a1, np.float32, nvox), (a2, np.float32, nvox), (S2, np.float32, ntab),
+                     (Nphotons, np.float32, rays), (Cphotons, np.float32, rays),
+                     (Amatrix, np.float32, p.amatrix_elems)):
+        pt, k = _ptr(a, dt, n)
         ptrs.append(pt)
         keep.append(k)
     fl = flags | (FWD_PLAIN_FP64 if plain else 0)
@@ -250,9 +266,11 @@ def forward_tables(p: Problem, spectrum, seg, a1, a2, S1, S2, q_min, q_max, a_mi
         Cphotons = np.empty(rays, np.float32)
     keep = []
     ptrs = []
-    for a, dt in ((spectrum, np.float32), (seg, np.int32), (a1, np.float32), (a2, np.float32),
-                  (S1, np.float32), (S2, np.float32), (Nphotons, np.float32), (Cphotons, np.float32)):
-        pt, k = _ptr(a, dt)
+    nvox, ntab = p.nx * p.ny, p.nq * p.na
+    for a, dt, n in ((spectrum, np.float32, p.nrg_src * p.nrg_det), (seg, np.int32, nvox), (a1, np.float32, nvox),
+                     (a2, np.float32, nvox), (S1, np.float32, ntab), (S2, np.float32, ntab),
+                     (Nphotons, np.float32, rays), (Cphotons, np.float32, rays)):
+        pt, k = _ptr(a, dt, n)
         ptrs.append(pt)
         keep.append(k)
     fl = flags | (TAB_BILINEAR if bilinear else 0)
@@ -476,19 +494,19 @@ class Operator:
 
     def forward(self, x, y=None):
         """y = Av x."""
-        px, kx = _ptr(x, np.float32)
+        px, kx = _ptr(x, np.float32, self.unknowns)
         if y is None:
             y = np.empty(self.p.rays, np.float32)
-        py, ky = _ptr(y, np.float32)
+        py, ky = _ptr(y, np.float32, self.p.rays)
         _check(lib().xrdt_op_forward(self.h, px, py, 0), self.ctx.h)
         return ky
 
     def adjoint(self, w, g=None):
         """g = Av^T w."""
-        pw, kw = _ptr(w, np.float32)
+        pw, kw = _ptr(w, np.float32, self.p.rays)
         if g is None:
             g = np.empty(self.unknowns, np.float32)
-        pg, kg = _ptr(g, np.float32)
+        pg, kg = _ptr(g, np.float32, self.unknowns)
         _check(lib().xrdt_op_adjoint(self.h, pw, pg, 0), self.ctx.h)
         return kg
 
