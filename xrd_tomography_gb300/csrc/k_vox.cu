@@ -218,30 +218,61 @@ __device__ __forceinline__ void vox_fwd_pair(const VoxJob &J, int64_t pidx, unsi
         const float2 Adv = J.op.walk[(pidx - J.pair0) * nv + v];
 
         const int nin = min(32, nv - chunk * 32);
-        for (int i = 0; i < nin; i++) {
-            const float2 Ad = make_float2(__shfl_sync(0xffffffffu, Adv.x, i), __shfl_sync(0xffffffffu, Adv.y, i));
-            const float sh = __shfl_sync(0xffffffffu, vg.s.hi, i);
-            const float sl = __shfl_sync(0xffffffffu, vg.s.lo, i);
-            const ff sg = {__shfl_sync(0xffffffffu, vg.sg.hi, i), __shfl_sync(0xffffffffu, vg.sg.lo, i)};
-            const float Wg = __shfl_sync(0xffffffffu, vg.Wg, i);
-            const float Asx = __shfl_sync(0xffffffffu, Asv.x, i);
-            const float Asy = __shfl_sync(0xffffffffu, Asv.y, i);
-            const SigmaGeom sgm = sigma_geom(sh, sl, sg, ff{en[4 * E], en[6 * E]});
+        // the (voxel, energy) term: lane's energy el for voxel i of the chunk
+        auto term = [&](int i, int el, float2 Ad, float sh, float sl, float Wg, float Asx, float Asy,
+                        const SigmaGeom &sgm) {
             const float *xrow = xd + (int64_t)(chunk * 32 + i) * K;
-#pragma unroll 1
-            for (int el = lane; el < E; el += 32) {
-                const EnergyTerm t = energy_term(en, E, el, Ad.x, Ad.y, Asx, Asy, sh, sl, sgm, Wg, rsqrt2pi);
-                if (t.pref == 0.f) continue;   // attenuation underflow: no contribution
-                int klo, khi;
-                coarse_window(t.w_hi, t.half, qlo_f, c.qpar_a, c.qpar_b, K, &klo, &khi);
-                float acc = 0.f;
-                for (int k = klo; k <= khi; k++) {
-                    const float4 q = cq[k];
-                    acc = fmaf(gauss_f32(t.w_hi, t.w_lo, q.x, q.y, t.c_hi, t.c_lo), __ldg(xrow + k), acc);
+            const EnergyTerm t = energy_term(en, E, el, Ad.x, Ad.y, Asx, Asy, sh, sl, sgm, Wg, rsqrt2pi);
+            if (t.pref == 0.f) return;   // attenuation underflow: no contribution
+            int klo, khi;
+            coarse_window(t.w_hi, t.half, qlo_f, c.qpar_a, c.qpar_b, K, &klo, &khi);
+            float acc = 0.f;
+            for (int k = klo; k <= khi; k++) {
+                const float4 q = cq[k];
+                acc = fmaf(gauss_f32(t.w_hi, t.w_lo, q.x, q.y, t.c_hi, t.c_lo), __ldg(xrow + k), acc);
+            }
+            float2 s = TNw[el];
+            kahan_add(s.x, s.y, t.pref * acc);
+            TNw[el] = s;
+        };
+        if (E > 32 && (E & 31)) {
+            // E not a multiple of 32 (40 on the 128x128 workload): the chunk's
+            // (voxel, energy) items nin*E, 32 consecutive ones per step, so
+            // that no step runs with a few lanes.  Consecutive items of a step
+            // have distinct energies (32 < E), hence distinct sums TNw[el].
+            // Each lane's voxel constants come from the lane that holds them.
+            const SigmaGeom sgv = sigma_geom(vg.s.hi, vg.s.lo, vg.sg, ff{en[4 * E], en[6 * E]});
+            int i = 0, el = lane;
+            for (int t0 = 0; t0 < nin * E; t0 += 32) {
+                const bool act = i < nin;
+                const float2 Ad = make_float2(__shfl_sync(0xffffffffu, Adv.x, i), __shfl_sync(0xffffffffu, Adv.y, i));
+                const float sh = __shfl_sync(0xffffffffu, vg.s.hi, i);
+                const float sl = __shfl_sync(0xffffffffu, vg.s.lo, i);
+                const float Wg = __shfl_sync(0xffffffffu, vg.Wg, i);
+                const float Asx = __shfl_sync(0xffffffffu, Asv.x, i);
+                const float Asy = __shfl_sync(0xffffffffu, Asv.y, i);
+                SigmaGeom sgm;
+                sgm.t1 = ff{__shfl_sync(0xffffffffu, sgv.t1.hi, i), __shfl_sync(0xffffffffu, sgv.t1.lo, i)};
+                sgm.sg_s2 = ff{__shfl_sync(0xffffffffu, sgv.sg_s2.hi, i), __shfl_sync(0xffffffffu, sgv.sg_s2.lo, i)};
+                if (act) term(i, el, Ad, sh, sl, Wg, Asx, Asy, sgm);
+                el += 32;
+                if (el >= E) {
+                    el -= E;
+                    i++;
                 }
-                float2 s = TNw[el];
-                kahan_add(s.x, s.y, t.pref * acc);
-                TNw[el] = s;
+            }
+        } else {
+            for (int i = 0; i < nin; i++) {
+                const float2 Ad = make_float2(__shfl_sync(0xffffffffu, Adv.x, i), __shfl_sync(0xffffffffu, Adv.y, i));
+                const float sh = __shfl_sync(0xffffffffu, vg.s.hi, i);
+                const float sl = __shfl_sync(0xffffffffu, vg.s.lo, i);
+                const ff sg = {__shfl_sync(0xffffffffu, vg.sg.hi, i), __shfl_sync(0xffffffffu, vg.sg.lo, i)};
+                const float Wg = __shfl_sync(0xffffffffu, vg.Wg, i);
+                const float Asx = __shfl_sync(0xffffffffu, Asv.x, i);
+                const float Asy = __shfl_sync(0xffffffffu, Asv.y, i);
+                const SigmaGeom sgm = sigma_geom(sh, sl, sg, ff{en[4 * E], en[6 * E]});
+#pragma unroll 1
+                for (int el = lane; el < E; el += 32) term(i, el, Ad, sh, sl, Wg, Asx, Asy, sgm);
             }
         }
     }
