@@ -1,11 +1,13 @@
-// walk.cuh -- the attenuation line integral (attenuator.cu:9-109) as a
-// warp-cooperative walk over the bilinear cell map.
+// walk.cuh -- the attenuation line integral (attenuator.cu:9-109) over the
+// bilinear cell map.
 //
 // The integer decisions (which ROI edge is entered, how many samples the ray
-// takes) are made in FP64 exactly as the reference defines them; the
-// samples themselves are summed in FP32 by the 32 lanes of a warp, lane l
-// taking samples l, l+32, ... (consecutive samples of one ray are 0.25 voxel
-// apart, so one warp instruction touches a few neighbouring cells).
+// takes) are those of the reference, made in FP32 with guard bands
+// (walk_setup_f32) or in FP64 (walk_setup).  Two ways to sum the samples:
+// walk_cells, one lane per ray, cell by cell with closed-form sums over the
+// samples inside each cell, anchored at the voxel with float-pair offsets
+// (the projector's and the operators' walks); and walk_coop, the 32 lanes of
+// a warp on one ray, lane l taking samples l, l+32, ... (the CT sinogram).
 #pragma once
 
 #include "xrdt_device.cuh"
