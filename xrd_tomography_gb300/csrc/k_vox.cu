@@ -19,24 +19,27 @@
 // (voxel chunk, pair group) tiles of all problems for the adjoint -- so that
 // uneven problems share one launch and the tail stays short.
 //
-// When the operator keeps the detector-side integrals of every (pair, voxel)
-// (VoxOp::walk, walked once by k_walk.cu when the operator is created), the
-// kernels read them instead of walking.
+// The detector-side integrals of each (pair, voxel) come from a table: the
+// operator's own (VoxOp::walk, walked once by k_walk.cu when the operator is
+// created) or the current tile of a walk streamed inside the call.
 //
 //  * forward (k_vox_fwd): one item = one (source, pixel) pair, as in
-//    k_fwd.cu; lane = source energy sums the coarse bins within 7.5 sigma of
-//    the wavevector transfer, weighted by x[v, k] dq_k, into compensated
-//    per-energy sums; the banded spectrum weights give the detector bins.  In
+//    k_fwd.cu; lane = source energy (or, for windows that are not a multiple
+//    of 32 energies, the chunk's (voxel, energy) items 32 at a time) sums the
+//    coarse bins within 7.5 sigma of the wavevector transfer, weighted by
+//    x[v, k] dq_k, into compensated per-energy sums; the banded spectrum
+//    weights give the detector bins.  In
 //    MLEM mode the block goes on to form the ratios y / (Av x + c + 1e-20) of
 //    main.m:162 for its detector bins and folds them back through the same
 //    spectrum band into per-energy weights what[pair, e] = sum_nrg RF[e,nrg]
 //    ratio[nrg].
 //  * adjoint (k_vox_adj): voxel-major, so that g stays on chip.  A warp owns
 //    32 voxels and loops over a group of pairs; per (pair, voxel) lane =
-//    energy forms what[pair,e] * (the energy's prefactor), then lane = coarse
-//    bin k adds sum_e of those times G(wvt_e - q_k) to the voxel's compensated
-//    sum.  The groups' partial sums are added in FP64 by k_vox_reduce, which
-//    also applies the MLEM update (main.m:163-176).
+//    energy forms what[pair,e] * (the energy's prefactor) and its coarse-bin
+//    window (13.25 sigma), then lane = coarse bin k adds the terms of the
+//    energies whose windows can hold k to the voxel's compensated sum.  The
+//    groups' partial sums (float pairs) are added in FP64 by k_vox_reduce,
+//    which also applies the MLEM update (main.m:163-176).
 #include "scatter.cuh"
 
 namespace xrdt {
