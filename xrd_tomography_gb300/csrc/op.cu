@@ -1,11 +1,21 @@
-// op.cu -- C ABI of the per-voxel-coefficient operator (xrdt_op_*).
+// op.cu -- C ABI of the per-voxel-coefficient operator (xrdt_op_*), of
+// batches of operators (xrdt_batch_*) and of the dense-basis operator
+// (xrdt_bop_*).
 //
 // An operator holds everything about one phantom and scanner that does not
 // change between forward and adjoint calls: the bilinear attenuation cells,
 // the non-empty voxels in the reference's loop order, the table of
-// (source, pixel) pairs, the source-side line integrals and the per-energy
-// tables.  The unknowns live in the compact voxel order [nv][NWT] on the
+// (source, pixel) pairs, the source-side line integrals, the per-energy
+// tables and, when it fits, the detector-side integrals of every (pair,
+// voxel).  The unknowns live in the compact voxel order [nv][NWT] on the
 // device; calls convert from and to the full-grid layout [NX*NY][NWT].
+//
+// Calls run through a Plan: the batch's job descriptors and work offsets,
+// the autotuned adjoint split, and -- for operators without a table of
+// their own -- the tiles of whole pixels whose detector-side integrals are
+// walked into a shared buffer inside each call (the forward, the adjoint
+// and each MLEM iteration walk every tile once).  Each MLEM iteration of a
+// plan is one CUDA graph.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
