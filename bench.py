@@ -48,10 +48,10 @@ FLUSH_BYTES = 256 << 20
 # ncu capture of a single launch on the 128x128 workload (4096 pairs x 5009
 # voxels); the traffic is the launch's walk table plus a fixed part, so the
 # 256x256 figure below is that rate times the pair-voxels of its mean launch
-K_FWD_DRAM_BYTES_PER_PAIR_VOXEL = (166039808 + 4460544) / (4096 * 5009)   # 8.31 B (read + write)
+K_FWD_DRAM_BYTES_PER_PAIR_VOXEL = (166727936 + 4232704) / (4096 * 5009)   # 8.33 B (read + write)
 # issue slots busy in k_fwd (ncu, the same capture): the kernel is bound by
 # instruction issue, not by the SFU rate of the roofline below
-K_FWD_ISSUE_BUSY = 0.8614
+K_FWD_ISSUE_BUSY = 0.8392
 
 
 def parse():

@@ -27,7 +27,9 @@
 // of 32 voxels.  For a chunk, lane = voxel computes the scattering geometry
 // and reads the voxel's line integrals; then for each voxel of the chunk
 // lane = source energy evaluates the (voxel, energy) term and adds it to the
-// warp's compensated per-energy sums.
+// warp's compensated per-energy sums.  A window of more than 32 energies that
+// is not a multiple of 32 takes the chunk's (voxel, energy) items 32 at a
+// time instead, so that no step runs with a few lanes.
 #include "scatter.cuh"
 
 namespace xrdt {
@@ -220,217 +222,259 @@ k_fwd(const FwdArgs args)
             const float tav = TAB == 2 ? args.vox_ta[v] : 0.f;
 
             const int nin = min(32, nv - chunk * 32);
-            for (int i = 0; i < nin; i++) {
-                // labels as at integrate_diffraction.cu:259-260: the detector-side
-                // integral feeds Pin, the source-side one Pout.
-                const float2 Ad = make_float2(__shfl_sync(0xffffffffu, Adv.x, i), __shfl_sync(0xffffffffu, Adv.y, i));
-                const float sh = __shfl_sync(0xffffffffu, vg.s.hi, i);
-                const float sl = __shfl_sync(0xffffffffu, vg.s.lo, i);
-                const float oh = __shfl_sync(0xffffffffu, vg.omc.hi, i);
-                const float ol = __shfl_sync(0xffffffffu, vg.omc.lo, i);
-                const float sg = __shfl_sync(0xffffffffu, vg.sg.hi, i);
-                const float gp = __shfl_sync(0xffffffffu, vg.gp, i);
-                const float Wg = __shfl_sync(0xffffffffu, vg.Wg, i);
-                const float cos2 = __shfl_sync(0xffffffffu, vg.cos2, i);
-                const int m = __shfl_sync(0xffffffffu, mv, i);
-                const int na = __shfl_sync(0xffffffffu, nav, i);
-                const float a2now = __shfl_sync(0xffffffffu, a2v, i);
-                const float Asx = __shfl_sync(0xffffffffu, Asv.x, i);
-                const float Asy = __shfl_sync(0xffffffffu, Asv.y, i);
-                const float ta = TAB == 2 ? __shfl_sync(0xffffffffu, tav, i) : 0.f;
-                const float s2f = sh * sh;
-                const float sg_s2 = __fdividef(sg, s2f);
-#pragma unroll 1
-                for (int el = pe0 + lane; el < pe1; el += 32) {
-                    // ---- (voxel, source energy) term, :266-356 ----
-                    // attenuation exponents with 1/f1, 1/f2 as pairs: X reaches
-                    // tens at the lowest energies, where FP32 constants alone
-                    // would move exp(-X) by a few 1e-6
-                    const float if1 = en_if1[el], if2 = en_if2[el];
-                    const float if1l = en_if1l[el], if2l = en_if2l[el];
-                    const float Xin = fmaf(Ad.x, if1, fmaf(Ad.y, if2, fmaf(Ad.x, if1l, Ad.y * if2l)));
-                    const float Xout = fmaf(Asx, if1, fmaf(Asy, if2, fmaf(Asx, if1l, Asy * if2l)));
-                    const float wh0 = en_wh[el], wl0 = en_wl[el];
-                    float w_hi = wh0 * sh;
-                    float w_lo = fmaf(wh0, sh, -w_hi) + fmaf(wh0, sl, wl0 * sh);
-                    {
-                        const float t = w_hi + w_lo;
-                        w_lo = w_lo - (t - w_hi);
-                        w_hi = t;
+            // the (voxel, source energy) term, :266-356, of voxel i of the chunk
+            // (its constants as arguments) for energy el.  Labels as at
+            // integrate_diffraction.cu:259-260: the detector-side integral Ad
+            // feeds Pin, the source-side one (Asx, Asy) Pout.
+            auto term = [&](int el, float2 Ad, float sh, float sl, float oh, float ol, float gp, float Wg,
+                            float cos2, int m, int na, float a2now, float Asx, float Asy, float ta, float s2f,
+                            float sg_s2) {
+                // ---- (voxel, source energy) term, :266-356 ----
+                // attenuation exponents with 1/f1, 1/f2 as pairs: X reaches
+                // tens at the lowest energies, where FP32 constants alone
+                // would move exp(-X) by a few 1e-6
+                const float if1 = en_if1[el], if2 = en_if2[el];
+                const float if1l = en_if1l[el], if2l = en_if2l[el];
+                const float Xin = fmaf(Ad.x, if1, fmaf(Ad.y, if2, fmaf(Ad.x, if1l, Ad.y * if2l)));
+                const float Xout = fmaf(Asx, if1, fmaf(Asy, if2, fmaf(Asx, if1l, Asy * if2l)));
+                const float wh0 = en_wh[el], wl0 = en_wl[el];
+                float w_hi = wh0 * sh;
+                float w_lo = fmaf(wh0, sh, -w_hi) + fmaf(wh0, sl, wl0 * sh);
+                {
+                    const float t = w_hi + w_lo;
+                    w_lo = w_lo - (t - w_hi);
+                    w_hi = t;
+                }
+                const float sig2 = fmaf(en_c1[el], s2f, en_c2[el] * sg_s2);
+                const float rs = rsqrtf(sig2);
+                const float cexp = -0.5f * kLog2e * rs * rs;
+                const float Xio = Xin + Xout;
+                const float PP = ex2_approx(-fmaf(Xio, kLog2e, Xio * kLog2e_lo));
+                nexp += 1;
+                const float pref = PP * Wg * rsqrt2pi * rs;
+                const float half = kSig * sig2 * rs;
+                if (WITH_N && TAB) {
+                    // the coherent term from the table S1 (the reference's
+                    // commented-out kernel, integrate_diffraction.cu:701-719):
+                    // Pin Pout geom Rayleigh a2 S1[wvt bin, a-ratio bin] with
+                    // wvt = ein sin(theta/2) on the tables' log2 axis
+                    const float ein = en_ein[el];
+                    float s1v;
+                    if (TAB == 1) {
+                        s1v = S1[coherent_bin(P, ein, sh, oh, ol, args.T.energy[lo_e + el].ein, qmin_t, inv_dqt) +
+                                 na * P.nq];
+                    } else {
+                        s1v = table_bilinear(S1, P.nq, P.na, (lg2_approx(ein * sh) - qmin_t) * c.inv_dqg, ta);
                     }
-                    const float sig2 = fmaf(en_c1[el], s2f, en_c2[el] * sg_s2);
-                    const float rs = rsqrtf(sig2);
-                    const float cexp = -0.5f * kLog2e * rs * rs;
-                    const float Xio = Xin + Xout;
-                    const float PP = ex2_approx(-fmaf(Xio, kLog2e, Xio * kLog2e_lo));
-                    nexp += 1;
-                    const float pref = PP * Wg * rsqrt2pi * rs;
-                    const float half = kSig * sig2 * rs;
-                    if (WITH_N && TAB) {
-                        // the coherent term from the table S1 (the reference's
-                        // commented-out kernel, integrate_diffraction.cu:701-719):
-                        // Pin Pout geom Rayleigh a2 S1[wvt bin, a-ratio bin] with
-                        // wvt = ein sin(theta/2) on the tables' log2 axis
-                        const float ein = en_ein[el];
-                        float s1v;
-                        if (TAB == 1) {
-                            s1v = S1[coherent_bin(P, ein, sh, oh, ol, args.T.energy[lo_e + el].ein, qmin_t, inv_dqt) +
-                                     na * P.nq];
+                    float2 k = TNw[el];
+                    kahan_add(k.x, k.y, PP * Wg * a2now * s1v);
+                    TNw[el] = k;
+                }
+                if (WITH_N && !TAB) {
+                    const float jc = (w_hi - qlo_f) * inv_dqf - 0.5f;
+                    // bounded floors: the indices are clamped to the grid and an
+                    // empty window is skipped
+                    const int jlo = max(ceil_bounded(jc - half * inv_dqf), 0);
+                    int jhi = min(floor_bounded(jc + half * inv_dqf), P.nqf - 1);
+                    float acc = 0.f;
+                    // pref == 0: the attenuation factor underflowed, every term is 0
+                    if (jlo <= jhi && pref != 0.f) {
+                        // a multiple of four bins, so the loop has no tail: the
+                        // extra bins are exact terms of the full sum or the zero
+                        // pads after the last bin.  (A tail would make the
+                        // compiler rebuild the float counter from the trip count
+                        // through an int-to-float conversion, which this GPU
+                        // issues on its FP64 pipe.)
+                        jhi += (4 - ((jhi - jlo + 1) & 3)) & 3;
+                        nexp += (unsigned)(jhi - jlo + 1);
+                        // The exponent c (w - q_j)^2 as a quadratic in u = j - jc
+                        // about the bin jc nearest the centre: with
+                        // delta = w - q_jc (|delta| <= dq/2),
+                        //   c (delta - u dq)^2 = A + B u + C u^2,
+                        // A = c delta^2, B = -2 c delta dq, C = c dq^2 (dq^2
+                        // with the grid step's low part).  Near the
+                        // peak the sum is A alone; far out C u^2 dominates, so
+                        // the exponent keeps the relative accuracy of the direct
+                        // form in two FMAs per bin.
+                        const float2 q0 = fq[jlo];
+                        const float d0 = (w_hi - q0.x) + (w_lo - q0.y);
+                        const float tc = rintf(d0 * inv_dqf);
+                        const float delta = fmaf(-tc, dqf_lo, fmaf(-tc, dqf_hi, d0));
+                        const float cd = cexp * delta;
+                        const float Aq = cd * delta;
+                        const float Bq = -2.f * cd * dqf_hi;
+                        const float Cq = cexp * fmaf(dqf_hi, dqf_hi, 2.f * dqf_hi * dqf_lo);
+                        const float *Ir = Is + m * (P.nqf + 3) + jlo;
+                        const float *Iend = Ir + (jhi - jlo + 1);
+                        float acc2 = 0.f;
+                        float u = -tc;   // bin offset from jc as a float: no conversion in the loop
+                        for (; Ir < Iend; Ir += 4, u += 4.f) {
+                            const float u1 = u + 1.f, u2 = u + 2.f, u3 = u + 3.f;
+                            acc = fmaf(ex2_approx(fmaf(fmaf(Cq, u, Bq), u, Aq)), Ir[0], acc);
+                            acc2 = fmaf(ex2_approx(fmaf(fmaf(Cq, u1, Bq), u1, Aq)), Ir[1], acc2);
+                            acc = fmaf(ex2_approx(fmaf(fmaf(Cq, u2, Bq), u2, Aq)), Ir[2], acc);
+                            acc2 = fmaf(ex2_approx(fmaf(fmaf(Cq, u3, Bq), u3, Aq)), Ir[3], acc2);
+                        }
+                        acc += acc2;
+                    }
+                    float2 k = TNw[el];
+                    kahan_add(k.x, k.y, pref * dqf_hi * acc);
+                    TNw[el] = k;
+                }
+                if (WITH_A) {
+                    int klo, khi;
+                    coarse_window(w_hi, half, qlo_f, c.qpar_a, c.qpar_b, P.nwt, &klo, &khi);
+                    float *tar = TA + ((size_t)(el - pe0) * P.n_mat + m) * P.nwt;
+                    nexp += (unsigned)max(0, khi - klo + 1);
+                    for (int k = klo; k <= khi; k++) {
+                        const float4 c = cq[k];
+                        const float d = (w_hi - c.x) + (w_lo - c.y);
+                        atomicAdd(tar + k, pref * c.z * ex2_approx(cexp * d * d));
+                    }
+                }
+                // ---- Compton, :318-356 ----
+                {
+                    const float ein = en_ein[el];
+                    // no contraction: the Compton bin check forms eratio the same way
+                    const float x = __fmul_rn(ein, oh);       // eratio - 1
+                    const float eratio = __fadd_rn(1.f, x);
+                    const float inv_er = rcp_approx(eratio);
+                    const int eg = lo_e + el;
+                    // detector bins whose window holds e and whose channel the
+                    // outgoing range [E1, E2]/eratio can overlap
+                    const float Eo_lo = en_e1[el];
+                    // channels overlapped by [E1, E2]/eratio (an FP32 misjudgement at a
+                    // channel edge drops an overlap below 1e-6 of the bin width)
+                    float fn0;
+                    // bounded floors: n0 is raised to the window, n1 lowered to it,
+                    // and an empty range is skipped
+                    int n0 = floor_bounded((Eo_lo * inv_er - edmin) * inv_dEd, &fn0);
+                    if (n0 < wn[2 * el]) {
+                        n0 = wn[2 * el];
+                        fn0 = en_wn0f[el];
+                    }
+                    const int n1 = min(wn[2 * el + 1], floor_bounded(((Eo_lo + dEsf) * inv_er - edmin) * inv_dEd));
+                    if (n0 <= n1) {
+                        // the table's value: nearest bin, or bilinear in the table path
+                        float s2v;
+                        if (TAB == 2) {
+                            const float wC = ein * sh;
+                            const float arg = eratio + wC * wC;
+                            const float l2 = lg2_approx(wC * arg * rsqrt_approx(arg) * inv_er);
+                            s2v = table_bilinear(S2, P.nq, P.na, (l2 - qmin_t) * c.inv_dqg, ta);
                         } else {
-                            s1v = table_bilinear(S1, P.nq, P.na, (lg2_approx(ein * sh) - qmin_t) * c.inv_dqg, ta);
+                            s2v = S2[compton_bin(P, ein, eratio, inv_er, sh, oh, ol, args.T.energy[eg].ein, qmin_t,
+                                                 inv_dqt) +
+                                     na * P.nq];
                         }
-                        float2 k = TNw[el];
-                        kahan_add(k.x, k.y, PP * Wg * a2now * s1v);
-                        TNw[el] = k;
-                    }
-                    if (WITH_N && !TAB) {
-                        const float jc = (w_hi - qlo_f) * inv_dqf - 0.5f;
-                        // bounded floors: the indices are clamped to the grid and an
-                        // empty window is skipped
-                        const int jlo = max(ceil_bounded(jc - half * inv_dqf), 0);
-                        int jhi = min(floor_bounded(jc + half * inv_dqf), P.nqf - 1);
-                        float acc = 0.f;
-                        // pref == 0: the attenuation factor underflowed, every term is 0
-                        if (jlo <= jhi && pref != 0.f) {
-                            // a multiple of four bins, so the loop has no tail: the
-                            // extra bins are exact terms of the full sum or the zero
-                            // pads after the last bin.  (A tail would make the
-                            // compiler rebuild the float counter from the trip count
-                            // through an int-to-float conversion, which this GPU
-                            // issues on its FP64 pipe.)
-                            jhi += (4 - ((jhi - jlo + 1) & 3)) & 3;
-                            nexp += (unsigned)(jhi - jlo + 1);
-                            // The exponent c (w - q_j)^2 as a quadratic in u = j - jc
-                            // about the bin jc nearest the centre: with
-                            // delta = w - q_jc (|delta| <= dq/2),
-                            //   c (delta - u dq)^2 = A + B u + C u^2,
-                            // A = c delta^2, B = -2 c delta dq, C = c dq^2 (dq^2
-                            // with the grid step's low part).  Near the
-                            // peak the sum is A alone; far out C u^2 dominates, so
-                            // the exponent keeps the relative accuracy of the direct
-                            // form in two FMAs per bin.
-                            const float2 q0 = fq[jlo];
-                            const float d0 = (w_hi - q0.x) + (w_lo - q0.y);
-                            const float tc = rintf(d0 * inv_dqf);
-                            const float delta = fmaf(-tc, dqf_lo, fmaf(-tc, dqf_hi, d0));
-                            const float cd = cexp * delta;
-                            const float Aq = cd * delta;
-                            const float Bq = -2.f * cd * dqf_hi;
-                            const float Cq = cexp * fmaf(dqf_hi, dqf_hi, 2.f * dqf_hi * dqf_lo);
-                            const float *Ir = Is + m * (P.nqf + 3) + jlo;
-                            const float *Iend = Ir + (jhi - jlo + 1);
-                            float acc2 = 0.f;
-                            float u = -tc;   // bin offset from jc as a float: no conversion in the loop
-                            for (; Ir < Iend; Ir += 4, u += 4.f) {
-                                const float u1 = u + 1.f, u2 = u + 2.f, u3 = u + 3.f;
-                                acc = fmaf(ex2_approx(fmaf(fmaf(Cq, u, Bq), u, Aq)), Ir[0], acc);
-                                acc2 = fmaf(ex2_approx(fmaf(fmaf(Cq, u1, Bq), u1, Aq)), Ir[1], acc2);
-                                acc = fmaf(ex2_approx(fmaf(fmaf(Cq, u2, Bq), u2, Aq)), Ir[2], acc);
-                                acc2 = fmaf(ex2_approx(fmaf(fmaf(Cq, u3, Bq), u3, Aq)), Ir[3], acc2);
-                            }
-                            acc += acc2;
+                        // Pc = exp(-(Xin + Xc)) with Xc the source-side exponent at
+                        // the outgoing energy eout = ein / eratio, formed as the
+                        // Rayleigh one plus the small Compton change, so that Pc
+                        // keeps the accuracy of PP:
+                        //   Asx (1/eout^3 - 1/ein^3) = Asx/ein^3 ((1 + x)^3 - 1)
+                        //   Asy (1/KN(eout) - 1/KN(ein))
+                        //     = Asy (ein - eout)(kn1 + kn2 (ein + eout)) / (KN(ein) KN(eout))
+                        const float eout = ein * inv_er;
+                        const float f2o = fmaf(kn2 * eout, eout, fmaf(kn1, eout, kn0));
+                        const float cube = x * fmaf(x, x + 3.f, 3.f);            // (1 + x)^3 - 1
+                        const float dX = fmaf(Asx * if1, cube,
+                                              Asy * (x * eout) * fmaf(kn2, ein + eout, kn1) * if2 * rcp_approx(f2o));
+                        const float Pc = PP * ex2_approx(-dX * kLog2e);
+                        nexp += 1;
+                        // an underflowed Pc adds exact zeros below: no branch
+                        const float Cf = eratio * eratio * (eratio + inv_er - 1.f + cos2) * 0.5f;
+                        const float base = Pc * gp * Cf * a2now * s2v;
+                        const float span = dEsf * inv_er;   // Eout2 - Eout1
+                        const float inv_span = rcp_approx(span);
+                        // this lane's (warp, energy) row of chunk sums, indexed by n;
+                        // the spectrum weight RF[e, n] is applied when the chunk is
+                        // flushed, so no two lanes ever write the same word
+                        const int wlo = wn[2 * el];
+                        float *cs = CS + ((size_t)wid * E + el) * SL - wlo;
+                        const float *oe = offse + (size_t)el * SL - wlo;
+                        const float bs = base * inv_span;
+                        float Ed1 = fmaf(fn0, dEdf, edmin);
+                        // outgoing range relative to the channel's left edge:
+                        // u1 = Eout1 - Edet1 = ((Esrc1 - Edet1) - Edet1*x)/eratio.
+                        // The range is one source bin wide over eratio >= 1, so
+                        // with dEs <= dEd it meets at most two channels: those
+                        // two straight-line, any further ones in a loop.
+                        {
+                            const float u1 = fmaf(-Ed1, x, oe[n0]) * inv_er;
+                            const float ov = fminf(u1 + span, dEdf) - fmaxf(u1, 0.f);
+                            if (ov > 0.f) cs[n0] += ov * bs;
                         }
-                        float2 k = TNw[el];
-                        kahan_add(k.x, k.y, pref * dqf_hi * acc);
-                        TNw[el] = k;
-                    }
-                    if (WITH_A) {
-                        int klo, khi;
-                        coarse_window(w_hi, half, qlo_f, c.qpar_a, c.qpar_b, P.nwt, &klo, &khi);
-                        float *tar = TA + ((size_t)(el - pe0) * P.n_mat + m) * P.nwt;
-                        nexp += (unsigned)max(0, khi - klo + 1);
-                        for (int k = klo; k <= khi; k++) {
-                            const float4 c = cq[k];
-                            const float d = (w_hi - c.x) + (w_lo - c.y);
-                            atomicAdd(tar + k, pref * c.z * ex2_approx(cexp * d * d));
-                        }
-                    }
-                    // ---- Compton, :318-356 ----
-                    {
-                        const float ein = en_ein[el];
-                        // no contraction: the Compton bin check forms eratio the same way
-                        const float x = __fmul_rn(ein, oh);       // eratio - 1
-                        const float eratio = __fadd_rn(1.f, x);
-                        const float inv_er = rcp_approx(eratio);
-                        const int eg = lo_e + el;
-                        // detector bins whose window holds e and whose channel the
-                        // outgoing range [E1, E2]/eratio can overlap
-                        const float Eo_lo = en_e1[el];
-                        // channels overlapped by [E1, E2]/eratio (an FP32 misjudgement at a
-                        // channel edge drops an overlap below 1e-6 of the bin width)
-                        float fn0;
-                        // bounded floors: n0 is raised to the window, n1 lowered to it,
-                        // and an empty range is skipped
-                        int n0 = floor_bounded((Eo_lo * inv_er - edmin) * inv_dEd, &fn0);
-                        if (n0 < wn[2 * el]) {
-                            n0 = wn[2 * el];
-                            fn0 = en_wn0f[el];
-                        }
-                        const int n1 = min(wn[2 * el + 1], floor_bounded(((Eo_lo + dEsf) * inv_er - edmin) * inv_dEd));
-                        if (n0 <= n1) {
-                            // the table's value: nearest bin, or bilinear in the table path
-                            float s2v;
-                            if (TAB == 2) {
-                                const float wC = ein * sh;
-                                const float arg = eratio + wC * wC;
-                                const float l2 = lg2_approx(wC * arg * rsqrt_approx(arg) * inv_er);
-                                s2v = table_bilinear(S2, P.nq, P.na, (l2 - qmin_t) * c.inv_dqg, ta);
-                            } else {
-                                s2v = S2[compton_bin(P, ein, eratio, inv_er, sh, oh, ol, args.T.energy[eg].ein, qmin_t,
-                                                     inv_dqt) +
-                                         na * P.nq];
-                            }
-                            // Pc = exp(-(Xin + Xc)) with Xc the source-side exponent at
-                            // the outgoing energy eout = ein / eratio, formed as the
-                            // Rayleigh one plus the small Compton change, so that Pc
-                            // keeps the accuracy of PP:
-                            //   Asx (1/eout^3 - 1/ein^3) = Asx/ein^3 ((1 + x)^3 - 1)
-                            //   Asy (1/KN(eout) - 1/KN(ein))
-                            //     = Asy (ein - eout)(kn1 + kn2 (ein + eout)) / (KN(ein) KN(eout))
-                            const float eout = ein * inv_er;
-                            const float f2o = fmaf(kn2 * eout, eout, fmaf(kn1, eout, kn0));
-                            const float cube = x * fmaf(x, x + 3.f, 3.f);            // (1 + x)^3 - 1
-                            const float dX = fmaf(Asx * if1, cube,
-                                                  Asy * (x * eout) * fmaf(kn2, ein + eout, kn1) * if2 * rcp_approx(f2o));
-                            const float Pc = PP * ex2_approx(-dX * kLog2e);
-                            nexp += 1;
-                            // an underflowed Pc adds exact zeros below: no branch
-                            const float Cf = eratio * eratio * (eratio + inv_er - 1.f + cos2) * 0.5f;
-                            const float base = Pc * gp * Cf * a2now * s2v;
-                            const float span = dEsf * inv_er;   // Eout2 - Eout1
-                            const float inv_span = rcp_approx(span);
-                            // this lane's (warp, energy) row of chunk sums, indexed by n;
-                            // the spectrum weight RF[e, n] is applied when the chunk is
-                            // flushed, so no two lanes ever write the same word
-                            const int wlo = wn[2 * el];
-                            float *cs = CS + ((size_t)wid * E + el) * SL - wlo;
-                            const float *oe = offse + (size_t)el * SL - wlo;
-                            const float bs = base * inv_span;
-                            float Ed1 = fmaf(fn0, dEdf, edmin);
-                            // outgoing range relative to the channel's left edge:
-                            // u1 = Eout1 - Edet1 = ((Esrc1 - Edet1) - Edet1*x)/eratio.
-                            // The range is one source bin wide over eratio >= 1, so
-                            // with dEs <= dEd it meets at most two channels: those
-                            // two straight-line, any further ones in a loop.
-                            {
-                                const float u1 = fmaf(-Ed1, x, oe[n0]) * inv_er;
-                                const float ov = fminf(u1 + span, dEdf) - fmaxf(u1, 0.f);
-                                if (ov > 0.f) cs[n0] += ov * bs;
-                            }
-                            if (n0 < n1) {
-                                const float Ed2 = Ed1 + dEdf;
-                                const float u1 = fmaf(-Ed2, x, oe[n0 + 1]) * inv_er;
-                                const float ov = fminf(u1 + span, dEdf) - fmaxf(u1, 0.f);
-                                if (ov > 0.f) cs[n0 + 1] += ov * bs;
-                                Ed1 = Ed2 + dEdf;
-                                for (int n = n0 + 2; n <= n1; n++, Ed1 += dEdf) {
-                                    const float u1n = fmaf(-Ed1, x, oe[n]) * inv_er;
-                                    const float ovn = fminf(u1n + span, dEdf) - fmaxf(u1n, 0.f);
-                                    if (ovn > 0.f) cs[n] += ovn * bs;
-                                }
+                        if (n0 < n1) {
+                            const float Ed2 = Ed1 + dEdf;
+                            const float u1 = fmaf(-Ed2, x, oe[n0 + 1]) * inv_er;
+                            const float ov = fminf(u1 + span, dEdf) - fmaxf(u1, 0.f);
+                            if (ov > 0.f) cs[n0 + 1] += ov * bs;
+                            Ed1 = Ed2 + dEdf;
+                            for (int n = n0 + 2; n <= n1; n++, Ed1 += dEdf) {
+                                const float u1n = fmaf(-Ed1, x, oe[n]) * inv_er;
+                                const float ovn = fminf(u1n + span, dEdf) - fmaxf(u1n, 0.f);
+                                if (ovn > 0.f) cs[n] += ovn * bs;
                             }
                         }
                     }
+                }
+            };
+            const int ne = pe1 - pe0;
+            if (ne > 32 && (ne & 31)) {
+                // a pass that is not a multiple of 32 energies (40 on the 64x64
+                // and 128x128 workloads): the chunk's (voxel, energy) items 32
+                // at a time, so that no step runs with a few lanes.  The items
+                // of a step have distinct energies (32 < ne): distinct sums
+                // TNw[el] and Compton cells, each still adding its voxels in
+                // order, so the counts are the same to the bit.
+                int i = 0, eo = lane;
+                for (int t0 = 0; t0 < nin * ne; t0 += 32) {
+                    const float2 Ad = make_float2(__shfl_sync(0xffffffffu, Adv.x, i), __shfl_sync(0xffffffffu, Adv.y, i));
+                    const float sh = __shfl_sync(0xffffffffu, vg.s.hi, i);
+                    const float sl = __shfl_sync(0xffffffffu, vg.s.lo, i);
+                    const float oh = __shfl_sync(0xffffffffu, vg.omc.hi, i);
+                    const float ol = __shfl_sync(0xffffffffu, vg.omc.lo, i);
+                    const float sg = __shfl_sync(0xffffffffu, vg.sg.hi, i);
+                    const float gp = __shfl_sync(0xffffffffu, vg.gp, i);
+                    const float Wg = __shfl_sync(0xffffffffu, vg.Wg, i);
+                    const float cos2 = __shfl_sync(0xffffffffu, vg.cos2, i);
+                    const int m = __shfl_sync(0xffffffffu, mv, i);
+                    const int na = __shfl_sync(0xffffffffu, nav, i);
+                    const float a2now = __shfl_sync(0xffffffffu, a2v, i);
+                    const float Asx = __shfl_sync(0xffffffffu, Asv.x, i);
+                    const float Asy = __shfl_sync(0xffffffffu, Asv.y, i);
+                    const float ta = TAB == 2 ? __shfl_sync(0xffffffffu, tav, i) : 0.f;
+                    const float s2f = sh * sh;
+                    const float sg_s2 = __fdividef(sg, s2f);
+                    if (i < nin) term(pe0 + eo, Ad, sh, sl, oh, ol, gp, Wg, cos2, m, na, a2now, Asx, Asy, ta, s2f, sg_s2);
+                    eo += 32;
+                    if (eo >= ne) {
+                        eo -= ne;
+                        i++;
+                    }
+                }
+            } else {
+                for (int i = 0; i < nin; i++) {
+                    const float2 Ad = make_float2(__shfl_sync(0xffffffffu, Adv.x, i), __shfl_sync(0xffffffffu, Adv.y, i));
+                    const float sh = __shfl_sync(0xffffffffu, vg.s.hi, i);
+                    const float sl = __shfl_sync(0xffffffffu, vg.s.lo, i);
+                    const float oh = __shfl_sync(0xffffffffu, vg.omc.hi, i);
+                    const float ol = __shfl_sync(0xffffffffu, vg.omc.lo, i);
+                    const float sg = __shfl_sync(0xffffffffu, vg.sg.hi, i);
+                    const float gp = __shfl_sync(0xffffffffu, vg.gp, i);
+                    const float Wg = __shfl_sync(0xffffffffu, vg.Wg, i);
+                    const float cos2 = __shfl_sync(0xffffffffu, vg.cos2, i);
+                    const int m = __shfl_sync(0xffffffffu, mv, i);
+                    const int na = __shfl_sync(0xffffffffu, nav, i);
+                    const float a2now = __shfl_sync(0xffffffffu, a2v, i);
+                    const float Asx = __shfl_sync(0xffffffffu, Asv.x, i);
+                    const float Asy = __shfl_sync(0xffffffffu, Asv.y, i);
+                    const float ta = TAB == 2 ? __shfl_sync(0xffffffffu, tav, i) : 0.f;
+                    const float s2f = sh * sh;
+                    const float sg_s2 = __fdividef(sg, s2f);
+#pragma unroll 1
+                    for (int el = pe0 + lane; el < pe1; el += 32)
+                        term(el, Ad, sh, sl, oh, ol, gp, Wg, cos2, m, na, a2now, Asx, Asy, ta, s2f, sg_s2);
                 }
             }
             // flush the chunk's Compton sums: lane = detector bin n gathers the
