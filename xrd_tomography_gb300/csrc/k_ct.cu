@@ -108,7 +108,7 @@ cudaError_t launch_ct_sinogram(const DevProblem &P, const SrcGeom *sg, const flo
 {
     const int64_t npairs = (int64_t)P.n_src * P.n_det;
     int64_t blocks = (npairs + 7) / 8;
-    if (blocks > 152 * 64) blocks = 152 * 64;
+    if (blocks > 64LL * current_sm_count()) blocks = 64LL * current_sm_count();
     k_ct_sinogram<<<(int)blocks, 256, 0, s>>>(P, sg, cells, energy, rf_win, win_lo, T, G0);
     if (launches) (*launches)++;
     return cudaGetLastError();

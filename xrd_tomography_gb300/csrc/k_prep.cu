@@ -196,6 +196,24 @@ cudaError_t launch_compact_voxels(const DevProblem &P, const int32_t *seg, PrepB
     return cudaGetLastError();
 }
 
+int current_sm_count()
+{
+    static int cached[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();   // a failed query leaves no error behind for the next launch check
+        return 152;
+    }
+    if (cached[dev] > 0) return cached[dev];
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) {
+        cudaGetLastError();
+        return 152;
+    }
+    cached[dev] = sms;
+    return sms;
+}
+
 cudaError_t launch_src_atten(const DevProblem &P, const SrcGeom *d_src, int nv, PrepBuffers &B,
                              cudaStream_t s, int64_t *launches)
 {

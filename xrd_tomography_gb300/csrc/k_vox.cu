@@ -653,10 +653,12 @@ __global__ void k_pair_table(DevProblem P, const SrcGeom *__restrict__ sg, PairR
     }
 }
 
+// a grid-stride loop over n items: at most 32 blocks per SM
 int grid_for(int64_t n, int threads)
 {
     int64_t b = (n + threads - 1) / threads;
-    if (b > 152 * 32) b = 152 * 32;
+    const int64_t cap = 32LL * current_sm_count();
+    if (b > cap) b = cap;
     return (int)(b < 1 ? 1 : b);
 }
 

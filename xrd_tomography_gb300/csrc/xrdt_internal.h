@@ -200,6 +200,10 @@ cudaError_t launch_gather_rays(const int64_t *idx, int64_t n, const float *Nc, c
                                const float *Ac, int mw, float *N, float *C, float *A, cudaStream_t s,
                                int64_t *launches);
 
+// k_prep.cu: the current device's SM count, cached per device (152 if the
+// query fails); sizes the grids of grid-stride loops.
+int current_sm_count();
+
 // k_mlem.cu: MLEM with an explicit model matrix (rows of K floats, K % 4 == 0,
 // K <= 1024); partial holds nparts rows of K floats.
 int mlem_pass_blocks(int sm_count, int K);
