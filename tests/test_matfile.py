@@ -78,6 +78,58 @@ def test_pattern_q_conversion():
     assert np.all(np.diff(qt) > 0) and 0.3 < qt[0] < qt[-1] < 6.0
 
 
+def _superblock(btree, heap, header=0):
+    """A MATLAB 7.3 header and a version-0 HDF5 superblock (8-byte offsets
+    and lengths, base address 512 as MATLAB writes it) whose root group entry
+    caches the given B-tree and heap (addresses relative to the base)."""
+    head = b"MATLAB 7.3 MAT-file".ljust(512, b" ")
+    sb = b"\x89HDF\r\n\x1a\n" + bytes([0, 0, 0, 0, 0, 8, 8, 0]) + (4).to_bytes(2, "little") \
+        + (16).to_bytes(2, "little") + bytes(4)
+    sb += (512).to_bytes(8, "little") + (2**64 - 1).to_bytes(8, "little") * 3   # base, free space, eof, driver
+    sb += bytes(8) + header.to_bytes(8, "little") + (1).to_bytes(4, "little") + bytes(4)
+    sb += btree.to_bytes(8, "little") + heap.to_bytes(8, "little")
+    return head + sb
+
+
+def test_damaged_files_raise_matfile_error(tmp_path):
+    """Damaged files end in MatFileError, not in another exception, an
+    endless recursion or a loop: a root entry that points past the end, and
+    a B-tree whose node is its own child."""
+    p = tmp_path / "past_end.mat"
+    p.write_bytes(_superblock(btree=1 << 40, heap=1 << 40))
+    with pytest.raises(MatFileError):
+        load_mat(str(p))
+
+    data = bytearray(_superblock(btree=512, heap=1536).ljust(4096, b"\0"))
+    # at file offset 1024 (address 512): an internal node (level 1) with one
+    # key and one child, itself
+    node = b"TREE" + bytes([0, 1]) + (1).to_bytes(2, "little") + bytes(16) + bytes(8) \
+        + (512).to_bytes(8, "little")
+    data[1024:1024 + len(node)] = node
+    p = tmp_path / "cycle.mat"
+    p.write_bytes(bytes(data))
+    with pytest.raises(MatFileError, match="cycle"):
+        load_mat(str(p))
+
+
+@needs_ref
+def test_truncated_reference_files_raise_matfile_error(tmp_path):
+    """Every truncation of a measured pattern file either still holds the
+    variable (the tail cut was unused) or raises MatFileError."""
+    src = os.path.join(REF, "open_source_data", "TNT.mat")
+    with open(src, "rb") as f:
+        data = f.read()
+    full = load_mat(src)["D"]
+    for frac in (0.1, 0.3, 0.5, 0.7, 0.9, 0.99):
+        p = tmp_path / f"cut{frac}.mat"
+        p.write_bytes(data[:int(len(data) * frac)])
+        try:
+            v = load_mat(str(p))
+        except MatFileError:
+            continue
+        assert np.array_equal(v["D"], full)
+
+
 def test_not_a_mat_file(tmp_path):
     p = tmp_path / "x.mat"
     p.write_bytes(b"\x89HDF\r\n\x1a\n" + bytes([3]) + bytes(100))

@@ -22,15 +22,20 @@ MATLAB stores an array of size d1 x d2 x ... as an HDF5 dataset of
 dimensions (..., d2, d1); `load_mat` returns arrays in MATLAB's shape, and
 the MATLAB_class attribute decides the element type (`char` becomes a
 string, `logical` a bool array).  Version-5 files go to scipy.io.loadmat.
+
+A damaged or truncated file raises MatFileError: reads past the end of the
+file, cycles of B-tree nodes or header continuations, arrays larger than
+MAX_ARRAY_BYTES and undecodable chunks are all reported that way.
 """
 from __future__ import annotations
 
-import struct
 import zlib
 
 import numpy as np
 
 _SIG = b"\x89HDF\r\n\x1a\n"
+MAX_ARRAY_BYTES = 1 << 34    # 16 GiB: larger arrays are taken as a damaged size field
+_MAX_DEPTH = 64              # B-tree levels and nested groups
 
 
 class MatFileError(ValueError):
@@ -63,11 +68,27 @@ class _Hdf5:
 
     # ---- little-endian helpers ----
     def _u(self, p, n):
+        if p < 0 or p + n > len(self.d):
+            raise MatFileError(f"read of {n} bytes at {p} is past the end of the file ({len(self.d)} bytes)")
         return int.from_bytes(self.d[p:p + n], "little")
 
     def _addr(self, p):
         a = self._u(p, self.so)
         return None if a == (1 << (8 * self.so)) - 1 else a + self.base
+
+    def _need(self, addr, n, what):
+        """An address that must hold n bytes of the file."""
+        if addr is None or addr < 0 or addr + n > len(self.d):
+            raise MatFileError(f"{what} at {addr} is outside the file")
+        return addr
+
+    def _nbytes(self, shape, dtype):
+        n = 1
+        for x in shape:
+            n *= int(x)
+        if n * dtype.itemsize > MAX_ARRAY_BYTES:
+            raise MatFileError(f"array of shape {tuple(shape)} is larger than {MAX_ARRAY_BYTES} bytes")
+        return n
 
     def _entry(self, p):
         name_off = self._u(p, self.so)
@@ -83,14 +104,20 @@ class _Hdf5:
     # ---- object headers ----
     def messages(self, addr):
         d = self.d
+        self._need(addr, 16, "object header")
         if d[addr] != 1:
             raise MatFileError(f"object header version {d[addr]} is not supported")
         nmsg = self._u(addr + 2, 2)
         size = self._u(addr + 8, 4)
         blocks = [(addr + 16, size)]
+        seen = set()
         out = []
         while blocks and len(out) < nmsg:
             start, length = blocks.pop(0)
+            if start in seen:
+                raise MatFileError("object header continuations form a cycle")
+            seen.add(start)
+            self._need(start, length, "object header block")
             p = start
             while p + 8 <= start + length and len(out) < nmsg:
                 mtype = self._u(p, 2)
@@ -139,7 +166,8 @@ class _Hdf5:
         q += pad(tlen)
         shape = self._dataspace(q)
         q += pad(slen)
-        n = int(np.prod(shape)) if shape else 1
+        n = self._nbytes(shape, dt) if shape else 1
+        self._need(q, n * dt.itemsize, "attribute data")
         raw = d[q:q + n * dt.itemsize]
         return name, np.frombuffer(raw, dt, n).reshape(shape) if shape else np.frombuffer(raw, dt, 1)[0]
 
@@ -165,17 +193,23 @@ class _Hdf5:
 
     # ---- groups ----
     def _heap_name(self, heap, off):
-        if self.d[heap:heap + 4] != b"HEAP":
+        if heap is None or self.d[heap:heap + 4] != b"HEAP":
             raise MatFileError("bad local heap")
-        data = self._addr(heap + 8 + 2 * self.sl)
-        end = self.d.index(b"\0", data + off)
+        data = self._need(self._addr(heap + 8 + 2 * self.sl), off + 1, "local heap data")
+        end = self.d.find(b"\0", data + off)
+        if end < 0:
+            raise MatFileError("unterminated name in a local heap")
         return self.d[data + off:end].decode("latin-1")
 
-    def _btree_children(self, addr, key_size):
+    def _btree_children(self, addr, key_size, depth=0, seen=None):
         d = self.d
-        if d[addr:addr + 4] != b"TREE":
+        seen = set() if seen is None else seen
+        if addr is None or d[addr:addr + 4] != b"TREE":
             raise MatFileError("bad B-tree node")
-        level = d[addr + 5]
+        if addr in seen or depth > _MAX_DEPTH:
+            raise MatFileError("B-tree nodes form a cycle")
+        seen.add(addr)
+        level = self._u(addr + 5, 1)
         n = self._u(addr + 6, 2)
         p = addr + 8 + 2 * self.so
         out = []
@@ -187,7 +221,7 @@ class _Hdf5:
         if level > 0:
             flat = []
             for _, child in out:
-                flat.extend(self._btree_children(child, key_size))
+                flat.extend(self._btree_children(child, key_size, depth + 1, seen))
             return flat
         return out
 
@@ -195,7 +229,7 @@ class _Hdf5:
         """Name -> object header address of a group's members."""
         members = {}
         for _, snod in self._btree_children(btree, self.sl):
-            if self.d[snod:snod + 4] != b"SNOD":
+            if snod is None or self.d[snod:snod + 4] != b"SNOD":
                 raise MatFileError("bad symbol table node")
             n = self._u(snod + 6, 2)
             for i in range(n):
@@ -232,12 +266,16 @@ class _Hdf5:
         if ver != 3:
             raise MatFileError(f"layout message version {ver} is not supported")
         cls = d[p + 1]
-        n = int(np.prod(shape)) if shape else 1
+        n = self._nbytes(shape, dtype) if shape else 1
         if cls == 0:                                    # compact
             size = self._u(p + 2, 2)
+            if size < n * dtype.itemsize:
+                raise MatFileError("compact data is shorter than its dataspace")
             raw = d[p + 4:p + 4 + size]
         elif cls == 1:                                  # contiguous
             a = self._addr(p + 2)
+            if a is not None:
+                self._need(a, n * dtype.itemsize, "contiguous data")
             raw = b"\0" * (n * dtype.itemsize) if a is None else d[a:a + n * dtype.itemsize]
         elif cls == 2:                                  # chunked
             nd = d[p + 2]
@@ -251,6 +289,10 @@ class _Hdf5:
 
     def _read_chunked(self, bt, shape, cdims, dtype, filters):
         nd = len(shape)
+        if len(cdims) != nd or any(c < 1 for c in cdims):
+            raise MatFileError("chunk dimensions do not match the dataspace")
+        self._nbytes(shape, dtype)
+        self._nbytes(cdims, dtype)
         out = np.zeros(shape, dtype)
         if bt is None:
             return out
@@ -259,7 +301,7 @@ class _Hdf5:
             csize = self._u(key, 4)
             mask = self._u(key + 4, 4)
             offs = [self._u(key + 8 + 8 * i, 8) for i in range(nd)]
-            raw = self.d[child:child + csize]
+            raw = self.d[self._need(child, csize, "chunk"):child + csize]
             for k, (fid, vals) in reversed(list(enumerate(filters))):
                 if mask & (1 << k):
                     continue
@@ -271,17 +313,21 @@ class _Hdf5:
                     raw = b.reshape(es, -1).T.tobytes()
                 else:
                     raise MatFileError(f"filter {fid} is not supported")
+            if len(raw) < int(np.prod(cdims)) * dtype.itemsize:
+                raise MatFileError("a chunk holds fewer bytes than its dimensions")
             chunk = np.frombuffer(raw, dtype, int(np.prod(cdims))).reshape(cdims)
             sl = tuple(slice(o, min(o + c, s)) for o, c, s in zip(offs, cdims, shape))
             out[sl] = chunk[tuple(slice(0, x.stop - x.start) for x in sl)]
         return out
 
 
-def _matlab_value(h5, kind, val, attrs):
+def _matlab_value(h5, kind, val, attrs, depth=0):
     cls = attrs.get("MATLAB_class")
     cls = cls.decode("latin-1") if isinstance(cls, bytes) else (str(cls) if cls is not None else None)
     if kind == "group":
-        return {name: _matlab_value(h5, *h5.read_object(addr))
+        if depth > _MAX_DEPTH:
+            raise MatFileError("groups nest deeper than the reader follows (a cycle?)")
+        return {name: _matlab_value(h5, *h5.read_object(addr), depth=depth + 1)
                 for name, addr in val.items() if not name.startswith("#")}
     if "MATLAB_empty" in attrs and int(np.asarray(attrs["MATLAB_empty"]).ravel()[0]):
         dims = tuple(int(x) for x in np.asarray(val).ravel()[::-1]) if np.size(val) else (0, 0)
@@ -305,16 +351,21 @@ def load_mat(path: str, names=None) -> dict:
         import scipy.io
         v = scipy.io.loadmat(path, variable_names=names)
         return {k: val for k, val in v.items() if not k.startswith("__")}
-    h5 = _Hdf5(data)
-    root = h5.root
-    members = h5.group(root["btree"], root["heap"]) if root["btree"] is not None \
-        else h5.read_object(root["header"])[1]
-    out = {}
-    for name, addr in members.items():
-        if name.startswith("#") or (names is not None and name not in names):
-            continue
-        out[name] = _matlab_value(h5, *h5.read_object(addr))
-    return out
+    try:
+        h5 = _Hdf5(data)
+        root = h5.root
+        members = h5.group(root["btree"], root["heap"]) if root["btree"] is not None \
+            else h5.read_object(root["header"])[1]
+        out = {}
+        for name, addr in members.items():
+            if name.startswith("#") or (names is not None and name not in names):
+                continue
+            out[name] = _matlab_value(h5, *h5.read_object(addr))
+        return out
+    except MatFileError:
+        raise
+    except (IndexError, KeyError, TypeError, ValueError, OverflowError, RecursionError, zlib.error) as e:
+        raise MatFileError(f"damaged or unsupported MAT-file {path}: {type(e).__name__}: {e}") from e
 
 
 def pattern_q(D, e_src_kev: float = 8.04, hbarc: float = 1.973269804):
