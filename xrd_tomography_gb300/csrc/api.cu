@@ -240,6 +240,7 @@ F32Consts make_f32_consts(const DevProblem &P)
     c.kn2 = (float)P.kn2;
     c.edmin = (float)P.e_det_min;
     c.inv_dEd = (float)(1.0 / P.dEd);
+    c.inv_dEs = (float)(1.0 / P.dEs);
     c.dEd = (float)P.dEd;
     c.dEs = (float)P.dEs;
     c.qmin_t = (float)P.q_min;

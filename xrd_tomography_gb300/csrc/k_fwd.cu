@@ -191,7 +191,7 @@ k_fwd(const FwdArgs args)
     const float inv_dqf = c.inv_dqf, qlo_f = c.q_lo;
     const float kn0 = c.kn0, kn1 = c.kn1, kn2 = c.kn2;
     const float edmin = c.edmin, inv_dEd = c.inv_dEd, dEdf = c.dEd;
-    const float dEsf = c.dEs;
+    const float dEsf = c.dEs, inv_dEs = c.inv_dEs;
     const float qmin_t = c.qmin_t, inv_dqt = c.inv_dqt;
     const int lo_e = P.e_lo;
     __syncthreads();
@@ -220,15 +220,21 @@ k_fwd(const FwdArgs args)
             const float2 Asv = args.atten_src[(int64_t)src * nv + v];
             const float2 Adv = walk[v];
             const float tav = TAB == 2 ? args.vox_ta[v] : 0.f;
+            // per-voxel factors, formed once here instead of once per term:
+            // the Compton weight gp a2 / 2 (the 1/2 of Cf, :347), the
+            // Rayleigh weight with 1/sqrt(2 pi), and sigma_geom / s^2
+            const float gpav = vg.gp * a2v * 0.5f;
+            const float wrv = vg.Wg * rsqrt2pi;
+            const float sgs2v = __fdividef(vg.sg.hi, vg.s.hi * vg.s.hi);
 
             const int nin = min(32, nv - chunk * 32);
             // the (voxel, source energy) term, :266-356, of voxel i of the chunk
             // (its constants as arguments) for energy el.  Labels as at
             // integrate_diffraction.cu:259-260: the detector-side integral Ad
             // feeds Pin, the source-side one (Asx, Asy) Pout.
-            auto term = [&](int el, float2 Ad, float sh, float sl, float oh, float ol, float gp, float Wg,
-                            float cos2, int m, int na, float a2now, float Asx, float Asy, float ta, float s2f,
-                            float sg_s2) {
+            auto term = [&](int el, float2 Ad, float sh, float sl, float oh, float ol, float gpa, float Wr,
+                            float Wg, float cos2, int m, int na, float a2now, float Asx, float Asy, float ta,
+                            float s2f, float sg_s2) {
                 // ---- (voxel, source energy) term, :266-356 ----
                 // attenuation exponents with 1/f1, 1/f2 as pairs: X reaches
                 // tens at the lowest energies, where FP32 constants alone
@@ -251,7 +257,7 @@ k_fwd(const FwdArgs args)
                 const float Xio = Xin + Xout;
                 const float PP = ex2_approx(-fmaf(Xio, kLog2e, Xio * kLog2e_lo));
                 nexp += 1;
-                const float pref = PP * Wg * rsqrt2pi * rs;
+                const float pref = PP * Wr * rs;
                 const float half = kSig * sig2 * rs;
                 if (WITH_N && TAB) {
                     // the coherent term from the table S1 (the reference's
@@ -382,10 +388,11 @@ k_fwd(const FwdArgs args)
                         const float Pc = PP * ex2_approx(-dX * kLog2e);
                         nexp += 1;
                         // an underflowed Pc adds exact zeros below: no branch
-                        const float Cf = eratio * eratio * (eratio + inv_er - 1.f + cos2) * 0.5f;
-                        const float base = Pc * gp * Cf * a2now * s2v;
+                        // twice Cf of :347 (gpa holds the 1/2)
+                        const float Cf2 = eratio * eratio * (eratio + inv_er - 1.f + cos2);
+                        const float base = Pc * gpa * Cf2 * s2v;
                         const float span = dEsf * inv_er;   // Eout2 - Eout1
-                        const float inv_span = rcp_approx(span);
+                        const float inv_span = eratio * inv_dEs;
                         // this lane's (warp, energy) row of chunk sums, indexed by n;
                         // the spectrum weight RF[e, n] is applied when the chunk is
                         // flushed, so no two lanes ever write the same word
@@ -434,19 +441,19 @@ k_fwd(const FwdArgs args)
                     const float sl = __shfl_sync(0xffffffffu, vg.s.lo, i);
                     const float oh = __shfl_sync(0xffffffffu, vg.omc.hi, i);
                     const float ol = __shfl_sync(0xffffffffu, vg.omc.lo, i);
-                    const float sg = __shfl_sync(0xffffffffu, vg.sg.hi, i);
-                    const float gp = __shfl_sync(0xffffffffu, vg.gp, i);
-                    const float Wg = __shfl_sync(0xffffffffu, vg.Wg, i);
+                    const float gpa = __shfl_sync(0xffffffffu, gpav, i);
+                    const float Wr = __shfl_sync(0xffffffffu, wrv, i);
+                    const float Wg = TAB ? __shfl_sync(0xffffffffu, vg.Wg, i) : 0.f;
                     const float cos2 = __shfl_sync(0xffffffffu, vg.cos2, i);
                     const int m = __shfl_sync(0xffffffffu, mv, i);
                     const int na = __shfl_sync(0xffffffffu, nav, i);
-                    const float a2now = __shfl_sync(0xffffffffu, a2v, i);
+                    const float a2now = TAB ? __shfl_sync(0xffffffffu, a2v, i) : 0.f;
                     const float Asx = __shfl_sync(0xffffffffu, Asv.x, i);
                     const float Asy = __shfl_sync(0xffffffffu, Asv.y, i);
                     const float ta = TAB == 2 ? __shfl_sync(0xffffffffu, tav, i) : 0.f;
                     const float s2f = sh * sh;
-                    const float sg_s2 = __fdividef(sg, s2f);
-                    if (i < nin) term(pe0 + eo, Ad, sh, sl, oh, ol, gp, Wg, cos2, m, na, a2now, Asx, Asy, ta, s2f, sg_s2);
+                    const float sg_s2 = __shfl_sync(0xffffffffu, sgs2v, i);
+                    if (i < nin) term(pe0 + eo, Ad, sh, sl, oh, ol, gpa, Wr, Wg, cos2, m, na, a2now, Asx, Asy, ta, s2f, sg_s2);
                     eo += 32;
                     if (eo >= ne) {
                         eo -= ne;
@@ -460,21 +467,21 @@ k_fwd(const FwdArgs args)
                     const float sl = __shfl_sync(0xffffffffu, vg.s.lo, i);
                     const float oh = __shfl_sync(0xffffffffu, vg.omc.hi, i);
                     const float ol = __shfl_sync(0xffffffffu, vg.omc.lo, i);
-                    const float sg = __shfl_sync(0xffffffffu, vg.sg.hi, i);
-                    const float gp = __shfl_sync(0xffffffffu, vg.gp, i);
-                    const float Wg = __shfl_sync(0xffffffffu, vg.Wg, i);
+                    const float gpa = __shfl_sync(0xffffffffu, gpav, i);
+                    const float Wr = __shfl_sync(0xffffffffu, wrv, i);
+                    const float Wg = TAB ? __shfl_sync(0xffffffffu, vg.Wg, i) : 0.f;
                     const float cos2 = __shfl_sync(0xffffffffu, vg.cos2, i);
                     const int m = __shfl_sync(0xffffffffu, mv, i);
                     const int na = __shfl_sync(0xffffffffu, nav, i);
-                    const float a2now = __shfl_sync(0xffffffffu, a2v, i);
+                    const float a2now = TAB ? __shfl_sync(0xffffffffu, a2v, i) : 0.f;
                     const float Asx = __shfl_sync(0xffffffffu, Asv.x, i);
                     const float Asy = __shfl_sync(0xffffffffu, Asv.y, i);
                     const float ta = TAB == 2 ? __shfl_sync(0xffffffffu, tav, i) : 0.f;
                     const float s2f = sh * sh;
-                    const float sg_s2 = __fdividef(sg, s2f);
+                    const float sg_s2 = __shfl_sync(0xffffffffu, sgs2v, i);
 #pragma unroll 1
                     for (int el = pe0 + lane; el < pe1; el += 32)
-                        term(el, Ad, sh, sl, oh, ol, gp, Wg, cos2, m, na, a2now, Asx, Asy, ta, s2f, sg_s2);
+                        term(el, Ad, sh, sl, oh, ol, gpa, Wr, Wg, cos2, m, na, a2now, Asx, Asy, ta, s2f, sg_s2);
                 }
             }
             // flush the chunk's Compton sums: lane = detector bin n gathers the

@@ -41,7 +41,7 @@ struct F32Consts {
     float vox, DQ, inv_DQ, nxf, nyf, rsqrt2pi;
     float dqf_hi, dqf_lo, inv_dqf, q_lo, q_hi;
     float kn0, kn1, kn2;
-    float edmin, inv_dEd, dEd, dEs;
+    float edmin, inv_dEd, dEd, dEs, inv_dEs;
     float qmin_t, inv_dqt, inv_dqg;
     float qpar_a, qpar_b;   // coarse bin edges: edge(n) = q_lo + qpar_b n + qpar_a n^2
 };
