@@ -82,24 +82,42 @@ def _rank_main(rank, world, port, out_dir):
     p, A, y, c, x0 = dense_problem()
     rows = shard_rays(p, *view_range(p.n_src, rank, world))
     Ar = torch.from_numpy(A[rows])
-    mlem = ShardedMLEM(lambda x: Ar @ x, lambda w: Ar.T @ w, lambda t: dist.all_reduce(t))
+    if len(rows):
+        mlem = ShardedMLEM(lambda x: Ar @ x, lambda w: Ar.T @ w, lambda t: dist.all_reduce(t))
+    else:   # more ranks than views: this rank holds none
+        mlem = ShardedMLEM(None, None, lambda t: dist.all_reduce(t))
     x = torch.from_numpy(x0.copy())
     mlem.run(torch.from_numpy(y[rows]), torch.from_numpy(c[rows]), x, 20)
     np.save(os.path.join(out_dir, f"x{rank}.npy"), x.numpy())
     dist.destroy_process_group()
 
 
-def test_two_rank_mlem_equals_one_rank(tmp_path):
+@pytest.mark.parametrize("world", [2, 5])
+def test_sharded_mlem_equals_one_rank(tmp_path, world):
+    """Two ranks of two views each; and five ranks over the tiny problem's
+    four views, the fifth without views (it adds zeros to the all-reduces)."""
     mp = pytest.importorskip("torch.multiprocessing")
     with socket.socket() as s:
         s.bind(("127.0.0.1", 0))
         port = s.getsockname()[1]
-    mp.spawn(_rank_main, args=(2, port, str(tmp_path)), nprocs=2, join=True)
-    x0r, x1r = (np.load(tmp_path / f"x{r}.npy") for r in range(2))
-    assert np.array_equal(x0r, x1r)          # every rank holds the same estimate
+    mp.spawn(_rank_main, args=(world, port, str(tmp_path)), nprocs=world, join=True)
+    xs = [np.load(tmp_path / f"x{r}.npy") for r in range(world)]
+    for xr in xs[1:]:
+        assert np.array_equal(xs[0], xr)     # every rank holds the same estimate
     p, A, y, c, x0 = dense_problem()
     ref = mlem_fp64(A, y, c, x0, 20)
-    assert np.abs(x0r - ref).max() <= 1e-10 * np.abs(ref).max()
+    assert np.abs(xs[0] - ref).max() <= 1e-10 * np.abs(ref).max()
+
+
+def test_rank_without_views():
+    p = synth.tiny_problem()
+    assert view_range(p.n_src, p.n_src, p.n_src + 1) == (p.n_src, p.n_src)
+    assert shard_rays(p, p.n_src, p.n_src).size == 0
+    with pytest.raises(ValueError):
+        view_shard_problem(p, 2, 2)
+    torch = pytest.importorskip("torch")
+    with pytest.raises(ValueError):
+        ShardedMLEM(None, None, lambda t: None).run(torch.ones(3), torch.ones(3), torch.ones(4), 1)
 
 
 @pytest.mark.gpu
