@@ -106,3 +106,55 @@ def test_python_boundary_checks_types_and_sizes():
     with pytest.raises(ValueError):
         _ptr(torch.zeros(3), np.float32, 4)
     assert _ptr(torch.zeros(4), np.float32, 4)[0] != 0
+
+
+def test_wrappers_check_sizes_before_calling_the_library():
+    """Every wrapper rejects an array shorter than the library will touch, a
+    tensor of another element type or a wrong-sized estimate with ValueError,
+    before it creates a context or calls the library (so this runs on CPU)."""
+    torch = pytest.importorskip("torch")
+    from xrd_tomography_gb300.api import Batch, BasisOperator, Operator
+    inp = synth.make_inputs(synth.tiny_problem(), 3)
+    p = inp.problem
+    nvox = p.nx * p.ny
+    f32 = lambda n: np.ones(n, np.float32)   # noqa: E731
+    with pytest.raises(ValueError):          # B is [K', N] with K' != K
+        xt.basis_expand(np.ones((8, 16), np.float32), np.ones((8, 16), np.float32))
+    with pytest.raises(ValueError):          # I shorter than M x N
+        xt.basis_expand(np.ones((8, 16), np.float32), np.ones((16, 16), np.float32), I=f32(10))
+    with pytest.raises(ValueError):
+        xt.spectrum_build(f32(5), f32(4), f32(3), f32(3), out=f32(3))
+    with pytest.raises(ValueError):
+        xt.ct_sinogram(p, inp.spectrum, f32(nvox - 1), inp.a2)
+    with pytest.raises(ValueError):
+        xt.forward_rays(p, [0], inp.spectrum, inp.Ifine, inp.seg, inp.a1, inp.a2, f32(3), 0.5, 4.0, 0.0, 1.0)
+    rays, K = 10, 8
+    with pytest.raises(ValueError):          # A shorter than rays x K
+        xt.mlem_matrix(f32(rays * K - 1), f32(rays), f32(rays), f32(K), 1)
+    with pytest.raises(ValueError):          # c shorter than y
+        xt.mlem_matrix(f32(rays * K), f32(rays), f32(rays - 1), f32(K), 1)
+    with pytest.raises(ValueError):          # estimate of another size than K
+        xt.mlem_matrix(f32(rays * K), f32(rays), f32(rays), f32(K - 1), 1, K=K)
+    with pytest.raises(ValueError):          # an FP64 tensor is never reinterpreted
+        xt.mlem_matrix(f32(rays * K), f32(rays), f32(rays), torch.ones(K, dtype=torch.float64), 1)
+    with pytest.raises(ValueError):
+        Operator(p, inp.spectrum, inp.seg[:-1], inp.a1, inp.a2)
+    op = Operator.__new__(Operator)          # sizes only: no handle behind it
+    op.p, op.h, op.ctx = p, None, None
+    n = op.unknowns
+    with pytest.raises(ValueError):
+        op.mlem(f32(p.rays), f32(p.rays), f32(n - 1), 1)
+    with pytest.raises(ValueError):
+        op.mlem(f32(p.rays - 1), f32(p.rays), f32(n), 1)
+    with pytest.raises(ValueError):
+        op.forward_rays_fp64(f32(n - 1), [0])
+    with pytest.raises(ValueError):
+        op.adjoint_rays_fp64(f32(1), [0, 1])
+    with pytest.raises(ValueError):          # the basis must be [J, NWT]
+        BasisOperator(op, np.ones((16, p.nwt + 1), np.float32))
+    b = Batch.__new__(Batch)
+    b.ops, b.h = [op], None
+    with pytest.raises(ValueError):          # one array per operator
+        b._ptrs([], "rays")
+    with pytest.raises(ValueError):          # host tensors are not batch arrays
+        b._ptrs([torch.ones(p.rays)], "rays")

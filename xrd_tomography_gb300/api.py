@@ -219,13 +219,30 @@ def _ptr(a, dtype, n=None):
     return arr.ctypes.data, arr
 
 
+def _numel(a) -> int:
+    return int(a.numel()) if hasattr(a, "numel") else int(np.size(a))
+
+
+def _estimate(x0, n, flat=True):
+    """An MLEM estimate of n elements: a torch tensor (contiguous float32,
+    updated in place by the library) or anything else, copied into a new
+    float32 array (flattened, or in x0's shape).  Returns (x, address)."""
+    if _numel(x0) != n:
+        raise ValueError(f"an estimate of {_numel(x0)} elements where {n} are needed")
+    if hasattr(x0, "data_ptr"):
+        return x0, _ptr(x0, np.float32, n)[0]
+    x = np.array(x0, dtype=np.float32, copy=True, order="C")
+    if flat:
+        x = x.reshape(-1)
+    return x, x.ctypes.data
+
+
 def forward(p: Problem, spectrum, Ifine, seg, a1, a2, S2, q_min, q_max, a_min, a_max,
             Nphotons=None, Cphotons=None, Amatrix=None, want_amatrix: bool = True,
             plain: bool = False, ctx: Context | None = None, flags: int = 0):
     """xrdt_forward.  Outputs default to new numpy arrays (host staging by
     the library); pass torch CUDA tensors to keep everything on the device.
     Returns (Nphotons, Cphotons, Amatrix-or-None) as flat arrays."""
-    ctx = ctx or default_context()
     rays = p.rays
     if Nphotons is None:
         Nphotons = np.empty(rays, np.float32)
@@ -244,6 +261,7 @@ def forward(p: Problem, spectrum, Ifine, seg, a1, a2, S2, q_min, q_max, a_min, a
         ptrs.append(pt)
         keep.append(k)
     fl = flags | (FWD_PLAIN_FP64 if plain else 0)
+    ctx = ctx or default_context()
     rc = lib().xrdt_forward(ctx.h, ctypes.byref(p), ptrs[0], ptrs[1], ptrs[2], ptrs[3], ptrs[4], ptrs[5],
                             float(q_min), float(q_max), float(a_min), float(a_max),
                             ptrs[6], ptrs[7], ptrs[8], fl)
@@ -258,7 +276,6 @@ def forward_tables(p: Problem, spectrum, seg, a1, a2, S1, S2, q_min, q_max, a_mi
     from the cross-section table S1 [NQ*NA] (nearest bins, or both tables
     bilinearly).  Returns (Nphotons, Cphotons) as flat arrays (numpy unless
     torch CUDA tensors are passed)."""
-    ctx = ctx or default_context()
     rays = p.rays
     if Nphotons is None:
         Nphotons = np.empty(rays, np.float32)
@@ -274,6 +291,7 @@ def forward_tables(p: Problem, spectrum, seg, a1, a2, S1, S2, q_min, q_max, a_mi
         ptrs.append(pt)
         keep.append(k)
     fl = flags | (TAB_BILINEAR if bilinear else 0)
+    ctx = ctx or default_context()
     rc = lib().xrdt_forward_tables(ctx.h, ctypes.byref(p), ptrs[0], ptrs[1], ptrs[2], ptrs[3], ptrs[4], ptrs[5],
                                    float(q_min), float(q_max), float(a_min), float(a_max), ptrs[6], ptrs[7], fl)
     _check(rc, ctx.h)
@@ -284,7 +302,6 @@ def forward_rays(p: Problem, rays, spectrum, Ifine, seg, a1, a2, S2, q_min, q_ma
                  want_amatrix: bool = False, plain: bool = False, ctx: Context | None = None):
     """xrdt_forward_rays: (N[n], C[n], A_rows[n, n_mat, nwt] or None) for the
     listed linear ray indices."""
-    ctx = ctx or default_context()
     rays = np.ascontiguousarray(rays, np.int64)
     n = rays.size
     N = np.empty(n, np.float32)
@@ -292,11 +309,13 @@ def forward_rays(p: Problem, rays, spectrum, Ifine, seg, a1, a2, S2, q_min, q_ma
     A = np.empty((n, p.n_mat, p.nwt), np.float32) if want_amatrix else None
     keep = []
     ptrs = []
-    for a, dt in ((spectrum, np.float32), (Ifine, np.float32), (seg, np.int32), (a1, np.float32),
-                  (a2, np.float32), (S2, np.float32)):
-        pt, k = _ptr(a, dt)
+    nvox, ntab = p.nx * p.ny, p.nq * p.na
+    for a, dt, m in ((spectrum, np.float32, p.nrg_src * p.nrg_det), (Ifine, np.float32, p.nqf * p.n_mat),
+                     (seg, np.int32, nvox), (a1, np.float32, nvox), (a2, np.float32, nvox), (S2, np.float32, ntab)):
+        pt, k = _ptr(a, dt, m)
         ptrs.append(pt)
         keep.append(k)
+    ctx = ctx or default_context()
     rc = lib().xrdt_forward_rays(ctx.h, ctypes.byref(p), *ptrs, float(q_min), float(q_max), float(a_min),
                                  float(a_max), rays.ctypes.data, n, N.ctypes.data, C.ctypes.data,
                                  A.ctypes.data if A is not None else None, FWD_PLAIN_FP64 if plain else 0)
@@ -336,15 +355,16 @@ def basis_expand(C, B, I=None, ctx: Context | None = None):
     """xrdt_basis_expand: I = C @ B in FP32 (3xTF32 on the tensor cores).
     C [M, K] and B [K, N] row-major; returns I [M, N] (numpy unless I is a
     torch CUDA tensor)."""
-    ctx = ctx or default_context()
     pc, kc = _ptr(C, np.float32)
     pb, kb = _ptr(B, np.float32)
-    shape_c = tuple(kc.shape) if hasattr(kc, "shape") else np.shape(kc)
-    M, K = int(shape_c[0]), int(shape_c[1])
+    if len(kc.shape) != 2 or len(kb.shape) != 2 or int(kb.shape[0]) != int(kc.shape[1]):
+        raise ValueError("C must be [M, K] and B [K, N]")
+    M, K = int(kc.shape[0]), int(kc.shape[1])
     N = int(kb.shape[1])
     if I is None:
         I = np.empty((M, N), np.float32)
-    pi, ki = _ptr(I, np.float32)
+    pi, ki = _ptr(I, np.float32, M * N)
+    ctx = ctx or default_context()
     _check(lib().xrdt_basis_expand(ctx.h, pc, M, K, pb, N, pi, 0), ctx.h)
     return ki
 
@@ -356,19 +376,16 @@ def spectrum_build(e_hd, n_hd, src_edges, det_edges, sigma0=0.805, sigma1=0.0125
     [H+1] in keV, photons per keV n_hd [H]) on coarse source and detector
     bins.  Returns the column-major flat [NS, ND] vector that forward()
     takes as its spectrum (numpy unless out is a torch CUDA tensor)."""
-    ctx = ctx or default_context()
-
-    def numel(a):
-        return int(a.numel()) if hasattr(a, "numel") else int(np.size(a))
-
-    ns = numel(src_edges) - 1
-    nd = numel(det_edges) - 1
-    nh = numel(n_hd)
-    if numel(e_hd) != nh + 1:
+    ns = _numel(src_edges) - 1
+    nd = _numel(det_edges) - 1
+    nh = _numel(n_hd)
+    if _numel(e_hd) != nh + 1:
         raise ValueError("e_hd must hold one more edge than n_hd has bins")
     if out is None:
         out = np.empty(ns * nd, np.float32)
-    ptrs = [_ptr(a, np.float32) for a in (e_hd, n_hd, src_edges, det_edges, out)]
+    ptrs = [_ptr(a, np.float32, m) for a, m in ((e_hd, nh + 1), (n_hd, nh), (src_edges, ns + 1),
+                                                 (det_edges, nd + 1), (out, ns * nd))]
+    ctx = ctx or default_context()
     _check(lib().xrdt_spectrum_build(ctx.h, ptrs[0][0], ptrs[1][0], nh, ptrs[2][0], ns, ptrs[3][0], nd,
                                      float(sigma0), float(sigma1), ptrs[4][0], 0), ctx.h)
     return ptrs[4][1]
@@ -377,12 +394,14 @@ def spectrum_build(e_hd, n_hd, src_edges, det_edges, sigma0=0.805, sigma1=0.0125
 def ct_sinogram(p: Problem, spectrum, a1, a2, Tphotons=None, gain0=None, ctx: Context | None = None):
     """xrdt_ct_sinogram: (Tphotons, gain0) per (source, pixel, energy bin) in
     the Nphotons layout; -log(Tphotons / gain0) is the CT sinogram."""
-    ctx = ctx or default_context()
     if Tphotons is None:
         Tphotons = np.empty(p.rays, np.float32)
     if gain0 is None:
         gain0 = np.empty(p.rays, np.float32)
-    ptrs = [_ptr(a, np.float32) for a in (spectrum, a1, a2, Tphotons, gain0)]
+    nvox = p.nx * p.ny
+    ptrs = [_ptr(a, np.float32, m) for a, m in ((spectrum, p.nrg_src * p.nrg_det), (a1, nvox), (a2, nvox),
+                                                 (Tphotons, p.rays), (gain0, p.rays))]
+    ctx = ctx or default_context()
     _check(lib().xrdt_ct_sinogram(ctx.h, ctypes.byref(p), *[q[0] for q in ptrs], 0), ctx.h)
     return ptrs[3][1], ptrs[4][1]
 
@@ -391,19 +410,14 @@ def mlem_matrix(A, y, c, x0, iters: int, K: int | None = None, ctx: Context | No
     """xrdt_mlem_matrix: MLEM of main.m:154-176 on the model matrix A
     ([rays, K] rows, the Amatrix layout).  x0 is updated in place when it is a
     torch CUDA tensor; numpy inputs return a new array."""
-    ctx = ctx or default_context()
     if K is None:
-        K = int(x0.numel() if hasattr(x0, "numel") else np.size(x0))
-    pa, ka = _ptr(A, np.float32)
+        K = _numel(x0)
+    rays = _numel(y)
+    pa, ka = _ptr(A, np.float32, rays * K)
     py, ky = _ptr(y, np.float32)
-    pc, kc = _ptr(c, np.float32)
-    if hasattr(x0, "data_ptr"):
-        x = x0
-        px = x.data_ptr()
-    else:
-        x = np.array(x0, dtype=np.float32, copy=True)
-        px = x.ctypes.data
-    rays = int(ky.numel() if hasattr(ky, "numel") else ky.size)
+    pc, kc = _ptr(c, np.float32, rays)
+    x, px = _estimate(x0, K, flat=False)
+    ctx = ctx or default_context()
     _check(lib().xrdt_mlem_matrix(ctx.h, pa, rays, K, py, pc, px, iters, 0), ctx.h)
     return x
 
@@ -457,10 +471,12 @@ class Operator:
     tensors; outputs default to new numpy arrays."""
 
     def __init__(self, p: Problem, spectrum, seg, a1, a2, ctx: Context | None = None):
+        nvox = p.nx * p.ny
+        keep = [_ptr(a, dt, m) for a, dt, m in ((spectrum, np.float32, p.nrg_src * p.nrg_det),
+                                                (seg, np.int32, nvox), (a1, np.float32, nvox),
+                                                (a2, np.float32, nvox))]
         self.ctx = ctx or default_context()
         self.p = p
-        keep = [_ptr(a, dt) for a, dt in ((spectrum, np.float32), (seg, np.int32), (a1, np.float32),
-                                          (a2, np.float32))]
         h = _vp()
         _check(lib().xrdt_op_create(self.ctx.h, ctypes.byref(p), *[k[0] for k in keep], ctypes.byref(h)),
                self.ctx.h)
@@ -513,7 +529,7 @@ class Operator:
     def forward_rays_fp64(self, x, rays):
         """(Av x)[rays] by the FP64 kernel at the reference's launch shape."""
         rays = np.ascontiguousarray(rays, np.int64)
-        px, kx = _ptr(x, np.float32)
+        px, kx = _ptr(x, np.float32, self.unknowns)
         y = np.empty(rays.size, np.float32)
         _check(lib().xrdt_op_forward_rays(self.h, px, rays.ctypes.data, rays.size, y.ctypes.data, OP_PLAIN_FP64),
                self.ctx.h)
@@ -522,7 +538,7 @@ class Operator:
     def adjoint_rays_fp64(self, w, rays):
         """sum_i w[i] Av[rays[i]] by the FP64 kernel at the reference's launch shape."""
         rays = np.ascontiguousarray(rays, np.int64)
-        pw, kw = _ptr(w, np.float32)
+        pw, kw = _ptr(w, np.float32, rays.size)
         g = np.empty(self.unknowns, np.float32)
         _check(lib().xrdt_op_adjoint_rays(self.h, pw, rays.ctypes.data, rays.size, g.ctypes.data, OP_PLAIN_FP64),
                self.ctx.h)
@@ -531,14 +547,9 @@ class Operator:
     def mlem(self, y, c, x0, iters: int):
         """iters MLEM updates from x0 (main.m:162-176 with per-voxel unknowns).
         A torch CUDA x0 is updated in place; numpy returns a new array."""
-        py, ky = _ptr(y, np.float32)
-        pc, kc = _ptr(c, np.float32)
-        if hasattr(x0, "data_ptr"):
-            x = x0
-            px = x.data_ptr()
-        else:
-            x = np.array(x0, dtype=np.float32, copy=True).reshape(-1)
-            px = x.ctypes.data
+        py, ky = _ptr(y, np.float32, self.p.rays)
+        pc, kc = _ptr(c, np.float32, self.p.rays)
+        x, px = _estimate(x0, self.unknowns)
         _check(lib().xrdt_op_mlem(self.h, py, pc, px, iters, 0), self.ctx.h)
         return x
 
@@ -553,6 +564,8 @@ class BasisOperator:
         self.op = op
         self.ctx = op.ctx
         pb, kb = _ptr(B, np.float32)
+        if len(kb.shape) != 2 or int(kb.shape[1]) != op.p.nwt:
+            raise ValueError(f"the basis must be [J, NWT = {op.p.nwt}]")
         self.J = int(kb.shape[0])
         h = _vp()
         _check(lib().xrdt_bop_create(op.h, pb, self.J, ctypes.byref(h)), self.ctx.h)
@@ -575,30 +588,25 @@ class BasisOperator:
             pass
 
     def forward(self, c, y=None):
-        pc, kc = _ptr(c, np.float32)
+        pc, kc = _ptr(c, np.float32, self.unknowns)
         if y is None:
             y = np.empty(self.op.p.rays, np.float32)
-        py, ky = _ptr(y, np.float32)
+        py, ky = _ptr(y, np.float32, self.op.p.rays)
         _check(lib().xrdt_bop_forward(self.h, pc, py, 0), self.ctx.h)
         return ky
 
     def adjoint(self, w, g=None):
-        pw, kw = _ptr(w, np.float32)
+        pw, kw = _ptr(w, np.float32, self.op.p.rays)
         if g is None:
             g = np.empty(self.unknowns, np.float32)
-        pg, kg = _ptr(g, np.float32)
+        pg, kg = _ptr(g, np.float32, self.unknowns)
         _check(lib().xrdt_bop_adjoint(self.h, pw, pg, 0), self.ctx.h)
         return kg
 
     def mlem(self, y, c, x0, iters: int):
-        py, ky = _ptr(y, np.float32)
-        pc, kc = _ptr(c, np.float32)
-        if hasattr(x0, "data_ptr"):
-            x = x0
-            px = x.data_ptr()
-        else:
-            x = np.array(x0, dtype=np.float32, copy=True).reshape(-1)
-            px = x.ctypes.data
+        py, ky = _ptr(y, np.float32, self.op.p.rays)
+        pc, kc = _ptr(c, np.float32, self.op.p.rays)
+        x, px = _estimate(x0, self.unknowns)
         _check(lib().xrdt_bop_mlem(self.h, py, pc, px, iters, 0), self.ctx.h)
         return x
 
@@ -628,23 +636,28 @@ class Batch:
         except Exception:
             pass
 
-    @staticmethod
-    def _ptrs(ts):
-        for t in ts:
-            if not hasattr(t, "data_ptr") or not t.is_cuda or not t.is_contiguous():
+    def _ptrs(self, ts, kind):
+        """One array per operator: contiguous float32 CUDA tensors of the
+        operator's ray count (kind "rays") or unknown count ("unknowns")."""
+        if len(ts) != len(self.ops):
+            raise ValueError(f"{len(ts)} arrays for {len(self.ops)} operators")
+        for t, op in zip(ts, self.ops):
+            if not hasattr(t, "data_ptr") or not t.is_cuda:
                 raise ValueError("batch arrays must be contiguous CUDA tensors")
+            _ptr(t, np.float32, op.p.rays if kind == "rays" else op.unknowns)
         return (_vp * len(ts))(*[t.data_ptr() for t in ts])
 
     def forward(self, xs, ys):
-        _check(lib().xrdt_batch_forward(self.h, self._ptrs(xs), self._ptrs(ys), 0), self.ctx.h)
+        _check(lib().xrdt_batch_forward(self.h, self._ptrs(xs, "unknowns"), self._ptrs(ys, "rays"), 0), self.ctx.h)
         return ys
 
     def adjoint(self, ws, gs):
-        _check(lib().xrdt_batch_adjoint(self.h, self._ptrs(ws), self._ptrs(gs), 0), self.ctx.h)
+        _check(lib().xrdt_batch_adjoint(self.h, self._ptrs(ws, "rays"), self._ptrs(gs, "unknowns"), 0), self.ctx.h)
         return gs
 
     def mlem(self, ys, cs, xs, iters: int):
-        _check(lib().xrdt_batch_mlem(self.h, self._ptrs(ys), self._ptrs(cs), self._ptrs(xs), iters, 0), self.ctx.h)
+        _check(lib().xrdt_batch_mlem(self.h, self._ptrs(ys, "rays"), self._ptrs(cs, "rays"),
+                                     self._ptrs(xs, "unknowns"), iters, 0), self.ctx.h)
         return xs
 
     def tune(self):
